@@ -1,0 +1,225 @@
+/*
+ * beachslope.h -- C-ABI of the GB300 (sm_103a) ISPH particle hot path.
+ *
+ * The reference (Sinchanrc/Beach-Slope, Fortran 2008 + OpenMP) exposes its
+ * per-step physics as argument-less module subroutines acting on module
+ * globals (dpcell, fmatrix, fvec, fsol, dt, h1: initialize.f90:54-69).  Those
+ * derived types hold allocatable/pointer components and are not
+ * interoperable, so this boundary replaces them with a context that owns all
+ * device state, plus plain SoA host buffers that the caller owns.
+ *
+ * Every function returns an int status: 0 = ok, negative = error class
+ * (BS_E_*).  No exception crosses the ABI, there is no global state, and a
+ * context is externally synchronised (one host thread at a time); work is
+ * ordered on the context's own CUDA stream.  A Fortran caller must call from
+ * outside `!$omp parallel` (or from `!$omp masked` followed by a barrier),
+ * because the reference's entry points are called by every thread of the
+ * enclosing parallel region (main.f90:238-261).
+ *
+ * A context holds a batch of one or more scenes.  Each scene has its own cell
+ * grid, parameters, time step and solver state; every stage runs over all
+ * scenes of the batch in one launch.
+ */
+#ifndef BEACHSLOPE_H
+#define BEACHSLOPE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define BS_OK              0
+#define BS_E_ARG          -1   /* bad argument / size                         */
+#define BS_E_CUDA         -2   /* CUDA runtime error                          */
+#define BS_E_NOMEM        -3   /* device or host allocation failed            */
+#define BS_E_CAPACITY     -4   /* particle, neighbour or cell capacity hit    */
+#define BS_E_NOTCONV      -5   /* PPE solve did not reach the tolerance       */
+#define BS_E_NONFINITE    -6   /* NaN/Inf detected in a checked field         */
+#define BS_E_DOMAIN       -7   /* particle outside the interior cell grid     */
+#define BS_E_STATE        -8   /* call order violated (e.g. solve before assemble) */
+
+/* device error-word bits (bs_error_bits) */
+#define BS_ERR_NBR_OVERFLOW    0x01u  /* neighbour list longer than kmax      */
+#define BS_ERR_ZERO_DIAG       0x02u  /* PPE row with zero diagonal (isph.f90:436) */
+#define BS_ERR_SOLVER_BREAK    0x04u  /* BiCGStab breakdown (rho or omega = 0) */
+#define BS_ERR_NOT_CONVERGED   0x08u  /* maxit reached before tolerance        */
+#define BS_ERR_NONFINITE       0x10u  /* NaN/Inf in pressure or positions      */
+#define BS_ERR_LOST_PARTICLE   0x20u  /* particle left the interior grid       */
+#define BS_ERR_ZERO_SHIFT      0x40u  /* opt2_shift with exactly zero shift (NaN, part_shift.f90:89) */
+#define BS_ERR_NO_NEIGHBOUR    0x80u  /* fluid particle with no neighbours     */
+
+/* particle type ids (particle.f90:11): 1 fixed wall, 2 ghost/dummy wall, 3 fluid */
+#define BS_TID_WALL   1
+#define BS_TID_GHOST  2
+#define BS_TID_FLUID  3
+
+/* particle flag bits (particles%free / %vicinity / %buffer, particle.f90:42-43) */
+#define BS_FLAG_FREE      0x01u
+#define BS_FLAG_VICINITY  0x02u
+#define BS_FLAG_BUFFER    0x04u
+
+/* precision modes */
+#define BS_PREC_FP64   0   /* plain FP64 drop-in                                      */
+#define BS_PREC_MIXED  1   /* FP32 sweeps/SpMV, FP64 dots, residual, refinement, positions */
+
+/* PPE stopping rules */
+#define BS_STOP_RELRES     0  /* ||b - A x||_2 / ||b||_2 <= ppe_tol                    */
+#define BS_STOP_REFERENCE  1  /* every |dx_i/(x_i+1e-5)| <= 1e-2 (solver.f90:233-242)  */
+
+/*
+ * Scene parameters.  Defaults and formulas follow initialize.f90:21-81 and
+ * setup.f90:10-150; bs_params_default() fills the reference's values.
+ */
+typedef struct bs_params {
+    /* resolution and cell grid */
+    double h;          /* smoothing length h1 (setup.f90:47)                          */
+    double dl;         /* lattice spacing dl = min particle spacing (setup.f90:53)    */
+    int32_t cellx;     /* cells in x incl. the empty border ring (setup.f90:51)       */
+    int32_t celly;     /* cells in y incl. the empty border ring (setup.f90:52)       */
+    /* time */
+    double dt;         /* time step (fixed unless adaptive_dt)                        */
+    double t0;         /* simulated time at upload                                    */
+    int32_t adaptive_dt; /* 1: timestep() rule integrator.f90:927-937 sets dt          */
+    int32_t scalar_on;   /* 1: salinity sub-steps run at the start of each step        */
+    /* fluid */
+    double rho;        /* reference density (initialize.f90:247)                      */
+    double rhomin;     /* scalar.f90:414                                              */
+    double rhomax;     /* rho*rel_den (setup.f90:19)                                  */
+    double rel_den;    /* initialize.f90:251                                          */
+    double g;          /* gravity along y (negative)                                  */
+    double mu;         /* viscosity in the timestep rule (initialize.f90:263)         */
+    double tschmidt;   /* turbulent Schmidt number (initialize.f90:249)               */
+    /* porous medium (porous.f90:111) */
+    double por;        /* grain-bed porosity                                          */
+    double lamk;       /* Ergun constant                                              */
+    double d50;        /* grain diameter                                              */
+    /* free surface and shifting */
+    double lamfs;      /* 0.8  (initialize.f90:270)                                   */
+    double maxdivr;    /* 2.0  (initialize.f90:269)                                   */
+    double csh;        /* 0.5  (initialize.f90:248)                                   */
+    double maxshift;   /* 0.1  (initialize.f90:264)                                   */
+    double sig1;       /* 0.2  CFL factor (initialize.f90:263)                        */
+    /* outflow cut-offs used by the second re-bin (integrator.f90:61-62) */
+    double xlcutoff;
+    double ytcutoff;
+    /* PPE */
+    double ppe_tol;    /* relative residual tolerance                                 */
+    int32_t ppe_maxit;
+    int32_t ppe_stop;  /* BS_STOP_*                                                   */
+    int32_t precision; /* BS_PREC_*                                                   */
+    int32_t kmax;      /* neighbour-list capacity per particle (<= 64)                */
+    /* mixed precision: inner FP32 BiCGStab tolerance per refinement sweep */
+    double mixed_inner_tol;
+    int32_t mixed_max_outer;
+    int32_t pad0;
+} bs_params;
+
+/*
+ * Host SoA view of one scene's particles.  On upload only the "state" fields
+ * are read (x..flags); on download every non-NULL pointer is filled, in the
+ * context's particle order: cell-major (column-major over cells, as resetid,
+ * isph.f90:97-108), walls first in each cell, then fluid in slot order.
+ */
+typedef struct bs_state {
+    int32_t n;
+    double *x, *y, *vx, *vy, *p, *mass, *rho, *oden, *ovol, *con;
+    int32_t *tid, *pid;
+    uint8_t *flags;
+    /* download-only per-particle fields (may be NULL) */
+    double *xs, *ys, *vxs, *vys;
+    double *porosity, *resx, *resy, *nut, *tke, *varts, *gradvx, *vel, *cdiff;
+    double *coff;      /* 4*n: L-matrix inverse (coff, search.f90:276-278)        */
+    int32_t *cell;     /* cell key (j-1)*celly + (i-1)                              */
+} bs_state;
+
+/* static grain particles of the porous bed (porlist, boundary.f90:582-585) */
+typedef struct bs_grains {
+    int32_t n;
+    double *x, *y, *mass, *rho;
+} bs_grains;
+
+/* per-scene scalars reported back to the host */
+typedef struct bs_scene_info {
+    int32_t n;            /* particles in the scene                         */
+    int32_t solsteps;     /* scalar sub-steps for the next step             */
+    int32_t ppe_iters;    /* BiCGStab iterations of the last solve          */
+    int32_t ppe_outer;    /* refinement sweeps of the last solve (mixed)    */
+    double dt, dtsol, t;  /* current step sizes and simulated time          */
+    double umax, numax;   /* timestep() maxima (integrator.f90:914-924)     */
+    double ppe_relres;    /* true FP64 relative residual of the last solve  */
+    uint32_t err_bits;    /* BS_ERR_* seen since the last bs_clear_errors   */
+    int32_t pad0;
+} bs_scene_info;
+
+/* ---- lifetime ------------------------------------------------------------- */
+void bs_params_default(bs_params* p);
+
+/* Create a context for nscenes scenes; params[s] and capacity[s] (max particles)
+ * per scene.  Replaces init/memalloc/matrixid (setup.f90:10, memory.f90:10,80). */
+int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
+              const int32_t* grain_capacity, struct bs_ctx** out);
+int bs_destroy(struct bs_ctx* ctx);
+
+/* Upload one scene's particles and grains (bins them into cells with the
+ * reference's comparison rule; walls first in a cell, then fluid). */
+int bs_upload(struct bs_ctx* ctx, int32_t scene, const bs_state* st, const bs_grains* gr);
+int bs_download(struct bs_ctx* ctx, int32_t scene, bs_state* st);
+int bs_scene_info_get(struct bs_ctx* ctx, int32_t scene, bs_scene_info* out);
+int bs_clear_errors(struct bs_ctx* ctx);
+int bs_sync(struct bs_ctx* ctx);
+const char* bs_last_error(struct bs_ctx* ctx);
+
+/* Neighbour lists for parity tests: counts[n] and idx[n*kmax] as particle
+ * indices in download order (list%nh, interactions.f90:26-35). */
+int bs_get_neighbours(struct bs_ctx* ctx, int32_t scene, int32_t* counts, int32_t* idx,
+                      double* dist, double* kx, double* ky);
+/* Assembled, Jacobi-scaled PPE rows (isph.f90:423-444): diag[n], off[n*kmax]
+ * aligned with the neighbour list, rhs[n]. */
+int bs_get_matrix(struct bs_ctx* ctx, int32_t scene, double* diag, double* off, double* rhs);
+
+/* ---- one entry point per reference subroutine ----------------------------- */
+/* Warm-up: neighbour lists, porosity, eddy viscosity and timestep maxima for
+ * the uploaded state (what the reference's spin-up leaves behind, main.f90:35-67). */
+int bs_prime(struct bs_ctx* ctx);
+int bs_scalar_substep(struct bs_ctx* ctx);  /* scalart_anisotropic+scalarupdate, scalar.f90:242,364 */
+int bs_projection(struct bs_ctx* ctx);      /* isph.f90:17                                   */
+int bs_cellshift(struct bs_ctx* ctx, int32_t alt); /* integrator.f90:251 (alt=0) / 33 (alt=1); resetid isph.f90:88 */
+int bs_search(struct bs_ctx* ctx);          /* neighbour/nsearch2, search.f90:13-399         */
+int bs_porosity(struct bs_ctx* ctx);        /* effpor/porsearch, porous.f90:32-224           */
+int bs_eddy(struct bs_ctx* ctx);            /* eddyvis, turbulence.f90:12                    */
+int bs_int_vel(struct bs_ctx* ctx);         /* int_vel, integrator.f90:459                   */
+int bs_ppe_assemble(struct bs_ctx* ctx);    /* ppesolve assembly, isph.f90:115-456           */
+int bs_ppe_solve(struct bs_ctx* ctx);       /* bicgstab (solver.f90:129) + scatter isph.f90:468 */
+int bs_comp_vel(struct bs_ctx* ctx);        /* comp_vel, integrator.f90:705                  */
+int bs_comp_pos(struct bs_ctx* ctx);        /* comp_pos, integrator.f90:845                  */
+int bs_free_surface(struct bs_ctx* ctx);    /* freesurf, isph.f90:49                         */
+int bs_shift(struct bs_ctx* ctx);           /* opt2_shift, part_shift.f90:12                 */
+int bs_density_update(struct bs_ctx* ctx);  /* densityupdate, scalar.f90:399                 */
+int bs_timestep(struct bs_ctx* ctx);        /* timestep, integrator.f90:885                  */
+
+/* Full production step (main.f90:199-272) with fused kernels, nsteps times. */
+int bs_step(struct bs_ctx* ctx, int32_t nsteps);
+
+/* Standalone BiCGStab on a CSR system (solver.f90:129-254 with the CSR
+ * operator spmv, solver.f90:53-82) -- the solvertest.f90 driver's path.
+ * Host arrays, 0-based row_ptr/col.  Returns iterations and relative residual. */
+int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                    const double* b, double* x, double tol, int32_t maxit, int32_t stop_rule,
+                    int32_t* iters, double* relres);
+
+/* ---- timing: CUDA events recorded on the context's stream ------------------ */
+int bs_event_record(struct bs_ctx* ctx, int32_t slot);
+int bs_event_elapsed_ms(struct bs_ctx* ctx, int32_t slot0, int32_t slot1, float* ms);
+/* per-kernel timing of bs_step: enable, then read {name, launches, total ms} */
+int bs_kernel_timing(struct bs_ctx* ctx, int32_t enable);
+int bs_kernel_timing_get(struct bs_ctx* ctx, int32_t idx, const char** name, int32_t* launches,
+                         double* total_ms);
+/* count of kernels launched by the library since context creation */
+int64_t bs_launch_count(struct bs_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEACHSLOPE_H */

@@ -1,0 +1,63 @@
+/*
+ * bs_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU FP64 restatement of the reference ISPH step (Sinchanrc/Beach-Slope,
+ * Fortran).  It is the parity checker for the CUDA library and the timed CPU
+ * baseline; nothing in the product links it.  Only tests/, the smoke check
+ * and bench.py's cpu_baseline / reference legs may load it.
+ *
+ * Parity status: pinned by the reference's only known-answer test
+ * (solvertest.f90:10-19, 5x5 system -> x=(1,2,3,4,5)) and by analytic
+ * identities of the kernel, inverse and porosity routines; the rest is
+ * parity against this restatement (the Fortran reference cannot be compiled
+ * here: no Fortran compiler, no MKL).
+ */
+#ifndef BS_ORACLE_H
+#define BS_ORACLE_H
+#include "../include/beachslope.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct or_scene or_scene;
+
+/* stage ids for or_stage (one per reference subroutine) */
+enum {
+    OR_PROJECTION = 1, OR_CELLSHIFT, OR_CELLSHIFTALT, OR_RESETID, OR_NEIGHBOUR,
+    OR_EFFPOR, OR_EDDYVIS, OR_INT_VEL, OR_PPE_ASSEMBLE, OR_PPE_SOLVE, OR_COMP_VEL,
+    OR_COMP_POS, OR_FREESURF, OR_OPT2_SHIFT, OR_DENSITYUPDATE, OR_TIMESTEP,
+    OR_SCALAR_SUBSTEP, OR_PRIME
+};
+
+or_scene* or_create(const bs_params* p, const bs_state* st, const bs_grains* gr);
+void or_destroy(or_scene* s);
+int or_n(or_scene* s);
+void or_set_threads(int nthreads);
+int or_get_threads(void);
+int or_get(or_scene* s, bs_state* out);
+int or_info(or_scene* s, bs_scene_info* out);
+int or_neighbours(or_scene* s, int32_t kmax, int32_t* counts, int32_t* idx,
+                  double* dist, double* kx, double* ky);
+int or_matrix(or_scene* s, int32_t kmax, double* diag, double* off, double* rhs);
+int or_stage(or_scene* s, int32_t stage);
+int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule,
+                 int32_t* iters, double* relres);
+int or_step(or_scene* s, int32_t nsteps);
+/* overwrite pressures (used to pin a common PPE guess in tests) */
+int or_set_pressure(or_scene* s, const double* p);
+int or_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                    const double* b, double* x, double tol, int32_t maxit, int32_t rule,
+                    int32_t* iters, double* relres);
+/* kernel functions for unit tests (kernel.f90:34-162, functions.f90:62-96) */
+double or_Wab(double r, double h);
+double or_Wo(double h);
+void or_gradW(double xj, double yj, double xi, double yi, double r, double h,
+              double* wx, double* wy);
+void or_invert2(double* a4);
+double or_vis(double oden);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
