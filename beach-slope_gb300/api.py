@@ -1,0 +1,218 @@
+"""Host-side context over libbeachslope.so (the C-ABI in include/beachslope.h).
+
+Mirrors the reference's per-step entry points (search, effpor, eddyvis,
+int_vel, ppesolve, comp_vel, comp_pos, freesurf, opt2_shift, densityupdate,
+timestep, scalart_anisotropic) as methods; every call goes through the
+CUDA library.  Errors from the library raise BeachSlopeError.  There is no
+CPU fallback: if the library cannot be loaded, importing this module fails.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libbeachslope.so")
+
+
+class BeachSlopeError(RuntimeError):
+    pass
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libbeachslope.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    i32 = C.c_int32
+    sig = {
+        "bs_params_default": (None, [vp]),
+        "bs_create": (C.c_int, [i32, vp, vp, vp, C.POINTER(vp)]),
+        "bs_destroy": (C.c_int, [vp]),
+        "bs_upload": (C.c_int, [vp, i32, vp, vp]),
+        "bs_download": (C.c_int, [vp, i32, vp]),
+        "bs_scene_info_get": (C.c_int, [vp, i32, vp]),
+        "bs_clear_errors": (C.c_int, [vp]),
+        "bs_sync": (C.c_int, [vp]),
+        "bs_last_error": (C.c_char_p, [vp]),
+        "bs_get_neighbours": (C.c_int, [vp, i32, vp, vp, vp, vp, vp]),
+        "bs_get_matrix": (C.c_int, [vp, i32, vp, vp, vp]),
+        "bs_prime": (C.c_int, [vp]),
+        "bs_scalar_substep": (C.c_int, [vp]),
+        "bs_projection": (C.c_int, [vp]),
+        "bs_cellshift": (C.c_int, [vp, i32]),
+        "bs_search": (C.c_int, [vp]),
+        "bs_porosity": (C.c_int, [vp]),
+        "bs_eddy": (C.c_int, [vp]),
+        "bs_int_vel": (C.c_int, [vp]),
+        "bs_ppe_assemble": (C.c_int, [vp]),
+        "bs_ppe_solve": (C.c_int, [vp]),
+        "bs_comp_vel": (C.c_int, [vp]),
+        "bs_comp_pos": (C.c_int, [vp]),
+        "bs_free_surface": (C.c_int, [vp]),
+        "bs_shift": (C.c_int, [vp]),
+        "bs_density_update": (C.c_int, [vp]),
+        "bs_timestep": (C.c_int, [vp]),
+        "bs_step": (C.c_int, [vp, i32]),
+        "bs_bicgstab_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, vp, vp]),
+        "bs_event_record": (C.c_int, [vp, i32]),
+        "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
+        "bs_kernel_timing": (C.c_int, [vp, i32]),
+        "bs_kernel_timing_get": (C.c_int, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(i32),
+                                           C.POINTER(C.c_double)]),
+        "bs_launch_count": (C.c_int64, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+lib = _load()
+
+STAGE_FUNCS = ["prime", "scalar_substep", "projection", "search", "porosity", "eddy", "int_vel",
+               "ppe_assemble", "ppe_solve", "comp_vel", "comp_pos", "free_surface", "shift",
+               "density_update", "timestep"]
+
+
+class Context:
+    """A batch of scenes resident on the GPU."""
+
+    def __init__(self, params, states, grains=None, capacity=None):
+        if not isinstance(params, (list, tuple)):
+            params, states, grains = [params], [states], [grains]
+        n = len(params)
+        if grains is None:
+            grains = [None] * n
+        self.nscenes = n
+        self.params = (abi.Params * n)(*params)
+        caps = capacity or [len(s["x"]) for s in states]
+        gcaps = [len(g["x"]) if g is not None else 0 for g in grains]
+        self._caps = (C.c_int32 * n)(*caps)
+        self._gcaps = (C.c_int32 * n)(*gcaps)
+        h = C.c_void_p()
+        rc = lib.bs_create(n, self.params, self._caps, self._gcaps, C.byref(h))
+        if rc != 0:
+            raise BeachSlopeError(f"bs_create failed ({rc})")
+        self.h = h
+        for s in range(n):
+            self.upload(s, states[s], grains[s])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.bs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib.bs_last_error(self.h)
+            raise BeachSlopeError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def upload(self, s, state, grains=None):
+        st = abi.state_in(state)
+        gr = abi.grains_in(grains) if grains is not None and len(grains["x"]) else None
+        self._check(lib.bs_upload(self.h, s, C.byref(st), C.byref(gr) if gr is not None else None), "upload")
+
+    def info(self, s=0):
+        si = abi.SceneInfo()
+        self._check(lib.bs_scene_info_get(self.h, s, C.byref(si)), "scene_info")
+        return si.as_dict()
+
+    def download(self, s=0, full=True):
+        n = self.info(s)["n"]
+        st, out = abi.state_out(n, full)
+        self._check(lib.bs_download(self.h, s, C.byref(st)), "download")
+        return out
+
+    def neighbours(self, s=0):
+        n = self.info(s)["n"]
+        K = self.params[s].kmax
+        counts = np.zeros(n, np.int32)
+        idx = np.full((n, K), -1, np.int32)
+        dist = np.zeros((n, K))
+        kx = np.zeros((n, K))
+        ky = np.zeros((n, K))
+        self._check(lib.bs_get_neighbours(self.h, s, counts.ctypes.data, idx.ctypes.data, dist.ctypes.data,
+                                          kx.ctypes.data, ky.ctypes.data), "get_neighbours")
+        return counts, idx, dist, kx, ky
+
+    def matrix(self, s=0):
+        n = self.info(s)["n"]
+        K = self.params[s].kmax
+        diag = np.zeros(n)
+        off = np.zeros((n, K))
+        rhs = np.zeros(n)
+        self._check(lib.bs_get_matrix(self.h, s, diag.ctypes.data, off.ctypes.data, rhs.ctypes.data),
+                    "get_matrix")
+        return diag, off, rhs
+
+    def stage(self, name):
+        f = getattr(lib, "bs_" + name)
+        self._check(f(self.h), name)
+
+    def cellshift(self, alt=False):
+        self._check(lib.bs_cellshift(self.h, 1 if alt else 0), "cellshift")
+
+    def step(self, n=1):
+        self._check(lib.bs_step(self.h, n), "step")
+
+    def sync(self):
+        self._check(lib.bs_sync(self.h), "sync")
+
+    def clear_errors(self):
+        self._check(lib.bs_clear_errors(self.h), "clear_errors")
+
+    def record(self, slot):
+        self._check(lib.bs_event_record(self.h, slot), "event_record")
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_float()
+        self._check(lib.bs_event_elapsed_ms(self.h, a, b, C.byref(ms)), "event_elapsed")
+        return ms.value
+
+    def kernel_timing(self, mask=1):
+        self._check(lib.bs_kernel_timing(self.h, mask), "kernel_timing")
+
+    def kernel_times(self):
+        out = {}
+        for k in range(64):
+            name = C.c_char_p()
+            cnt = C.c_int32()
+            ms = C.c_double()
+            if lib.bs_kernel_timing_get(self.h, k, C.byref(name), C.byref(cnt), C.byref(ms)) != 0:
+                break
+            if cnt.value:
+                out[name.value.decode()] = (cnt.value, ms.value)
+        return out
+
+    def launch_count(self):
+        return int(lib.bs_launch_count(self.h))
+
+
+for _name in STAGE_FUNCS:
+    def _mk(nm):
+        def f(self):
+            self.stage(nm)
+        f.__name__ = nm
+        return f
+    setattr(Context, _name, _mk(_name))
+
+
+def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=abi.STOP_RELRES):
+    """solvertest.f90's path: BiCGStab on a host CSR system, solved on the GPU."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    it = C.c_int32()
+    rr = C.c_double()
+    rc = lib.bs_bicgstab_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data, b.ctypes.data,
+                             x.ctypes.data, tol, maxit, rule, C.byref(it), C.byref(rr))
+    return rc, x, it.value, rr.value

@@ -1,0 +1,364 @@
+// bs_bin.cu -- cell re-binning by counting sort (cellshift / cellshiftalt /
+// resetid, integrator.f90:33-392, isph.f90:88-113), plus projection,
+// per-cell maxima and the timestep rule.
+//
+// The reference moves each fluid particle to one of its cell's 8 neighbours
+// by half-open comparisons against the cell bounds and rebuilds every cell's
+// list as [walls][stayers in slot order][arrivals from (i+1,j), (i-1,j),
+// (i,j+1), (i,j-1), (i-1,j-1), (i+1,j-1), (i-1,j+1), (i+1,j+1), each in the
+// source cell's slot order].  That order is a stable sort by the key
+// (destination cell, arrival category) over rows that are already sorted by
+// source cell, so a counting sort over BS_NCAT buckets per cell reproduces
+// it exactly:  k_rank (one warp per source cell: codes + ballot ranks +
+// bucket counts) -> k_cell_prefix (per cell: prefix over its buckets) ->
+// k_scan_cells (per scene: exclusive scan of cell totals) -> k_permute.
+#include "bs_internal.cuh"
+
+namespace {
+
+// arrival category = code; destination key offset for each code
+// 0 wall, 1 stay, 2 moved north (tn, to i-1), 3 south (ts, i+1), 4 west (tw,
+// j-1), 5 east (te, j+1), 6 south-east (tse, i+1,j+1), 7 north-east (tne,
+// i-1,j+1), 8 south-west (tsw, i+1,j-1), 9 north-west (tnw, i-1,j-1), 10 lost
+__device__ __forceinline__ void code_di_dj(int code, int& di, int& dj) {
+    const int tdi[10] = {0, 0, -1, 1, 0, 0, 1, -1, 1, -1};
+    const int tdj[10] = {0, 0, 0, 0, -1, 1, 1, 1, -1, -1};
+    di = tdi[code];
+    dj = tdj[code];
+}
+
+__device__ __forceinline__ int classify(const ScenePar& P, int i, int j, double x1, double y1) {
+    const double xl = cell_xleft(P, j), xr = cell_xright(P, j);
+    const double yb = cell_ybot(P, i), yt = cell_ytop(P, i);
+    if ((x1 >= xl) && (x1 < xr)) {
+        if ((y1 >= yb) && (y1 < yt)) return 1;
+        if (y1 < yb) return 3;
+        if (y1 >= yt) return 2;
+    } else if (x1 >= xr) {
+        if (y1 >= yt) return 7;
+        if ((y1 >= yb) && (y1 < yt)) return 5;
+        if (y1 < yb) return 6;
+    } else if (x1 < xl) {
+        if (y1 >= yt) return 9;
+        if ((y1 >= yb) && (y1 < yt)) return 4;
+        if (y1 < yb) return 8;
+    }
+    return 10;
+}
+
+// projection, isph.f90:17-47: x = x + (dt*vx/porosity), written without FMA
+__device__ __forceinline__ double project(double x, double dt, double v, double por) {
+    return __dadd_rn(x, __ddiv_rn(__dmul_rn(dt, v), por));
+}
+
+__global__ void k_rank(Dev D, int projection, int cutoff) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= D.ncell_total) return;
+    const int c = warp;
+    const int s = D.cell_scene[c];
+    const ScenePar& P = D.par[s];
+    const int lc = c - P.cell0;
+    const int i = lc % P.celly + 1, j = lc / P.celly + 1;
+    const int r0 = D.cell_start[c], r1 = D.cell_end[c];
+    int cnt[11];
+#pragma unroll
+    for (int d = 0; d < 11; ++d) cnt[d] = 0;
+    const double dt = D.dyn[s].dt;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int base = r0; base < r1; base += 32) {
+        const int r = base + lane;
+        int code = 11;   // inactive lane
+        if (r < r1) {
+            if (D.tid[r] != BS_TID_FLUID) {
+                code = 0;
+            } else {
+                double x1 = D.x[r], y1 = D.y[r];
+                if (projection) {
+                    const double por = D.por[r];
+                    x1 = project(x1, dt, D.vx[r], por);
+                    y1 = project(y1, dt, D.vy[r], por);
+                }
+                code = classify(P, i, j, x1, y1);
+                if (cutoff && code != 10) {   // integrator.f90:61-62
+                    const bool buf = D.flags[r] & BS_FLAG_BUFFER;
+                    const bool keep = (x1 > P.xlcutoff) || buf || ((x1 <= P.xlcutoff) && (y1 <= P.ytcutoff));
+                    if (!keep) code = 10;
+                }
+                if (code >= 2 && code <= 9) {   // destination must be an interior cell
+                    int di, dj;
+                    code_di_dj(code, di, dj);
+                    const int ii = i + di, jj = j + dj;
+                    if (ii < 2 || ii > P.celly - 1 || jj < 2 || jj > P.cellx - 1) code = 10;
+                }
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 11; ++d) {
+            const unsigned m = __ballot_sync(0xffffffffu, code == d);
+            if (code == d) D.coderank[r] = (d << 24) | (cnt[d] + __popc(m & lt));
+            cnt[d] += __popc(m);
+        }
+    }
+    if (lane < 10) {
+        int di, dj;
+        code_di_dj(lane, di, dj);
+        const int ii = i + di, jj = j + dj;
+        if (ii >= 2 && ii <= P.celly - 1 && jj >= 2 && jj <= P.cellx - 1) {
+            int v = 0;
+#pragma unroll
+            for (int d = 0; d < 10; ++d)
+                if (d == lane) v = cnt[d];
+            if (v) D.bucket[(long)(c + di + dj * P.celly) * BS_NCAT + lane] = v;
+        }
+    }
+    if (lane == 0 && cnt[10] > 0) {
+        atomicAdd(&D.dyn[s].lost, cnt[10]);
+        if (!cutoff) set_err(D, s, BS_ERR_LOST_PARTICLE);
+    }
+}
+
+__global__ void k_cell_prefix(Dev D) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= D.ncell_total) return;
+    int* b = D.bucket + (long)c * BS_NCAT;
+    int acc = 0;
+#pragma unroll
+    for (int d = 0; d < BS_NCAT; ++d) {
+        const int v = b[d];
+        b[d] = acc;
+        acc += v;
+    }
+    D.cell_total[c] = acc;
+}
+
+// one block per scene: exclusive scan of the scene's cell totals
+__global__ void k_scan_cells(Dev D) {
+    const int s = blockIdx.x;
+    const ScenePar& P = D.par[s];
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int nb = blockDim.x;
+    for (int base = 0; base < P.ncell; base += nb) {
+        const int q = base + threadIdx.x;
+        const int v = (q < P.ncell) ? D.cell_total[P.cell0 + q] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < nb; o <<= 1) {   // Hillis-Steele inclusive scan
+            const int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (q < P.ncell) {
+            const int st = P.row0 + carry + sh[threadIdx.x] - v;
+            D.cell_start2[P.cell0 + q] = st;
+            D.cell_end2[P.cell0 + q] = st + v;
+        }
+        __syncthreads();
+        if (threadIdx.x == nb - 1) carry += sh[nb - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        D.dyn[s].n_prev = D.dyn[s].n;
+        D.dyn[s].n = carry;
+    }
+}
+
+__global__ void k_permute(Dev D, int projection) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[blockIdx.x];
+    const ScenePar& P = D.par[s];
+    if (r >= P.row0 + D.dyn[s].n_prev) return;
+    const int cr = D.coderank[r];
+    const int code = cr >> 24, rank = cr & 0xffffff;
+    if (code >= 10) return;
+    const int c = D.cell[r];
+    int di, dj;
+    code_di_dj(code, di, dj);
+    const int dc = c + di + dj * P.celly;
+    const int dr = D.cell_start2[dc] + D.bucket[(long)dc * BS_NCAT + code] + rank;
+    double x = D.x[r], y = D.y[r], xs = D.xs[r], ys = D.ys[r];
+    if (projection && D.tid[r] == BS_TID_FLUID) {
+        const double dt = D.dyn[s].dt, por = D.por[r];
+        xs = x;
+        ys = y;
+        x = project(x, dt, D.vx[r], por);
+        y = project(y, dt, D.vy[r], por);
+    }
+    D.x2[dr] = x; D.y2[dr] = y; D.xs2[dr] = xs; D.ys2[dr] = ys;
+    D.vx2[dr] = D.vx[r]; D.vy2[dr] = D.vy[r]; D.vxs2[dr] = D.vxs[r]; D.vys2[dr] = D.vys[r];
+    D.p2[dr] = D.p[r]; D.mass2[dr] = D.mass[r]; D.rho2[dr] = D.rho[r]; D.oden2[dr] = D.oden[r];
+    D.ovol2[dr] = D.ovol[r]; D.con2[dr] = D.con[r]; D.vol2[dr] = D.vol[r]; D.nu2[dr] = D.nu[r];
+    D.tid2[dr] = D.tid[r]; D.flags2[dr] = D.flags[r]; D.pid2[dr] = D.pid[r]; D.cell2[dr] = dc;
+}
+
+// projection alone (isph.f90:17-47), for the per-stage entry point
+__global__ void k_projection(Dev D) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[blockIdx.x];
+    const ScenePar& P = D.par[s];
+    if (r >= P.row0 + D.dyn[s].n || D.tid[r] != BS_TID_FLUID) return;
+    const double dt = D.dyn[s].dt, por = D.por[r];
+    const double x = D.x[r], y = D.y[r];
+    D.xs[r] = x;
+    D.ys[r] = y;
+    D.x[r] = project(x, dt, D.vx[r], por);
+    D.y[r] = project(y, dt, D.vy[r], por);
+}
+
+// Per-cell maxima of |vel| and |nut| (integrator.f90:831-841; an empty cell
+// keeps its old values) and the timestep rule (integrator.f90:885-953).
+// One thread per cell; per-scene finisher = last block of the scene.
+__global__ void k_cellmax(Dev D, int do_cellmax) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= D.ncell_total || !do_cellmax) return;
+    const int r0 = D.cell_start[c], r1 = D.cell_end[c];
+    if (r1 > r0) {
+        double mv = 0.0, me = 0.0;
+        for (int r = r0; r < r1; ++r) {
+            mv = fmax(mv, fabs(D.vel[r]));
+            me = fmax(me, fabs(D.nut[r]));
+        }
+        D.cell_maxvel[c] = mv;
+        D.cell_maxeddy[c] = me;
+    }
+}
+
+// one block per scene
+__global__ void k_timestep(Dev D) {
+    const int s = blockIdx.x;
+    const ScenePar& P = D.par[s];
+    __shared__ double sh[2 * 32];
+    double v[2] = {0.0, 0.0};
+    for (int q = threadIdx.x; q < P.ncell; q += blockDim.x) {
+        const int lc = q;
+        const int i = lc % P.celly + 1, j = lc / P.celly + 1;
+        if (i < 2 || i > P.celly - 1 || j < 2 || j > P.cellx - 1) continue;
+        v[0] = fmax(v[0], D.cell_maxvel[P.cell0 + q]);
+        v[1] = fmax(v[1], D.cell_maxeddy[P.cell0 + q]);
+    }
+    block_max<2>(v, sh);
+    if (threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        const double umax = v[0];
+        double numax = v[1];
+        Y.umax = umax;
+        const double sig1 = P.sig1, dl = P.dl, mu = P.mu, rho = P.rho, t = Y.t;
+        double dt = Y.dt;
+        if (P.adaptive_dt) {
+            if (t <= 1.0)
+                dt = fmin(fmin(sig1 * (dl) / umax, sig1 * ((dl) * (dl)) / ((mu / rho) + numax)), 0.0010);
+            else if ((t > 1.0) && (t <= 2.50))
+                dt = (double)fminf(fminf((float)(sig1 * (dl) / umax), (float)(sig1 * ((dl) * (dl)) * rho / mu)), 0.002f);
+            else if ((t > 3.0) && (t <= 4.0))
+                dt = (double)fminf(fminf((float)(sig1 * (dl) / umax), (float)(sig1 * ((dl) * (dl)) * rho / mu)), 0.004f);
+            else
+                dt = fmin(fmin(sig1 * (dl) / umax, sig1 * ((dl) * (dl)) / ((mu / rho) + numax)), 0.0050);
+            Y.dt = dt;
+        }
+        if (!isfinite(numax)) numax = 0.0;
+        Y.numax = numax;
+        double dtsol = sig1 * (dl * dl) / (BS_SP1EM9 + numax / P.tschmidt);
+        int solsteps = 1;
+        if (dtsol < dt) {
+            solsteps = (int)ceil(dt / dtsol);
+            dtsol = dt / solsteps;
+        }
+        dtsol = (dtsol < dt) ? dtsol : dt;
+        Y.dtsol = dtsol;
+        Y.solsteps = solsteps;
+    }
+}
+
+__global__ void k_advance_time(Dev D) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < D.nscene) D.dyn[s].t = D.dyn[s].t + D.dyn[s].dt;
+}
+
+// derived per-particle fields after upload / density update
+__global__ void k_derive(Dev D) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[blockIdx.x];
+    const ScenePar& P = D.par[s];
+    if (r >= P.row0 + D.dyn[s].n) return;
+    D.vol[r] = D.mass[r] / D.rho[r];
+    const double od = D.oden[r];
+    D.nu[r] = (D.tid[r] == BS_TID_FLUID) ? bs_vis(od) / od : 0.0;
+}
+
+inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace
+
+namespace bs {
+
+void rebin(const Dev& D, const Launch& L, int projection, int cutoff) {
+    cudaMemsetAsync(D.bucket, 0, sizeof(int) * (size_t)D.ncell_total * BS_NCAT, L.stream);
+    int q = tbegin(L, K_RANK);
+    k_rank<<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D, projection, cutoff);
+    tend(L, q);
+    q = tbegin(L, K_CELLPREFIX);
+    k_cell_prefix<<<gdiv(D.ncell_total, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
+    tend(L, q);
+    q = tbegin(L, K_SCANCELLS);
+    k_scan_cells<<<D.nscene, 1024, 0, L.stream>>>(D);
+    tend(L, q);
+    q = tbegin(L, K_PERMUTE);
+    k_permute<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, projection);
+    tend(L, q);
+}
+
+void projection_only(const Dev& D, const Launch& L) {
+    const int q = tbegin(L, K_PROJECTION);
+    k_projection<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    tend(L, q);
+}
+
+void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_timestep) {
+    if (do_cellmax) {
+        const int q = tbegin(L, K_CELLMAX);
+        k_cellmax<<<gdiv(D.ncell_total, BS_THREADS), BS_THREADS, 0, L.stream>>>(D, 1);
+        tend(L, q);
+    }
+    if (do_timestep) {
+        const int q = tbegin(L, K_TIMESTEP);
+        k_timestep<<<D.nscene, BS_THREADS, 0, L.stream>>>(D);
+        tend(L, q);
+    }
+}
+
+void advance_time(const Dev& D, const Launch& L) {
+    const int q = tbegin(L, K_ADVANCE);
+    k_advance_time<<<gdiv(D.nscene, 64), 64, 0, L.stream>>>(D);
+    tend(L, q);
+}
+
+void derive_fields(const Dev& D, const Launch& L) {
+    const int q = tbegin(L, K_DERIVE);
+    k_derive<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    tend(L, q);
+}
+
+const char* const kernel_names[K_COUNT] = {
+    "rank", "cell_prefix", "scan_cells", "permute", "search_effpor", "freesurf", "eddy", "int_vel",
+    "assemble", "comp_vel_pos", "cell_max", "timestep", "shift", "apply_density", "disp", "scalar",
+    "bicg_init", "bicg_it1_spmv", "bicg_it2_spmv", "bicg_it3_axpy", "true_residual", "advance_time",
+    "derive", "velmag", "projection", "mx_init", "mx_it1_spmv", "mx_it2_spmv", "mx_it3_axpy",
+    "mx_residual", "mx_convert"};
+
+void timer_collect(KTimer* T) {
+    if (!T || !T->ready) return;
+    for (int q = 0; q < T->used; ++q) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, T->ev[2 * q], T->ev[2 * q + 1]) == cudaSuccess) {
+            T->total_ms[T->id_of[q]] += ms;
+            T->count[T->id_of[q]] += 1;
+        }
+    }
+    T->used = 0;
+}
+
+}  // namespace bs

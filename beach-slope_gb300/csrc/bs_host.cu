@@ -1,0 +1,833 @@
+// bs_host.cu -- the C-ABI (include/beachslope.h): context lifetime, upload /
+// download, one entry point per reference subroutine and the fused step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bs_internal.cuh"
+
+namespace bs {
+void projection_only(const Dev& D, const Launch& L);
+void disp(const Dev& D, const Launch& L);
+void velmag(const Dev& D, const Launch& L);
+}  // namespace bs
+
+struct bs_ctx {
+    int nscene = 0;
+    std::vector<bs_params> prm;
+    std::vector<ScenePar> hpar;
+    int nrow_total = 0, nblk_total = 0, ncell_total = 0, kmax = 0, ngrain_total = 0;
+    int precision = 0;
+    std::vector<int> grain0, gcap;
+    Dev D{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[16] = {};
+    cudaEvent_t evsync = nullptr;
+    int64_t launches = 0;
+    std::string err;
+    int* h_pinned = nullptr;   // [0] converged counter, [1..] solsteps per scene
+    int* d_nconv = nullptr;
+    std::vector<void*> allocs;
+    bool assembled = false;
+    bool disp_ready = false;
+    int max_solsteps = 1;
+    bs::KTimer timer;
+};
+
+namespace {
+
+int fail(bs_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return fail(ctx, BS_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(bs_ctx* ctx, T** p, size_t n) {
+    void* q = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) return fail(ctx, BS_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    cudaMemset(q, 0, n * sizeof(T));
+    ctx->allocs.push_back(q);
+    *p = (T*)q;
+    return 0;
+}
+
+bs::Launch launch_of(bs_ctx* c) {
+    bs::Launch L;
+    L.stream = c->stream;
+    L.nblk_rows = c->nblk_total;
+    L.ncell_total = c->ncell_total;
+    L.launches = &c->launches;
+    L.timer = &c->timer;
+    return L;
+}
+
+// cell bounds as setup.f90:120-123
+double xleft_of(const bs_params& p, int j) { return (double)(j - 2) * (4.0 * p.h); }
+double xright_of(const bs_params& p, int j) { return (double)(j - 1) * (4.0 * p.h); }
+double ybot_of(const bs_params& p, int i) { return (double)(-i + p.celly - 1) * (4.0 * p.h); }
+double ytop_of(const bs_params& p, int i) { return (double)(-i + p.celly) * (4.0 * p.h); }
+
+bool locate(const bs_params& p, double x, double y, int* ci, int* cj) {
+    if (!std::isfinite(x) || !std::isfinite(y)) return false;
+    const double cw = 4.0 * p.h;
+    int j = (int)std::floor(x / cw) + 2;
+    j = std::max(1, std::min(p.cellx, j));
+    for (int it = 0; it < 4; ++it) {
+        if (x < xleft_of(p, j) && j > 1) --j;
+        else if (!(x < xright_of(p, j)) && j < p.cellx) ++j;
+        else break;
+    }
+    int i = p.celly - 1 - (int)std::floor(y / cw);
+    i = std::max(1, std::min(p.celly, i));
+    for (int it = 0; it < 4; ++it) {
+        if (y < ybot_of(p, i) && i < p.celly) ++i;
+        else if (!(y < ytop_of(p, i)) && i > 1) --i;
+        else break;
+    }
+    if (!(x >= xleft_of(p, j) && x < xright_of(p, j) && y >= ybot_of(p, i) && y < ytop_of(p, i))) return false;
+    if (i < 2 || i > p.celly - 1 || j < 2 || j > p.cellx - 1) return false;
+    *ci = i;
+    *cj = j;
+    return true;
+}
+
+void swap_particles(Dev& D) {
+    std::swap(D.x, D.x2); std::swap(D.y, D.y2); std::swap(D.xs, D.xs2); std::swap(D.ys, D.ys2);
+    std::swap(D.vx, D.vx2); std::swap(D.vy, D.vy2); std::swap(D.vxs, D.vxs2); std::swap(D.vys, D.vys2);
+    std::swap(D.p, D.p2); std::swap(D.mass, D.mass2); std::swap(D.rho, D.rho2); std::swap(D.oden, D.oden2);
+    std::swap(D.ovol, D.ovol2); std::swap(D.con, D.con2); std::swap(D.vol, D.vol2); std::swap(D.nu, D.nu2);
+    std::swap(D.tid, D.tid2); std::swap(D.flags, D.flags2); std::swap(D.pid, D.pid2); std::swap(D.cell, D.cell2);
+    std::swap(D.cell_start, D.cell_start2);
+    std::swap(D.cell_end, D.cell_end2);
+}
+
+int read_solsteps(bs_ctx* ctx) {
+    Dev& D = ctx->D;
+    CK(cudaMemcpy2DAsync(ctx->h_pinned + 1, sizeof(int), &D.dyn[0].solsteps, sizeof(SceneDyn), sizeof(int),
+                         ctx->nscene, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int mx = 1;
+    for (int s = 0; s < ctx->nscene; ++s) mx = std::max(mx, ctx->h_pinned[1 + s]);
+    ctx->max_solsteps = mx;
+    bs::timer_collect(&ctx->timer);
+    return 0;
+}
+
+int check_launch(bs_ctx* ctx) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, BS_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+// stage helpers (no sync)
+void st_rebin(bs_ctx* c, int projection, int cutoff) {
+    bs::rebin(c->D, launch_of(c), projection, cutoff);
+    swap_particles(c->D);
+}
+void st_search(bs_ctx* c, int do_search, int do_effpor) {
+    bs::search(c->D, launch_of(c), c->precision, do_search, do_effpor);
+    if (do_effpor) {
+        std::swap(c->D.rho, c->D.rho_new);
+        std::swap(c->D.vol, c->D.vol_new);
+    }
+}
+void st_scalar(bs_ctx* c, int substep) {
+    bs::scalar(c->D, launch_of(c), c->precision, substep);
+    std::swap(c->D.con, c->D.con_new);
+}
+int st_solve(bs_ctx* c) {
+    bs::Launch L = launch_of(c);
+    int maxit = 0;
+    for (auto& p : c->prm) maxit = std::max(maxit, (int)p.ppe_maxit);
+    if (c->precision == BS_PREC_MIXED)
+        bs::solve_mixed(c->D, L, maxit, 8, c->d_nconv, c->h_pinned, c->evsync);
+    else
+        bs::solve_fp64(c->D, L, maxit, 8, nullptr, c->d_nconv, c->h_pinned, c->evsync);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bs_params_default(bs_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->h = 0.013; p->dl = 0.01; p->dt = 1e-4; p->scalar_on = 1;
+    p->rho = 1000.0; p->rhomin = 1000.0; p->rel_den = 1.025; p->rhomax = p->rho * p->rel_den;
+    p->g = -9.81; p->mu = 0.001; p->tschmidt = 1.0;
+    p->por = 0.38; p->lamk = 600.0; p->d50 = 0.00102;
+    p->lamfs = 0.80; p->maxdivr = 2.0; p->csh = 0.50; p->maxshift = 0.1; p->sig1 = 0.20;
+    p->xlcutoff = -1e300; p->ytcutoff = 1e300;
+    p->ppe_tol = 1e-8; p->ppe_maxit = 5000; p->ppe_stop = BS_STOP_RELRES; p->precision = BS_PREC_FP64;
+    p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 30;
+}
+
+int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity, const int32_t* grain_capacity,
+              bs_ctx** out) {
+    if (nscenes <= 0 || !params || !capacity || !out) return BS_E_ARG;
+    bs_ctx* ctx = new bs_ctx();
+    ctx->nscene = nscenes;
+    ctx->prm.assign(params, params + nscenes);
+    ctx->precision = params[0].precision;
+    ctx->kmax = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        if (params[s].precision != ctx->precision) { delete ctx; return BS_E_ARG; }
+        if (params[s].cellx < 4 || params[s].celly < 4 || params[s].h <= 0) { delete ctx; return BS_E_ARG; }
+        ctx->kmax = std::max(ctx->kmax, (int)params[s].kmax);
+    }
+    if (ctx->kmax <= 0 || ctx->kmax > 64) { delete ctx; return BS_E_ARG; }
+    // layout
+    int row = 0, blk = 0, cell = 0, gr = 0;
+    std::vector<int> blk_scene, cell_scene;
+    ctx->hpar.resize(nscenes);
+    for (int s = 0; s < nscenes; ++s) {
+        const bs_params& p = params[s];
+        ScenePar& P = ctx->hpar[s];
+        std::memset(&P, 0, sizeof(P));
+        const int cap = ((std::max(capacity[s], 1) + BS_ALIGN - 1) / BS_ALIGN) * BS_ALIGN;
+        P.h = p.h; P.twoh = 2.0 * p.h; P.lam = 0.0010 * (p.h * p.h); P.dl = p.dl; P.cw = 4.0 * p.h;
+        P.inv_h = 1.0 / p.h; P.inv_h2 = 1.0 / (p.h * p.h); P.inv_h3 = 1.0 / (p.h * p.h * p.h);
+        P.cn1 = 0.1 * (10.0 / (BS_C28 * (p.h * p.h)));
+        P.cn2 = (1.0 - 0.1) * (1.0 / (BS_C3 * (p.h * p.h)));
+        P.wo = 0.1 * 4.0 * (10.0 / (BS_C28 * (p.h * p.h))) + (1.0 - 0.1) * 6.0 * (1.0 / (BS_C3 * (p.h * p.h)));
+        P.rho = p.rho; P.rhomin = p.rhomin; P.rhomax = p.rhomax; P.rel_den = p.rel_den; P.g = p.g;
+        P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
+        P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;
+        P.xlcutoff = p.xlcutoff; P.ytcutoff = p.ytcutoff; P.ppe_tol = p.ppe_tol; P.inner_tol = p.mixed_inner_tol;
+        P.cellx = p.cellx; P.celly = p.celly; P.ncell = p.cellx * p.celly; P.cell0 = cell;
+        P.row0 = row; P.cap = cap; P.kmax = ctx->kmax; P.maxit = p.ppe_maxit;
+        P.adaptive_dt = p.adaptive_dt; P.scalar_on = p.scalar_on; P.precision = p.precision; P.stop_rule = p.ppe_stop;
+        P.nblk = cap / BS_THREADS; P.blk0 = blk; P.max_outer = p.mixed_max_outer;
+        for (int b = 0; b < P.nblk; ++b) blk_scene.push_back(s);
+        for (int q = 0; q < P.ncell; ++q) cell_scene.push_back(s);
+        row += cap;
+        blk += P.nblk;
+        cell += P.ncell;
+        ctx->grain0.push_back(gr);
+        const int gc = grain_capacity ? std::max(grain_capacity[s], 0) : 0;
+        ctx->gcap.push_back(gc);
+        gr += gc;
+    }
+    ctx->nrow_total = row;
+    ctx->nblk_total = blk;
+    ctx->ncell_total = cell;
+    ctx->ngrain_total = gr;
+    Dev& D = ctx->D;
+    const size_t R = row, E = (size_t)row * ctx->kmax, C = cell;
+    int rc = 0;
+#define A(ptr, n) if (!rc) rc = dalloc(ctx, &D.ptr, n)
+    A(x, R); A(y, R); A(xs, R); A(ys, R); A(vx, R); A(vy, R); A(vxs, R); A(vys, R); A(p, R);
+    A(mass, R); A(rho, R); A(oden, R); A(ovol, R); A(con, R); A(vol, R); A(nu, R);
+    A(tid, R); A(flags, R); A(pid, R); A(cell, R);
+    A(x2, R); A(y2, R); A(xs2, R); A(ys2, R); A(vx2, R); A(vy2, R); A(vxs2, R); A(vys2, R); A(p2, R);
+    A(mass2, R); A(rho2, R); A(oden2, R); A(ovol2, R); A(con2, R); A(vol2, R); A(nu2, R);
+    A(tid2, R); A(flags2, R); A(pid2, R); A(cell2, R);
+    A(por, R); A(resx, R); A(resy, R); A(nut, R); A(tke, R); A(varts, R); A(gradvx, R); A(vel, R); A(cdiff, R);
+    A(c0, R); A(c1, R); A(c2, R); A(c3, R); A(Dp0, R); A(Dp1, R); A(Dp2, R); A(Dp3, R); A(Dt, R);
+    A(rho_new, R); A(vol_new, R); A(con_new, R);
+    A(ncount, R); A(nidx, E);
+    A(adiag, R); A(rhs, R);
+    A(sr, R); A(srhat, R); A(sp, R); A(sp2, R); A(sv, R); A(sv2, R); A(ss, R); A(st, R); A(sxd, R);
+    A(cell_start, C); A(cell_end, C); A(cell_start2, C); A(cell_end2, C);
+    A(bucket, C * BS_NCAT); A(cell_total, C); A(coderank, R);
+    A(cell_maxvel, C); A(cell_maxeddy, C);
+    A(gx, (size_t)gr); A(gy, (size_t)gr); A(gv, (size_t)gr); A(gcell_start, C); A(gcell_end, C);
+    A(part, (size_t)blk * BS_MAXDOT);
+    A(err_word, 1);
+#undef A
+    const size_t pw = (ctx->precision == BS_PREC_MIXED) ? sizeof(float) : sizeof(double);
+    if (!rc) {
+        double* tmp;
+        rc = dalloc(ctx, &tmp, E);
+        D.aval = tmp;
+    }
+    char* bytes[4];
+    for (int q = 0; q < 4 && !rc; ++q) rc = dalloc(ctx, &bytes[q], E * pw);
+    if (!rc) { D.ndist = bytes[0]; D.nrinv = bytes[1]; D.nkx = bytes[2]; D.nky = bytes[3]; }
+    if (ctx->precision == BS_PREC_MIXED && !rc) {
+        float* f;
+        rc = dalloc(ctx, &f, E);
+        D.aval_lo = f;
+        float** fv[] = {&D.fr, &D.fp, &D.fp2, &D.fv, &D.fv2, &D.fs, &D.ft, &D.fd, &D.frhat};
+        for (auto q : fv)
+            if (!rc) rc = dalloc(ctx, q, R);
+    }
+    ScenePar* dpar = nullptr;
+    SceneDyn* ddyn = nullptr;
+    int *dbs = nullptr, *dcs = nullptr, *dbd = nullptr;
+    if (!rc) rc = dalloc(ctx, &dpar, nscenes);
+    if (!rc) rc = dalloc(ctx, &ddyn, nscenes);
+    if (!rc) rc = dalloc(ctx, &dbs, blk);
+    if (!rc) rc = dalloc(ctx, &dcs, cell);
+    if (!rc) rc = dalloc(ctx, &dbd, nscenes);
+    if (!rc) rc = dalloc(ctx, &ctx->d_nconv, 1);
+    if (rc) {
+        int r2 = rc;
+        bs_destroy(ctx);
+        return r2;
+    }
+    cudaMemcpy(dpar, ctx->hpar.data(), sizeof(ScenePar) * nscenes, cudaMemcpyHostToDevice);
+    cudaMemcpy(dbs, blk_scene.data(), sizeof(int) * blk, cudaMemcpyHostToDevice);
+    cudaMemcpy(dcs, cell_scene.data(), sizeof(int) * cell, cudaMemcpyHostToDevice);
+    std::vector<SceneDyn> hd(nscenes);
+    for (int s = 0; s < nscenes; ++s) {
+        std::memset(&hd[s], 0, sizeof(SceneDyn));
+        hd[s].dt = params[s].dt;
+        hd[s].t = params[s].t0;
+        hd[s].dtsol = params[s].dt;
+        hd[s].solsteps = 1;
+    }
+    cudaMemcpy(ddyn, hd.data(), sizeof(SceneDyn) * nscenes, cudaMemcpyHostToDevice);
+    D.par = dpar;
+    D.dyn = ddyn;
+    D.blk_scene = dbs;
+    D.cell_scene = dcs;
+    D.blk_done = dbd;
+    D.ncell_total = cell;
+    D.nrow_total = row;
+    D.nblk_total = blk;
+    D.nscene = nscenes;
+    D.kmax = ctx->kmax;
+    cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (auto& e : ctx->ev) cudaEventCreate(&e);
+    cudaEventCreateWithFlags(&ctx->evsync, cudaEventDisableTiming);
+    cudaMallocHost(&ctx->h_pinned, sizeof(int) * (nscenes + 4));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        bs_destroy(ctx);
+        return BS_E_CUDA;
+    }
+    *out = ctx;
+    return BS_OK;
+}
+
+int bs_destroy(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void* q : ctx->allocs) cudaFree(q);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->evsync) cudaEventDestroy(ctx->evsync);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->timer.ready)
+        for (auto& e : ctx->timer.ev) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BS_OK;
+}
+
+const char* bs_last_error(bs_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !st) return BS_E_ARG;
+    const bs_params& p = ctx->prm[s];
+    const ScenePar& P = ctx->hpar[s];
+    const int n = st->n;
+    if (n > P.cap) return fail(ctx, BS_E_CAPACITY, "scene larger than its capacity");
+    // bin: (cell key, walls first, input order) -- boundary.f90:140-190, internal.f90:73-95
+    std::vector<long long> key(n);
+    for (int q = 0; q < n; ++q) {
+        int ci, cj;
+        if (!locate(p, st->x[q], st->y[q], &ci, &cj)) return fail(ctx, BS_E_DOMAIN, "particle outside the interior cell grid");
+        const long long k = (long long)(cj - 1) * p.celly + (ci - 1);
+        key[q] = (k << 33) | ((long long)(st->tid[q] == BS_TID_FLUID ? 1 : 0) << 32) | q;
+    }
+    std::vector<int> ord(n);
+    for (int q = 0; q < n; ++q) ord[q] = q;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return key[a] < key[b]; });
+    std::vector<double> f64[16];
+    const double* src[] = {st->x, st->y, st->vx, st->vy, st->p, st->mass, st->rho, st->oden, st->ovol, st->con};
+    for (int f = 0; f < 10; ++f) {
+        f64[f].resize(n);
+        for (int q = 0; q < n; ++q) f64[f][q] = src[f][ord[q]];
+    }
+    std::vector<int8_t> tid(n);
+    std::vector<uint8_t> flags(n);
+    std::vector<int> pid(n), cellv(n);
+    std::vector<int> cstart(P.ncell, 0), cend(P.ncell, 0);
+    for (int q = 0; q < n; ++q) {
+        tid[q] = (int8_t)st->tid[ord[q]];
+        flags[q] = st->flags ? st->flags[ord[q]] : 0;
+        pid[q] = st->pid ? st->pid[ord[q]] : ord[q] + 1;
+        cellv[q] = (int)(key[ord[q]] >> 33) + P.cell0;
+    }
+    {   // cell ranges (empty cells: start == end, ranges stay monotone)
+        std::vector<int> cnt(P.ncell, 0);
+        for (int q = 0; q < n; ++q) cnt[cellv[q] - P.cell0]++;
+        int acc = P.row0;
+        for (int c = 0; c < P.ncell; ++c) {
+            cstart[c] = acc;
+            acc += cnt[c];
+            cend[c] = acc;
+        }
+    }
+    Dev& D = ctx->D;
+    const size_t off = P.row0;
+    double* dst[] = {D.x, D.y, D.vx, D.vy, D.p, D.mass, D.rho, D.oden, D.ovol, D.con};
+    for (int f = 0; f < 10; ++f) CK(cudaMemcpy(dst[f] + off, f64[f].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    std::vector<double> zero(n, 0.0);
+    CK(cudaMemcpy(D.xs + off, f64[0].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.ys + off, f64[1].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.vxs + off, zero.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.vys + off, zero.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    std::vector<double> one(n, 1.0);
+    CK(cudaMemcpy(D.por + off, one.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.tid + off, tid.data(), n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.flags + off, flags.data(), n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.pid + off, pid.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.cell + off, cellv.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.cell_start + P.cell0, cstart.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.cell_end + P.cell0, cend.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    // grains: sorted by cell
+    const int ng = gr ? gr->n : 0;
+    if (ng > ctx->gcap[s]) return fail(ctx, BS_E_CAPACITY, "more grains than the grain capacity");
+    {
+        std::vector<std::pair<int, int>> gk;
+        for (int q = 0; q < ng; ++q) {
+            int ci, cj;
+            if (!locate(p, gr->x[q], gr->y[q], &ci, &cj)) continue;
+            gk.push_back({(cj - 1) * p.celly + (ci - 1), q});
+        }
+        std::stable_sort(gk.begin(), gk.end());
+        const int m = (int)gk.size();
+        std::vector<double> gx(m), gy(m), gv(m);
+        std::vector<int> gs(P.ncell, 0), ge(P.ncell, 0), cnt(P.ncell, 0);
+        for (int q = 0; q < m; ++q) {
+            const int k = gk[q].second;
+            gx[q] = gr->x[k];
+            gy[q] = gr->y[k];
+            gv[q] = gr->mass[k] / gr->rho[k];
+            cnt[gk[q].first]++;
+        }
+        int acc = ctx->grain0[s];
+        for (int c = 0; c < P.ncell; ++c) {
+            gs[c] = acc;
+            acc += cnt[c];
+            ge[c] = acc;
+        }
+        const int g0 = ctx->grain0[s];
+        if (m) {
+            CK(cudaMemcpy(D.gx + g0, gx.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(D.gy + g0, gy.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(D.gv + g0, gv.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(D.gcell_start + P.cell0, gs.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(D.gcell_end + P.cell0, ge.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    }
+    SceneDyn hd;
+    std::memset(&hd, 0, sizeof(hd));
+    hd.n = n;
+    hd.t = p.t0;
+    hd.dt = p.dt;
+    hd.dtsol = p.dt;
+    hd.solsteps = 1;
+    CK(cudaMemcpy(D.dyn + s, &hd, sizeof(hd), cudaMemcpyHostToDevice));
+    bs::derive_fields(D, launch_of(ctx));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->assembled = false;
+    return check_launch(ctx);
+}
+
+int bs_download(bs_ctx* ctx, int32_t s, bs_state* o) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !o) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    const int n = hd.n;
+    if (o->n < n) return fail(ctx, BS_E_CAPACITY, "download buffer too small");
+    o->n = n;
+    const size_t off = ctx->hpar[s].row0;
+    Dev& D = ctx->D;
+    auto get = [&](double* dst, const double* src) -> int {
+        if (!dst) return 0;
+        cudaError_t e = cudaMemcpy(dst, src + off, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        return e == cudaSuccess ? 0 : BS_E_CUDA;
+    };
+    int rc = 0;
+    rc |= get(o->x, D.x); rc |= get(o->y, D.y); rc |= get(o->vx, D.vx); rc |= get(o->vy, D.vy);
+    rc |= get(o->p, D.p); rc |= get(o->mass, D.mass); rc |= get(o->rho, D.rho); rc |= get(o->oden, D.oden);
+    rc |= get(o->ovol, D.ovol); rc |= get(o->con, D.con); rc |= get(o->xs, D.xs); rc |= get(o->ys, D.ys);
+    rc |= get(o->vxs, D.vxs); rc |= get(o->vys, D.vys); rc |= get(o->porosity, D.por); rc |= get(o->resx, D.resx);
+    rc |= get(o->resy, D.resy); rc |= get(o->nut, D.nut); rc |= get(o->tke, D.tke); rc |= get(o->varts, D.varts);
+    rc |= get(o->gradvx, D.gradvx); rc |= get(o->vel, D.vel); rc |= get(o->cdiff, D.cdiff);
+    if (rc) return fail(ctx, BS_E_CUDA, "download copy failed");
+    if (o->tid) {
+        std::vector<int8_t> t(n);
+        CK(cudaMemcpy(t.data(), D.tid + off, n, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < n; ++q) o->tid[q] = t[q];
+    }
+    if (o->flags) CK(cudaMemcpy(o->flags, D.flags + off, n, cudaMemcpyDeviceToHost));
+    if (o->pid) CK(cudaMemcpy(o->pid, D.pid + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (o->cell) {
+        CK(cudaMemcpy(o->cell, D.cell + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < n; ++q) o->cell[q] -= ctx->hpar[s].cell0;
+    }
+    if (o->coff) {
+        std::vector<double> c[4];
+        double* src[4] = {D.c0, D.c1, D.c2, D.c3};
+        for (int k = 0; k < 4; ++k) {
+            c[k].resize(n);
+            CK(cudaMemcpy(c[k].data(), src[k] + off, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        }
+        for (int q = 0; q < n; ++q)
+            for (int k = 0; k < 4; ++k) o->coff[4 * q + k] = c[k][q];
+    }
+    return 0;
+}
+
+int bs_scene_info_get(bs_ctx* ctx, int32_t s, bs_scene_info* o) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !o) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    std::memset(o, 0, sizeof(*o));
+    o->n = hd.n;
+    o->solsteps = hd.solsteps;
+    o->ppe_iters = hd.iters;
+    o->ppe_outer = hd.outer;
+    o->dt = hd.dt;
+    o->dtsol = hd.dtsol;
+    o->t = hd.t;
+    o->umax = hd.umax;
+    o->numax = hd.numax;
+    o->ppe_relres = hd.relres;
+    o->err_bits = hd.err;
+    return 0;
+}
+
+int bs_clear_errors(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::vector<SceneDyn> hd(ctx->nscene);
+    CK(cudaMemcpy(hd.data(), ctx->D.dyn, sizeof(SceneDyn) * ctx->nscene, cudaMemcpyDeviceToHost));
+    for (auto& d : hd) d.err = 0;
+    CK(cudaMemcpy(ctx->D.dyn, hd.data(), sizeof(SceneDyn) * ctx->nscene, cudaMemcpyHostToDevice));
+    CK(cudaMemset(ctx->D.err_word, 0, sizeof(unsigned)));
+    return 0;
+}
+
+int bs_sync(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return check_launch(ctx);
+}
+
+int bs_get_neighbours(bs_ctx* ctx, int32_t s, int32_t* counts, int32_t* idx, double* dist, double* kx, double* ky) {
+    if (!ctx || s < 0 || s >= ctx->nscene) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    const ScenePar& P = ctx->hpar[s];
+    const int n = hd.n, K = ctx->kmax;
+    const size_t e0 = (size_t)P.row0 * K, ne = (size_t)P.cap * K;
+    std::vector<int> cnt(n), id(ne);
+    CK(cudaMemcpy(cnt.data(), ctx->D.ncount + P.row0, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(id.data(), ctx->D.nidx + e0, sizeof(int) * ne, cudaMemcpyDeviceToHost));
+    const bool mixed = ctx->precision == BS_PREC_MIXED;
+    std::vector<double> vals[3];
+    void* srcs[3] = {ctx->D.ndist, ctx->D.nkx, ctx->D.nky};
+    double* outs[3] = {dist, kx, ky};
+    for (int q = 0; q < 3; ++q) {
+        if (!outs[q]) continue;
+        vals[q].resize(ne);
+        if (mixed) {
+            std::vector<float> f(ne);
+            CK(cudaMemcpy(f.data(), (float*)srcs[q] + e0, sizeof(float) * ne, cudaMemcpyDeviceToHost));
+            for (size_t e = 0; e < ne; ++e) vals[q][e] = f[e];
+        } else {
+            CK(cudaMemcpy(vals[q].data(), (double*)srcs[q] + e0, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+        }
+    }
+    for (int r = 0; r < n; ++r) {
+        if (counts) counts[r] = cnt[r];
+        for (int k = 0; k < cnt[r]; ++k) {
+            const size_t e = ((size_t)(r >> 5) * K + k) * 32 + (r & 31);
+            const size_t o = (size_t)r * K + k;
+            if (idx) idx[o] = id[e] - P.row0;
+            for (int q = 0; q < 3; ++q)
+                if (outs[q]) outs[q][o] = vals[q][e];
+        }
+    }
+    return 0;
+}
+
+int bs_get_matrix(bs_ctx* ctx, int32_t s, double* diag, double* off, double* rhs) {
+    if (!ctx || s < 0 || s >= ctx->nscene) return BS_E_ARG;
+    if (!ctx->assembled) return fail(ctx, BS_E_STATE, "matrix not assembled");
+    CK(cudaStreamSynchronize(ctx->stream));
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    const ScenePar& P = ctx->hpar[s];
+    const int n = hd.n, K = ctx->kmax;
+    if (diag) CK(cudaMemcpy(diag, ctx->D.adiag + P.row0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (rhs) CK(cudaMemcpy(rhs, ctx->D.rhs + P.row0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (off) {
+        const size_t e0 = (size_t)P.row0 * K, ne = (size_t)P.cap * K;
+        std::vector<double> v(ne);
+        std::vector<int> cnt(n);
+        CK(cudaMemcpy(v.data(), (double*)ctx->D.aval + e0, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cnt.data(), ctx->D.ncount + P.row0, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        for (int r = 0; r < n; ++r)
+            for (int k = 0; k < cnt[r]; ++k) off[(size_t)r * K + k] = v[((size_t)(r >> 5) * K + k) * 32 + (r & 31)];
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------ stages
+int bs_prime(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::Launch L = launch_of(ctx);
+    st_search(ctx, 1, 1);
+    bs::eddy(ctx->D, L, ctx->precision, 0, 0);
+    bs::velmag(ctx->D, L);
+    bs::cell_max_timestep(ctx->D, L, 1, 1);
+    bs::disp(ctx->D, L);
+    ctx->disp_ready = true;
+    int rc = check_launch(ctx);
+    if (rc) return rc;
+    return read_solsteps(ctx);
+}
+
+int bs_scalar_substep(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::disp(ctx->D, launch_of(ctx));
+    st_scalar(ctx, 0);
+    return check_launch(ctx);
+}
+int bs_projection(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::projection_only(ctx->D, launch_of(ctx));
+    return check_launch(ctx);
+}
+int bs_cellshift(bs_ctx* ctx, int32_t alt) {
+    if (!ctx) return BS_E_ARG;
+    st_rebin(ctx, 0, alt ? 1 : 0);
+    return check_launch(ctx);
+}
+int bs_search(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    st_search(ctx, 1, 0);
+    return check_launch(ctx);
+}
+int bs_porosity(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    st_search(ctx, 0, 1);
+    return check_launch(ctx);
+}
+int bs_eddy(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 0, 0);
+    return check_launch(ctx);
+}
+int bs_int_vel(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 1, 0);   // varts (integrator.f90:468-507)
+    bs::int_vel(ctx->D, launch_of(ctx), ctx->precision);
+    return check_launch(ctx);
+}
+int bs_ppe_assemble(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::assemble(ctx->D, launch_of(ctx), ctx->precision);
+    ctx->assembled = true;
+    return check_launch(ctx);
+}
+int bs_ppe_solve(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    if (!ctx->assembled) return fail(ctx, BS_E_STATE, "solve before assemble");
+    st_solve(ctx);
+    int rc = bs_sync(ctx);
+    if (rc) return rc;
+    unsigned e = 0;
+    CK(cudaMemcpy(&e, ctx->D.err_word, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (e & BS_ERR_NOT_CONVERGED) return fail(ctx, BS_E_NOTCONV, "PPE solve did not converge");
+    return 0;
+}
+int bs_comp_vel(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::comp_vel(ctx->D, launch_of(ctx), ctx->precision, 1, 0);
+    bs::cell_max_timestep(ctx->D, launch_of(ctx), 1, 0);
+    return check_launch(ctx);
+}
+int bs_comp_pos(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::comp_vel(ctx->D, launch_of(ctx), ctx->precision, 0, 1);
+    return check_launch(ctx);
+}
+int bs_free_surface(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::freesurf(ctx->D, launch_of(ctx));
+    return check_launch(ctx);
+}
+int bs_shift(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::shift(ctx->D, launch_of(ctx), ctx->precision);
+    bs::apply_density(ctx->D, launch_of(ctx), 1, 0);
+    return check_launch(ctx);
+}
+int bs_density_update(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::apply_density(ctx->D, launch_of(ctx), 0, 1);
+    return check_launch(ctx);
+}
+int bs_timestep(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::cell_max_timestep(ctx->D, launch_of(ctx), 0, 1);
+    return check_launch(ctx);
+}
+
+// Full production step, main.f90:199-272 (open-boundary buffers excluded).
+int bs_step(bs_ctx* ctx, int32_t nsteps) {
+    if (!ctx || nsteps < 0) return BS_E_ARG;
+    Dev& D = ctx->D;
+    for (int it = 0; it < nsteps; ++it) {
+        bs::Launch L = launch_of(ctx);
+        bs::advance_time(D, L);
+        bool any_scalar = false;
+        for (auto& p : ctx->prm) any_scalar |= p.scalar_on != 0;
+        if (any_scalar) {
+            if (!ctx->disp_ready) {
+                bs::disp(D, L);
+                ctx->disp_ready = true;
+            }
+            // solsteps of the previous timestep() (read back at the end of the last step)
+            for (int j1 = 0; j1 < ctx->max_solsteps; ++j1) st_scalar(ctx, j1);
+        }
+        st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
+        st_search(ctx, 1, 1);                // neighbour + effpor
+        bs::eddy(D, L, ctx->precision, 1, 0);  // eddyvis (+ varts of int_vel)
+        bs::int_vel(D, L, ctx->precision);
+        bs::assemble(D, L, ctx->precision);
+        ctx->assembled = true;
+        st_solve(ctx);                       // bicgstab + pressure scatter
+        bs::comp_vel(D, L, ctx->precision, 1, 1);   // comp_vel + comp_pos
+        bs::cell_max_timestep(D, L, 1, 0);
+        st_rebin(ctx, 0, 1);                 // cellshiftalt
+        st_search(ctx, 1, 1);                // neighbour + effpor
+        bs::freesurf(D, L);
+        bs::shift(D, L, ctx->precision);     // opt2_shift
+        bs::apply_density(D, L, 1, 1);       // shift apply + densityupdate
+        bs::cell_max_timestep(D, L, 0, 1);   // timestep
+        bs::eddy(D, L, ctx->precision, 0, 1);  // eddyvis (+ dispersion for the next scalar)
+        ctx->disp_ready = true;
+        int rc = check_launch(ctx);
+        if (rc) return rc;
+        rc = read_solsteps(ctx);   // next step's scalar sub-step count
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+// Stand-alone BiCGStab on a host CSR system: the system becomes a one-scene
+// context (diagonal entries summed into adiag, the rest in the sliced ELL).
+int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val, const double* b,
+                    double* x, double tol, int32_t maxit, int32_t stop_rule, int32_t* iters, double* relres) {
+    if (n <= 0 || !row_ptr || !col || !val || !b || !x) return BS_E_ARG;
+    int kmax = 1;
+    for (int r = 0; r < n; ++r) {
+        int m = 0;
+        for (int e = row_ptr[r]; e < row_ptr[r + 1]; ++e)
+            if (col[e] != r) ++m;
+        kmax = std::max(kmax, m);
+    }
+    if (kmax > 64) return BS_E_CAPACITY;
+    bs_params p;
+    bs_params_default(&p);
+    p.cellx = p.celly = 4;
+    p.kmax = kmax;
+    p.ppe_tol = tol;
+    p.ppe_maxit = maxit;
+    p.ppe_stop = stop_rule;
+    bs_ctx* ctx = nullptr;
+    int rc = bs_create(1, &p, &n, nullptr, &ctx);
+    if (rc) return rc;
+    const ScenePar& P = ctx->hpar[0];
+    const size_t E = (size_t)P.cap * kmax;
+    std::vector<double> diag(n, 0.0), aval(E, 0.0);
+    std::vector<int> idx(E, 0), cnt(n, 0);
+    for (int r = 0; r < n; ++r)
+        for (int e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
+            if (col[e] == r) { diag[r] += val[e]; continue; }
+            const size_t q = ((size_t)(r >> 5) * kmax + cnt[r]) * 32 + (r & 31);
+            idx[q] = col[e];
+            aval[q] = val[e];
+            cnt[r]++;
+        }
+    Dev& D = ctx->D;
+    SceneDyn hd;
+    std::memset(&hd, 0, sizeof(hd));
+    hd.n = n;
+    CK(cudaMemcpy(D.dyn, &hd, sizeof(hd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.adiag, diag.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.rhs, b, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.p, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.ncount, cnt.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.nidx, idx.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.aval, aval.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+    ctx->assembled = true;
+    bs::solve_fp64(D, launch_of(ctx), maxit, 1, nullptr, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
+    rc = bs_sync(ctx);
+    if (!rc) {
+        CK(cudaMemcpy(x, D.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&hd, D.dyn, sizeof(hd), cudaMemcpyDeviceToHost));
+        if (iters) *iters = hd.iters;
+        if (relres) *relres = hd.relres;
+        if (hd.err & BS_ERR_NOT_CONVERGED) rc = BS_E_NOTCONV;
+    }
+    bs_destroy(ctx);
+    return rc;
+}
+
+int bs_event_record(bs_ctx* ctx, int32_t slot) {
+    if (!ctx || slot < 0 || slot >= 16) return BS_E_ARG;
+    CK(cudaEventRecord(ctx->ev[slot], ctx->stream));
+    return 0;
+}
+int bs_event_elapsed_ms(bs_ctx* ctx, int32_t a, int32_t b, float* ms) {
+    if (!ctx || a < 0 || a >= 16 || b < 0 || b >= 16 || !ms) return BS_E_ARG;
+    CK(cudaEventSynchronize(ctx->ev[b]));
+    CK(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+    return 0;
+}
+// enable: bit mask of kernel ids to bracket with events (0 disables); resets totals
+int bs_kernel_timing(bs_ctx* ctx, int32_t enable) {
+    if (!ctx) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    bs::KTimer& T = ctx->timer;
+    if (!T.ready && enable) {
+        for (int q = 0; q < bs::KTimer::NEV; ++q) CK(cudaEventCreate(&T.ev[q]));
+        T.ready = true;
+    }
+    bs::timer_collect(&T);
+    T.mask = enable == 1 ? ~0ull : (unsigned long long)(uint32_t)enable;
+    if (!enable) T.mask = 0;
+    for (int k = 0; k < bs::K_COUNT; ++k) {
+        T.total_ms[k] = 0.0;
+        T.count[k] = 0;
+    }
+    return 0;
+}
+int bs_kernel_timing_get(bs_ctx* ctx, int32_t idx, const char** name, int32_t* launches, double* total_ms) {
+    if (!ctx || idx < 0 || idx >= bs::K_COUNT) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    bs::timer_collect(&ctx->timer);
+    if (name) *name = bs::kernel_names[idx];
+    if (launches) *launches = (int32_t)ctx->timer.count[idx];
+    if (total_ms) *total_ms = ctx->timer.total_ms[idx];
+    return 0;
+}
+int64_t bs_launch_count(bs_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

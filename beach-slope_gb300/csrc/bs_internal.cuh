@@ -1,0 +1,280 @@
+// bs_internal.cuh -- device data layout and shared device helpers.
+//
+// Layout in HBM (one context = a batch of scenes):
+//  * particle rows: SoA arrays over all scenes; scene s owns rows
+//    [row0[s], row0[s] + cap[s]), cap a multiple of BS_ALIGN so that a
+//    256-thread block never straddles two scenes; rows beyond n[s] are idle.
+//    Inside a scene rows are kept sorted by cell key (column-major over
+//    cells, as resetid numbers them, isph.f90:97-108), walls first in a
+//    cell, then fluid in the reference's slot order (integrator.f90:319-387).
+//  * neighbour lists: sliced ELL, slice = 32 rows, kmax entries per row,
+//    element (row,k) at ((row/32)*kmax + k)*32 + row%32, so a warp reading
+//    the k-th neighbour of its 32 rows issues one coalesced request.
+//  * PPE matrix: values aligned with the neighbour list (the list is the
+//    column array), a per-row diagonal (1 after Jacobi scaling except the
+//    reference's leftover-entry rows), right-hand side.
+//  * cells: per-scene grids concatenated; cell_start/cell_end rows.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/beachslope.h"
+
+#define BS_ALIGN 256
+#define BS_THREADS 256
+#define BS_NCAT 10      // bucket categories per cell in the re-bin (see k_rank)
+#define BS_MAXDOT 8     // partial sums per block in the solver
+
+// constants with the reference's literal precision (default REAL = single)
+#define BS_C28 ((double)(28.0f * 3.14f))   // kernel.f90:61
+#define BS_C3 ((double)(3.0f * 3.14f))     // kernel.f90:62
+#define BS_SP1EM5 ((double)1e-5f)          // functions.f90:324
+#define BS_SP1EM6 ((double)1e-6f)          // integrator.f90:581
+#define BS_SP1EM9 ((double)1e-9f)          // scalar.f90:246 (Dm)
+
+struct ScenePar {                 // per-scene constants
+    double h, twoh, lam, dl, cw;  // cw = 4h cell width (setup.f90:51, incr=4)
+    double inv_h, inv_h2, inv_h3;
+    double cn1, cn2;              // alp*10/(C28 h^2), (1-alp)/(C3 h^2)
+    double wo;                    // Wo(h)
+    double rho, rhomin, rhomax, rel_den, g, mu, tschmidt;
+    double por, lamk, d50;
+    double freethr;               // lamfs*maxdivr
+    double csh, maxshift, sig1;
+    double xlcutoff, ytcutoff;
+    double ppe_tol, inner_tol;
+    int cellx, celly, ncell, cell0;   // grid dims and first global cell
+    int row0, cap, kmax, maxit;
+    int adaptive_dt, scalar_on, precision, stop_rule;
+    int nblk, blk0, max_outer, pad;
+};
+
+struct SceneDyn {                 // per-scene dynamic state (device)
+    int n, solsteps, lost, n_prev;
+    double t, dt, dtsol, umax, numax;
+    // solver scalars
+    double rho_old, alpha, omega, beta, rhonew;
+    double bnorm2, rnorm2, relres, rtrue2;
+    int iters, converged, breakdown, outer;
+    unsigned err;
+    int pad1;
+    double part_tmp;
+};
+
+// device pointers of one context (passed by value to kernels)
+struct Dev {
+    // particle fields (current buffer)
+    double *x, *y, *xs, *ys, *vx, *vy, *vxs, *vys, *p, *mass, *rho, *oden, *ovol, *con;
+    double *vol, *nu;               // derived: m/rho, vis(oden)/oden
+    int8_t* tid;
+    uint8_t* flags;
+    int* pid;
+    int* cell;                      // global cell index of the row
+    // particle fields (alternate buffer, permute target)
+    double *x2, *y2, *xs2, *ys2, *vx2, *vy2, *vxs2, *vys2, *p2, *mass2, *rho2, *oden2, *ovol2, *con2;
+    double *vol2, *nu2;
+    int8_t* tid2;
+    uint8_t* flags2;
+    int* pid2;
+    int* cell2;
+    // per-particle properties (recomputed after every re-bin)
+    double *por, *resx, *resy, *nut, *tke, *varts, *gradvx, *vel, *cdiff;
+    double *c0, *c1, *c2, *c3;      // coff (L^-1), search.f90:276-278
+    double *Dp0, *Dp1, *Dp2, *Dp3, *Dt;   // scalar dispersion per particle
+    double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
+    double *con_new;
+    // neighbour lists (ELL)
+    int* ncount;
+    int* nidx;
+    void *ndist, *nrinv, *nkx, *nky;   // double (FP64) or float (mixed)
+    // PPE
+    void* aval;                     // ELL values (double or float hi)
+    float* aval_lo;                 // mixed: lo part of the FP64 value
+    double *adiag, *rhs;
+    double *sx, *sr, *srhat, *sp, *sp2, *sv, *sv2, *ss, *st, *sxd;  // solver vectors
+    float *fr, *fp, *fp2, *fv, *fv2, *fs, *ft, *fd, *frhat;          // mixed inner vectors
+    // per-scene
+    const ScenePar* par;
+    SceneDyn* dyn;
+    const int* blk_scene;           // row block -> scene
+    const int* cell_scene;          // global cell -> scene
+    int* blk_done;                  // per-scene block counters for finisher reductions
+    double* part;                   // per-block partial sums [nblk_total][BS_MAXDOT]
+    // cells
+    int *cell_start, *cell_end, *cell_start2, *cell_end2;
+    int* bucket;                    // [ncell_total*BS_NCAT] counts then starts
+    int* cell_total;                // [ncell_total]
+    int* coderank;                  // per row: code<<24 | rank
+    double *cell_maxvel, *cell_maxeddy;
+    // grains (static, sorted by cell)
+    double *gx, *gy, *gv;           // gv = mass/density
+    int *gcell_start, *gcell_end;
+    int ncell_total, nrow_total, nblk_total, nscene;
+    int kmax;
+    unsigned* err_word;
+};
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ long ell(int row, int k, int kmax) {
+    return ((long)(row >> 5) * kmax + k) * 32 + (row & 31);
+}
+
+// cell bounds exactly as setup.f90:120-123 (local 1-based i,j)
+__device__ __forceinline__ double cell_xleft(const ScenePar& P, int j) { return (double)(j - 2) * (4.0 * P.h); }
+__device__ __forceinline__ double cell_xright(const ScenePar& P, int j) { return (double)(j - 1) * (4.0 * P.h); }
+__device__ __forceinline__ double cell_ybot(const ScenePar& P, int i) { return (double)(-i + P.celly - 1) * (4.0 * P.h); }
+__device__ __forceinline__ double cell_ytop(const ScenePar& P, int i) { return (double)(-i + P.celly) * (4.0 * P.h); }
+
+// Hybrid kernel value W(r) (kernel.f90:34-66)
+__device__ __forceinline__ double bs_W(double r, const ScenePar& P) {
+    const double q = r * P.inv_h;
+    double t1, t2;
+    if (r < P.h) {
+        t1 = 4.0 - 6.0 * q * q + 3.0 * q * q * q;
+        t2 = q * q * q - 6.0 * q + 6.0;
+    } else {
+        const double a = 2.0 - q;
+        t1 = a * a * a;
+        t2 = t1;
+    }
+    return P.cn1 * t1 + P.cn2 * t2;
+}
+
+// Radial factor F(r) of the hybrid-kernel gradient: grad_i W_ij = F(r) (r_i - r_j)
+// (kernel.f90:94-162: Wabx(p1=j, p2=i) = F * (p2%x - p1%x)).
+__device__ __forceinline__ double bs_F(double r, const ScenePar& P) {
+    if (r < P.h) {
+        const double t1 = 9.0 * r * P.inv_h3 - 12.0 * P.inv_h2;
+        const double t2 = 3.0 * r * P.inv_h3 - 6.0 * P.inv_h / r;
+        return P.cn1 * t1 + P.cn2 * t2;
+    }
+    const double a = 2.0 - r * P.inv_h;
+    const double c = (3.0 * P.inv_h / r) * a * a;
+    return -(P.cn1 + P.cn2) * c;
+}
+__device__ __forceinline__ float bs_Ff(float r, const ScenePar& P) {
+    const float ih = (float)P.inv_h, ih2 = (float)P.inv_h2, ih3 = (float)P.inv_h3;
+    const float c1 = (float)P.cn1, c2 = (float)P.cn2;
+    if (r < (float)P.h) {
+        const float t1 = 9.0f * r * ih3 - 12.0f * ih2;
+        const float t2 = 3.0f * r * ih3 - 6.0f * ih / r;
+        return c1 * t1 + c2 * t2;
+    }
+    const float a = 2.0f - r * ih;
+    const float c = (3.0f * ih / r) * a * a;
+    return -(c1 + c2) * c;
+}
+
+// viscosity (integrator.f90:12-30)
+__device__ __forceinline__ double bs_vis(double oden) {
+    const double Sp = oden - 1000.0;
+    return (1.002 + 0.001652 * Sp + 0.0000083 * (Sp * Sp)) * 0.001;
+}
+
+__device__ __forceinline__ void set_err(const Dev& D, int s, unsigned bits) {
+    atomicOr(&D.dyn[s].err, bits);
+    atomicOr(D.err_word, bits);
+}
+
+// block reductions (BS_THREADS threads)
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh /*[NV*32]*/) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[q * 32 + w] = v[q];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double a = (l < (int)(blockDim.x >> 5)) ? sh[q * 32 + l] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            v[q] = a;
+        }
+    }
+}
+
+template <int NV>
+__device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q] = fmax(v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[q * 32 + w] = v[q];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double a = (l < (int)(blockDim.x >> 5)) ? sh[q * 32 + l] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+            v[q] = a;
+        }
+    }
+}
+
+// ---------------------------------------------------------- launchers
+// (defined in the kernel translation units, called by the host code)
+namespace bs {
+// kernel ids for the per-kernel event timer
+enum KId {
+    K_RANK = 0, K_CELLPREFIX, K_SCANCELLS, K_PERMUTE, K_SEARCH, K_FREESURF, K_EDDY, K_INTVEL,
+    K_ASSEMBLE, K_COMPVEL, K_CELLMAX, K_TIMESTEP, K_SHIFT, K_APPLY, K_DISP, K_SCALAR,
+    K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
+    K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_COUNT
+};
+extern const char* const kernel_names[K_COUNT];
+struct KTimer {
+    unsigned long long mask = 0;
+    static const int NEV = 4096;
+    cudaEvent_t ev[NEV];
+    int id_of[NEV / 2];
+    int used = 0;
+    bool ready = false;
+    double total_ms[K_COUNT] = {};
+    long long count[K_COUNT] = {};
+};
+struct Launch {
+    cudaStream_t stream;
+    int nblk_rows;      // total row blocks
+    int ncell_total;
+    int64_t* launches;  // launch counter
+    KTimer* timer;
+};
+// bracket one launch with timer events (no-op unless the id is enabled)
+inline int tbegin(const Launch& L, int id) {
+    *L.launches += 1;
+    KTimer* T = L.timer;
+    if (!T || !T->ready || !((T->mask >> id) & 1ull) || T->used >= KTimer::NEV / 2) return -1;
+    const int q = T->used++;
+    T->id_of[q] = id;
+    cudaEventRecord(T->ev[2 * q], L.stream);
+    return q;
+}
+inline void tend(const Launch& L, int q) {
+    if (q >= 0) cudaEventRecord(L.timer->ev[2 * q + 1], L.stream);
+}
+void timer_collect(KTimer* T);
+void rebin(const Dev& D, const Launch& L, int projection, int cutoff);
+void search(const Dev& D, const Launch& L, int precision, int do_search, int do_effpor);
+void freesurf(const Dev& D, const Launch& L);
+void eddy(const Dev& D, const Launch& L, int precision, int with_varts, int with_disp);
+void int_vel(const Dev& D, const Launch& L, int precision);
+void assemble(const Dev& D, const Launch& L, int precision);
+void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_pos);
+void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_timestep);
+void shift(const Dev& D, const Launch& L, int precision);
+void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density);
+void scalar(const Dev& D, const Launch& L, int precision, int substep);
+void advance_time(const Dev& D, const Launch& L);
+void derive_fields(const Dev& D, const Launch& L);
+// solver
+void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const int* h_conv_flag,
+                int* d_all_conv, int* h_all_conv_pinned, cudaEvent_t ev);
+void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_all_conv,
+                 int* h_all_conv_pinned, cudaEvent_t ev);
+}  // namespace bs

@@ -1,0 +1,674 @@
+// bs_sweep.cu -- neighbour search and the neighbour-list sweeps of one ISPH
+// step.  One thread per particle row; the neighbour list of a 32-row slice
+// is read column by column (sliced ELL), so every warp-wide read of the k-th
+// neighbour entry is one coalesced request.  Template parameter T is the
+// storage/arithmetic type of the per-pair data (dist, 1/(r^2+lam), grad W)
+// and of the sweep sums: double for the FP64 drop-in, float for the mixed
+// form.  Positions and the exact pair test are always FP64.
+#include "bs_internal.cuh"
+
+namespace {
+
+struct RowCtx {
+    int r, s;
+    bool active;
+};
+
+__device__ __forceinline__ RowCtx row_ctx(const Dev& D) {
+    RowCtx c;
+    c.r = blockIdx.x * blockDim.x + threadIdx.x;
+    c.s = D.blk_scene[blockIdx.x];
+    c.active = c.r < D.par[c.s].row0 + D.dyn[c.s].n;
+    return c;
+}
+
+// The four cells of the quadrant stencil in the reference's order
+// (search.f90:328-388); false for a non-finite position.
+__device__ __forceinline__ bool quad_cells(const ScenePar& P, int c, double xi, double yi, int cc[4], int& own_q) {
+    const int lc = c - P.cell0;
+    const int i = lc % P.celly + 1, j = lc / P.celly + 1;
+    const double xl = cell_xleft(P, j), xr = cell_xright(P, j);
+    const double yb = cell_ybot(P, i), yt = cell_ytop(P, i);
+    const double mx = xl + fabs((xl - xr) / 2.0);
+    const double my = yb + fabs((yt - yb) / 2.0);
+    int ci[4], cj[4];
+    if (xi <= mx && yi <= my) {
+        ci[0] = i; cj[0] = j - 1; ci[1] = i + 1; cj[1] = j - 1; ci[2] = i; cj[2] = j; ci[3] = i + 1; cj[3] = j;
+        own_q = 2;
+    } else if (xi > mx && yi <= my) {
+        ci[0] = i; cj[0] = j; ci[1] = i + 1; cj[1] = j; ci[2] = i; cj[2] = j + 1; ci[3] = i + 1; cj[3] = j + 1;
+        own_q = 0;
+    } else if (xi > mx && yi > my) {
+        ci[0] = i - 1; cj[0] = j; ci[1] = i; cj[1] = j; ci[2] = i - 1; cj[2] = j + 1; ci[3] = i; cj[3] = j + 1;
+        own_q = 1;
+    } else if (xi <= mx && yi > my) {
+        ci[0] = i - 1; cj[0] = j - 1; ci[1] = i; cj[1] = j - 1; ci[2] = i - 1; cj[2] = j; ci[3] = i; cj[3] = j;
+        own_q = 3;
+    } else {
+        return false;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cc[q] = P.cell0 + (cj[q] - 1) * P.celly + (ci[q] - 1);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T ld(const void* p, long e) { return ((const T*)p)[e]; }
+template <typename T>
+__device__ __forceinline__ void st(void* p, long e, T v) { ((T*)p)[e] = v; }
+
+// ------------------------------------------------------------------ search
+// nsearch2 (search.f90:13-308) and effpor/porsearch (porous.f90:32-224)
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int do_effpor) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const int tid = D.tid[r];
+    const double xi = D.x[r], yi = D.y[r];
+    int cc[4], own_q;
+    const bool ok = quad_cells(P, D.cell[r], xi, yi, cc, own_q);
+    uint8_t fl = D.flags[r];
+    if (do_search) {
+        const int kmax = D.kmax;
+        const double twoh = P.twoh;
+        const float thr_hi = (float)(twoh * twoh) * (1.0f + 1e-5f);
+        double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+        int cnt = 0;
+        if (ok) {
+            for (int q = 0; q < 4; ++q) {
+                const int r1 = D.cell_end[cc[q]];
+                for (int rj = D.cell_start[cc[q]]; rj < r1; ++rj) {
+                    if (rj == r) continue;   // (tid, matid) self-exclusion
+                    const double dx = D.x[rj] - xi, dy = D.y[rj] - yi;
+                    const float fx = (float)dx, fy = (float)dy;
+                    if (fx * fx + fy * fy > thr_hi) continue;
+                    // exact test as functions.f90:38 / search.f90:59, no FMA
+                    const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                    if (!(rad < twoh)) continue;
+                    if (cnt < kmax) {
+                        const double F = bs_F(rad, P);
+                        const double kx = F * (-dx), ky = F * (-dy);   // grad_i W = F (r_i - r_j)
+                        const long e = ell(r, cnt, kmax);
+                        D.nidx[e] = rj;
+                        st<T>(D.ndist, e, (T)rad);
+                        st<T>(D.nrinv, e, (T)(1.0 / (rad * rad + P.lam)));
+                        st<T>(D.nkx, e, (T)kx);
+                        st<T>(D.nky, e, (T)ky);
+                        const double vj = D.vol[rj];
+                        const double res1 = vj * dx, res3 = vj * dy;
+                        a00 += kx * res1;
+                        a01 += ky * res1;
+                        a10 += kx * res3;
+                        a11 += ky * res3;
+                    }
+                    ++cnt;
+                }
+            }
+        }
+        if (cnt > kmax) set_err(D, R.s, BS_ERR_NBR_OVERFLOW);
+        D.ncount[r] = cnt < kmax ? cnt : kmax;
+        fl &= ~BS_FLAG_FREE;
+        double gv = 0.0;
+        if (tid == BS_TID_FLUID) {
+            fl &= ~BS_FLAG_VICINITY;
+            gv = a00 + a11;
+            // invertmat2D, functions.f90:62-96
+            const double det = a00 * a11 - a01 * a10;
+            double c0 = 1.0, c1 = 0.0, c2 = 0.0, c3 = 1.0;
+            if (fabs(det) >= BS_SP1EM5 && isfinite(det)) {
+                c0 = a11 / det;
+                c1 = -a01 / det;
+                c2 = -a10 / det;
+                c3 = a00 / det;
+            }
+            D.c0[r] = c0; D.c1[r] = c1; D.c2[r] = c2; D.c3[r] = c3;
+            if ((gv <= P.freethr) && !(fl & BS_FLAG_BUFFER)) fl |= BS_FLAG_FREE;
+        }
+        D.gradvx[r] = gv;
+        D.flags[r] = fl;
+    }
+    if (do_effpor) {
+        double phi = 1.0, res = 0.0;
+        if (tid == BS_TID_FLUID) {
+            double sf = 0.0;
+            if (ok) {
+                // effpor's cell order (porous.f90:125-176): its own cell, then
+                // the other three of the same quadrant in the listed order
+                int ord[4];
+                if (own_q == 2) { ord[0] = cc[2]; ord[1] = cc[0]; ord[2] = cc[3]; ord[3] = cc[1]; }
+                else if (own_q == 0) { ord[0] = cc[0]; ord[1] = cc[2]; ord[2] = cc[1]; ord[3] = cc[3]; }
+                else if (own_q == 1) { ord[0] = cc[1]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[3]; }
+                else { ord[0] = cc[3]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[1]; }
+                const double wsolid = 1.0 - P.por * 1.0;
+                for (int q = 0; q < 4; ++q) {
+                    const int g1 = D.gcell_end[ord[q]];
+                    for (int g = D.gcell_start[ord[q]]; g < g1; ++g) {
+                        const double dx = xi - D.gx[g], dy = yi - D.gy[g];
+                        const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                        if (rad < P.twoh) sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
+                    }
+                }
+            }
+            if (sf > (1.0 - P.por)) sf = 1.0 - P.por;
+            phi = 1.0 - sf;
+            const double od = D.oden[r];
+            const double rn = phi * od;
+            D.rho_new[r] = rn;
+            D.vol_new[r] = D.mass[r] / rn;
+            const double phi3 = phi * phi * phi;
+            const double Fch = 1.750 / sqrt(150.0 * phi3);
+            const double vx = D.vx[r], vy = D.vy[r];
+            const double vm = sqrt(vx * vx + vy * vy);
+            res = -((bs_vis(od) / od) * P.lamk * ((1.0 - phi) * (1.0 - phi)) / (phi3 * (P.d50 * P.d50))) -
+                  ((Fch * vm * sqrt(P.lamk) * (1.0 - phi)) / (sqrt(phi3) * P.d50));
+        } else {
+            D.rho_new[r] = D.rho[r];
+            D.vol_new[r] = D.vol[r];
+        }
+        D.por[r] = phi;
+        D.resx[r] = res;
+        D.resy[r] = res;
+    }
+}
+
+// freesurf, isph.f90:49-86 (concurrent writes of the same bit: benign)
+__global__ void k_freesurf(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    const uint8_t fl = D.flags[r];
+    if (D.tid[r] != BS_TID_FLUID || (fl & BS_FLAG_BUFFER)) return;
+    if (!(D.gradvx[r] <= D.par[R.s].freethr)) return;
+    const int n = D.ncount[r];
+    for (int k = 0; k < n; ++k) {
+        const int j = D.nidx[ell(r, k, D.kmax)];
+        D.flags[j] = D.flags[j] | BS_FLAG_VICINITY;
+    }
+}
+
+// ------------------------------------------------------------------ eddyvis
+// turbulence.f90:12-113, with int_vel's varts (integrator.f90:468-507: the
+// same L-corrected velocity-gradient sums) and optionally the per-particle
+// dispersion tensor used by the next scalar sub-steps (scalar.f90:276-301).
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_varts, int with_disp) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    if (D.tid[r] != BS_TID_FLUID) {
+        D.nut[r] = 0.0;
+        D.tke[r] = 0.0;
+        if (with_varts) D.varts[r] = 0.0;
+        return;
+    }
+    const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
+    const double phi = D.por[r];
+    const double vx = D.vx[r], vy = D.vy[r];
+    const T ui = (T)(vx / phi), wi = (T)(vy / phi);
+    T t1 = 0, t2 = 0, t3 = 0;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
+        const double pj = D.por[j];
+        const T a = (T)(D.vx[j] / pj) - ui, b = (T)(D.vy[j] / pj) - wi;
+        const T V = (T)D.vol[j];
+        const T Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+        t1 += V * a * Lx;
+        t2 += V * b * Ly;
+        t3 += (T)0.5 * V * (a * Ly + b * Lx);
+    }
+    const double cs = 0.150, cv = 0.080, ce = 1.0, dl = P.dl;
+    const double t4 = sqrt(2.0 * ((double)t1 * t1 + (double)t2 * t2) + (2.0 * t3) * (2.0 * t3));
+    const double nut = ((cs * dl) * (cs * dl)) * t4;
+    D.nut[r] = nut;
+    D.tke[r] = (cv / ce) * ((dl * t4) * (dl * t4));
+    if (with_varts) {
+        double va = 0.0;
+        if (D.flags[r] & BS_FLAG_FREE)
+            va = (dl * dl) * sqrt((double)t1 * t1 + (double)t2 * t2) * sqrt(vx * vx + vy * vy) /
+                 ((D.dyn[R.s].umax + BS_SP1EM6) * phi);
+        D.varts[r] = va;
+    }
+    if (with_disp) {
+        const double al = 0.0025, at = 0.00025, Dm = BS_SP1EM9;
+        const double vi = sqrt(vx * vx + vy * vy) / phi;
+        const double dl_ = sqrt((al * vi) + Dm) * vi * phi, dt_ = sqrt((at * vi) + Dm) * vi * phi;
+        D.Dp0[r] = vx / dl_;
+        D.Dp1[r] = vy / dl_;
+        D.Dp2[r] = (-vy) / dt_;
+        D.Dp3[r] = vx / dt_;
+        D.Dt[r] = Dm + nut / P.tschmidt;
+    }
+}
+
+// ------------------------------------------------------------------ int_vel
+// integrator.f90:510-701 (non-pressure velocity v*)
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    if (D.tid[r] != BS_TID_FLUID) return;
+    const uint8_t fl = D.flags[r];
+    const double dt = D.dyn[R.s].dt;
+    const double phi = D.por[r];
+    if (fl & BS_FLAG_BUFFER) {
+        D.vxs[r] = D.vx[r];
+        D.vys[r] = P.g * phi * dt;
+        return;
+    }
+    const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
+    const double xi = D.x[r], yi = D.y[r], vxi = D.vx[r], vyi = D.vy[r];
+    const double nui = D.nu[r], nuti = D.nut[r], tkei = D.tke[r], vartsi = D.varts[r];
+    const bool freei = fl & BS_FLAG_FREE;
+    T sx = 0, sy = 0;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    const T two3 = (T)(2.0 / 3);
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
+        const T pd = ld<T>(D.nrinv, e);
+        const int tj = D.tid[j];
+        T cmu;
+        if (tj == BS_TID_FLUID) {
+            const double nuj = D.nu[j];
+            cmu = (T)(2.0 * nui * nuj / (nui + nuj));
+        } else {
+            cmu = (T)nui;
+        }
+        T vart = 0;
+        if (freei) vart = (T)vartsi;
+        else if (D.flags[j] & BS_FLAG_FREE) vart = (T)(bs_W((double)ld<T>(D.ndist, e), P) * D.varts[j] / P.wo);
+        const T pvol = (T)D.vol[j];
+        const T Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+        const T dxi = (T)(xi - D.x[j]), dyi = (T)(yi - D.y[j]);
+        const T gg = (T)2 * pvol * (dxi * Lx + dyi * Ly) * pd;
+        const T ax = (T)(vxi - D.vx[j]) * gg, ay = (T)(vyi - D.vy[j]) * gg;
+        sx += ax * (cmu + vart);
+        sy += ay * (cmu + vart);
+        if (tj > 2) {
+            const double nutj = D.nut[j];
+            T mix;
+            if ((nuti < BS_SP1EM6) && (nutj < BS_SP1EM6)) mix = (T)((nuti + nutj) * 0.50);
+            else mix = (T)((2 * nuti * nutj) / (nuti + nutj));
+            sx += ax * mix;
+            sy += ay * mix;
+        }
+        const T tk = pvol * (T)(D.tke[j] - tkei);
+        sx -= tk * Lx * (T)phi * two3;
+        sy -= tk * Ly * (T)phi * two3;
+    }
+    double vxs = (vxi + (dt * (double)sx)) / (1.0 - dt * D.resx[r] * phi);
+    double vys = (vyi + dt * ((double)sy)) / (1.0 - dt * D.resy[r] * phi);
+    vys = vys + P.g * phi * dt;
+    D.vxs[r] = vxs;
+    D.vys[r] = vys;
+}
+
+// ------------------------------------------------------------- assembly
+// ppesolve, isph.f90:136-444: rows in the neighbour-list order (ascending
+// row = matid, so already column-sorted as after qsort), Jacobi-scaled.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const int ti = D.tid[r];
+    const uint8_t fl = D.flags[r];
+    const double dt = D.dyn[R.s].dt;
+    const double xi = D.x[r], yi = D.y[r];
+    const double rhoi = D.rho[r], phii = D.por[r];
+    const double rho_i = rhoi * (1.0 / phii);
+    const double vxsi = D.vxs[r], vysi = D.vys[r], mi = D.mass[r];
+    const double c0 = D.c0[r], c1 = D.c1[r], c2 = D.c2[r], c3 = D.c3[r];
+    const bool freei = fl & BS_FLAG_FREE;
+    const double lampf = 1.0 / (P.rho * P.rel_den);
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    double dia = 0.0, fv = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        const double z1 = (double)ld<T>(D.nkx, e), z2 = (double)ld<T>(D.nky, e);
+        const double pd = (double)ld<T>(D.nrinv, e);
+        const int tj = D.tid[j];
+        const double dxi = xi - D.x[j], dyi = yi - D.y[j];
+        double off = 0.0;
+        if (ti == BS_TID_FLUID) {
+            const double lamp = (freei && tj == BS_TID_FLUID) ? (1.0 + D.oden[j] * lampf) : 1.0;
+            const double pvol = D.vol[j];
+            const double Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const double t12 = 2 * pvol * (Lx * dxi + Ly * dyi) * pd;
+            off = -t12;
+            dia += t12 * lamp;
+            const double phij = D.por[j];
+            double ax, ay;
+            if (tj == BS_TID_FLUID) {
+                const double rhoj = D.rho[j];
+                const double rho_ij = 2 * rhoj * rhoi * (1.0 / (phij * phii)) * (1.0 / ((rhoj / phij) + (rhoi / phii)));
+                ax = D.vxs[j] * rho_ij / phij - vxsi * rho_ij / phii;
+                ay = D.vys[j] * rho_ij / phij - vysi * rho_ij / phii;
+            } else {
+                ax = D.vxs[j] * rho_i / phii - vxsi * rho_i / phii;
+                ay = D.vys[j] * rho_i / phii - vysi * rho_i / phii;
+            }
+            fv += (pvol * (ax * Lx + ay * Ly)) / dt;
+        } else if (ti == BS_TID_GHOST) {
+            if (tj <= 2) {
+                const double t12 = 2 * D.vol[j] * (z1 * dxi + z2 * dyi) * pd;
+                off = -t12;
+                dia += t12;
+            }
+        } else if (ti == BS_TID_WALL) {
+            if (tj == BS_TID_FLUID) {
+                const double d0 = D.c0[j], d1 = D.c1[j], d2 = D.c2[j], d3 = D.c3[j];
+                const double Lx = d0 * z1 + d1 * z2, Ly = d2 * z1 + d3 * z2;
+                const double t12 = 2 * mi * (Lx * dxi + Ly * dyi) * pd / rhoi;
+                off = -t12;
+                dia += t12;
+                const double phij = D.por[j];
+                const double rho_j = D.rho[j] * (1.0 / phij);
+                const double ax = D.vxs[j] * rho_j / phij - vxsi * rho_j / phii;
+                const double ay = D.vys[j] * rho_j / phij - vysi * rho_j / phii;
+                fv += (mi * (ax * Lx + ay * Ly)) / rhoi / dt;
+            } else {
+                const double t12 = 2 * D.vol[j] * (z1 * dxi + z2 * dyi) * pd;
+                off = -t12;
+                dia += t12;
+            }
+        }
+        st<double>(D.aval, e, off);   // unscaled, scaled below
+    }
+    // Jacobi scaling (isph.f90:432-440).  A ghost row whose first neighbour
+    // is a lower-numbered fluid particle keeps the row initialiser's
+    // val(1)=1.0 at col=row (isph.f90:125-128): an extra 1/dia on the diagonal.
+    const double inv = 1.0 / dia;
+    double extra = 0.0;
+    if (ti == BS_TID_GHOST && n > 0) {
+        const int j0 = D.nidx[ell(r, 0, kmax)];
+        if (j0 < r && D.tid[j0] == BS_TID_FLUID) extra = 1.0;
+    }
+    if (!(dia != 0.0) || !isfinite(dia)) set_err(D, R.s, BS_ERR_ZERO_DIAG);
+    D.adiag[r] = dia / dia + extra / dia;
+    D.rhs[r] = fv / dia;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        double* a = (double*)D.aval;
+        a[e] = a[e] / dia;
+    }
+    (void)inv;
+}
+
+// ---------------------------------------------------- comp_vel + comp_pos
+// integrator.f90:705-829 and 845-883
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int do_pos) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    const int ti = D.tid[r];
+    const uint8_t fl = D.flags[r];
+    const double dt = D.dyn[R.s].dt;
+    double vx = D.vx[r], vy = D.vy[r];
+    const double phi = D.por[r];
+    if (do_vel) {
+        double vel = 0.0;
+        if (ti == BS_TID_FLUID && !(fl & BS_FLAG_BUFFER)) {
+            const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
+            const double pi = D.p[r], rhoi = D.rho[r];
+            const T phi2 = (T)(phi * phi);
+            T ax = 0, ay = 0;
+            const int n = D.ncount[r];
+            const int kmax = D.kmax;
+            for (int k = 0; k < n; ++k) {
+                const long e = ell(r, k, kmax);
+                const int j = D.nidx[e];
+                const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
+                const T Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+                const double pj = D.p[j];
+                T q;
+                if (D.tid[j] == BS_TID_FLUID) {
+                    const double rhoj = D.rho[j], phij = D.por[j];
+                    q = (T)(2.0 * D.vol[j] * (phi * phi) * ((pj * rhoi / phi) + (pi * rhoj / phij)) /
+                            ((rhoi) * ((rhoi / phi) + (rhoj / phij))));
+                } else {
+                    q = (T)D.vol[j] * phi2 * (T)(pj + pi) / (T)rhoi;
+                }
+                ax -= q * Lx;
+                ay -= q * Ly;
+            }
+            vx = D.vxs[r] + (double)ax * dt;
+            vy = D.vys[r] + (double)ay * dt;
+            vel = sqrt(vx * vx + vy * vy) / phi;
+            D.vx[r] = vx;
+            D.vy[r] = vy;
+        } else if (fl & BS_FLAG_BUFFER) {
+            vx = D.vxs[r];
+            vy = 0.0;
+            D.vx[r] = vx;
+            D.vy[r] = vy;
+        }
+        D.vel[r] = vel;
+    }
+    if (do_pos && ti == BS_TID_FLUID) {
+        // x = (x + xs + dt*vx/porosity)/2 (integrator.f90:859-863), no FMA
+        const double x = D.x[r], y = D.y[r];
+        D.x[r] = __ddiv_rn(__dadd_rn(__dadd_rn(x, D.xs[r]), __ddiv_rn(__dmul_rn(dt, vx), phi)), 2.0);
+        D.y[r] = __ddiv_rn(__dadd_rn(__dadd_rn(y, D.ys[r]), __ddiv_rn(__dmul_rn(dt, vy), phi)), 2.0);
+    }
+}
+
+// ------------------------------------------------------------ opt2_shift
+// part_shift.f90:12-169 (shift and Taylor velocity correction; applied by
+// k_apply_density).  The free-surface normals are forced to zero (67-68)
+// and pint = 0 (69), so the shift uses the raw kernel gradient.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const uint8_t fl = D.flags[r];
+    if (D.tid[r] != BS_TID_FLUID || (fl & BS_FLAG_BUFFER)) return;
+    const int n = D.ncount[r];
+    if (n == 0) {   // keeps stale xs/ys/vxs/vys, as the reference (part_shift.f90:39)
+        set_err(D, R.s, BS_ERR_NO_NEIGHBOUR);
+        return;
+    }
+    const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
+    const double vxi = D.vx[r], vyi = D.vy[r];
+    T sxs = 0, sys = 0, a1 = 0, a2 = 0, b1 = 0, b2 = 0;
+    const int kmax = D.kmax;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
+        const T V = (T)D.vol[j];
+        sxs += z1 * V;
+        sys += z2 * V;
+        const T Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+        const T du = (T)(D.vx[j] - vxi), dv = (T)(D.vy[j] - vyi);
+        a1 += Lx * du * V;
+        a2 += Ly * du * V;
+        b1 += Lx * dv * V;
+        b2 += Ly * dv * V;
+    }
+    const double frac = (fl & BS_FLAG_FREE) ? 0.01 : 1.0;
+    const double cfac = -P.csh * (P.h * P.h) * frac;
+    const double xs = cfac * (double)sxs, ys = cfac * (double)sys;
+    const double cap = P.maxshift * P.dl;
+    if (xs == 0.0 || ys == 0.0) set_err(D, R.s, BS_ERR_ZERO_SHIFT);
+    D.xs[r] = fmin(fabs(xs), cap) * xs / fabs(xs);
+    D.ys[r] = fmin(fabs(ys), cap) * ys / fabs(ys);
+    D.vxs[r] = (double)a1 * xs + (double)a2 * ys;
+    D.vys[r] = (double)b1 * xs + (double)b2 * ys;
+}
+
+// apply the shift (part_shift.f90:172-189) and densityupdate (scalar.f90:399-426)
+__global__ void k_apply_density(Dev D, int do_apply, int do_density) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    if (D.tid[r] != BS_TID_FLUID) return;
+    const uint8_t fl = D.flags[r];
+    if (do_apply && !(fl & BS_FLAG_BUFFER)) {
+        D.x[r] = __dadd_rn(D.x[r], D.xs[r]);
+        D.y[r] = __dadd_rn(D.y[r], D.ys[r]);
+        D.vx[r] = D.vx[r] + D.vxs[r];
+        D.vy[r] = D.vy[r] + D.vys[r];
+    }
+    if (do_density) {
+        const double od = 0.5 * (P.rhomax + P.rhomin) + D.con[r] * (P.rhomax - P.rhomin);
+        const double m = od * D.ovol[r];
+        const double rh = od * D.por[r];
+        D.oden[r] = od;
+        D.mass[r] = m;
+        D.rho[r] = rh;
+        D.vol[r] = m / rh;
+        D.nu[r] = bs_vis(od) / od;
+    }
+}
+
+// |v|/porosity for fluid rows (the vel of comp_vel, integrator.f90:814-815),
+// from the uploaded velocities: initial timestep maxima
+__global__ void k_velmag(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    double v = 0.0;
+    if (D.tid[r] == BS_TID_FLUID && !(D.flags[r] & BS_FLAG_BUFFER)) {
+        const double vx = D.vx[r], vy = D.vy[r];
+        v = sqrt(vx * vx + vy * vy) / D.por[r];
+    }
+    D.vel[r] = v;
+}
+
+// dispersion tensor per particle (scalar.f90:267-301), for the stand-alone
+// scalar entry point (the fused step computes it in the final k_eddy)
+__global__ void k_disp(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    if (D.tid[r] != BS_TID_FLUID) return;
+    const double al = 0.0025, at = 0.00025, Dm = BS_SP1EM9;
+    const double vx = D.vx[r], vy = D.vy[r], phi = D.por[r];
+    const double vi = sqrt(vx * vx + vy * vy) / phi;
+    const double dl_ = sqrt((al * vi) + Dm) * vi * phi, dt_ = sqrt((at * vi) + Dm) * vi * phi;
+    D.Dp0[r] = vx / dl_;
+    D.Dp1[r] = vy / dl_;
+    D.Dp2[r] = (-vy) / dt_;
+    D.Dp3[r] = vx / dt_;
+    D.Dt[r] = Dm + D.nut[r] / P.tschmidt;
+}
+
+// ------------------------------------------------------------- scalar
+// scalart_anisotropic (scalar.f90:242-362) + scalarupdate (364-397); reads
+// con, writes con_new (swapped by the host).  Uses the stored pair distance
+// with the current positions, as the reference does.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const double coni = D.con[r];
+    // sub-steps beyond this scene's solsteps (integrator.f90:941-949) copy through
+    if (D.tid[r] != BS_TID_FLUID || !P.scalar_on || substep >= D.dyn[R.s].solsteps) {
+        D.con_new[r] = coni;
+        return;
+    }
+    const double thr = 0.7;
+    const double phii = D.por[r], nuti = D.nut[r];
+    const double xi = D.x[r], yi = D.y[r];
+    const double Pi0 = D.Dp0[r], Pi1 = D.Dp1[r], Pi2 = D.Dp2[r], Pi3 = D.Dp3[r], Dti = D.Dt[r];
+    const double cap = 0.12 * (P.dl * P.dl) / D.dyn[R.s].dt;
+    const double ovoli = D.ovol[r];
+    double cd = 0.0;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        if (D.tid[j] != BS_TID_FLUID) continue;
+        const double phij = D.por[j];
+        const bool pz = (phii < thr) && (phij < thr);
+        const double dm = (double)ld<T>(D.ndist, e);
+        const double dxi = xi - D.x[j], dyi = yi - D.y[j];
+        double t1x;
+        if (pz) {
+            const double Dxx = Pi0 + D.Dp0[j], Dxy = Pi1 + D.Dp1[j], Dyx = Pi2 + D.Dp2[j], Dyy = Pi3 + D.Dp3[j];
+            const double pdist = 1.0 / dm;
+            const double A = (Dxx * dxi * pdist * 0.5) + (Dxy * dyi * pdist * 0.5);
+            const double B = (Dyx * dxi * pdist * 0.5) + (Dyy * dyi * pdist * 0.5);
+            t1x = 1.0 / (A * A + B * B);
+            t1x = (t1x <= cap) ? t1x : cap;
+        } else {
+            const double Dxxj = D.Dt[j];
+            if ((nuti < BS_SP1EM6) && (D.nut[j] < BS_SP1EM6)) t1x = (Dti + Dxxj) * 0.50;
+            else t1x = 2 * Dti * Dxxj / (Dti + Dxxj);
+        }
+        const double t3 = ovoli * (phii + phij) / (phii * phij);
+        const double F = bs_F(dm, P);
+        const double pd = (double)ld<T>(D.nrinv, e);
+        const double dc = coni - D.con[j];
+        cd += (t1x * t3 * dc * dxi * (F * dxi) * pd) + (t1x * t3 * dc * dyi * (F * dyi) * pd);
+    }
+    D.cdiff[r] = cd;
+    double cn = coni + cd * D.dyn[R.s].dtsol;
+    if ((D.flags[r] & BS_FLAG_BUFFER) && (xi < 1.6)) cn = 0.5;
+    D.con_new[r] = cn;
+}
+
+}  // namespace
+
+namespace bs {
+
+#define BS_DISPATCH(id, prec, kern, ...)                                                          \
+    do {                                                                                          \
+        const int q_ = tbegin(L, id);                                                             \
+        if ((prec) == BS_PREC_MIXED) kern<float><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__); \
+        else kern<double><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__);                  \
+        tend(L, q_);                                                                              \
+    } while (0)
+#define BS_PLAIN(id, kern, ...)                                                                   \
+    do {                                                                                          \
+        const int q_ = tbegin(L, id);                                                             \
+        kern<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__);                              \
+        tend(L, q_);                                                                              \
+    } while (0)
+
+void search(const Dev& D, const Launch& L, int precision, int do_search, int do_effpor) {
+    BS_DISPATCH(K_SEARCH, precision, k_search, D, do_search, do_effpor);
+}
+void freesurf(const Dev& D, const Launch& L) { BS_PLAIN(K_FREESURF, k_freesurf, D); }
+void eddy(const Dev& D, const Launch& L, int precision, int with_varts, int with_disp) {
+    BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_varts, with_disp);
+}
+void int_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_INTVEL, precision, k_intvel, D); }
+void assemble(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D); }
+void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_pos) {
+    BS_DISPATCH(K_COMPVEL, precision, k_compvel, D, do_vel, do_pos);
+}
+void shift(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_SHIFT, precision, k_shift, D); }
+void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density) {
+    BS_PLAIN(K_APPLY, k_apply_density, D, do_apply, do_density);
+}
+void disp(const Dev& D, const Launch& L) { BS_PLAIN(K_DISP, k_disp, D); }
+void velmag(const Dev& D, const Launch& L) { BS_PLAIN(K_VELMAG, k_velmag, D); }
+void scalar(const Dev& D, const Launch& L, int precision, int substep) {
+    BS_DISPATCH(K_SCALAR, precision, k_scalar, D, substep);
+}
+
+}  // namespace bs
