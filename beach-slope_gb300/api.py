@@ -39,6 +39,7 @@ def _load():
         "bs_last_error": (C.c_char_p, [vp]),
         "bs_get_neighbours": (C.c_int, [vp, i32, vp, vp, vp, vp, vp]),
         "bs_get_matrix": (C.c_int, [vp, i32, vp, vp, vp]),
+        "bs_set_rhs": (C.c_int, [vp, i32, vp]),
         "bs_prime": (C.c_int, [vp]),
         "bs_scalar_substep": (C.c_int, [vp]),
         "bs_projection": (C.c_int, [vp]),
@@ -151,6 +152,10 @@ class Context:
         self._check(lib.bs_get_matrix(self.h, s, diag.ctypes.data, off.ctypes.data, rhs.ctypes.data),
                     "get_matrix")
         return diag, off, rhs
+
+    def set_rhs(self, b, s=0):
+        b = np.ascontiguousarray(b, np.float64)
+        self._check(lib.bs_set_rhs(self.h, s, b.ctypes.data), "set_rhs")
 
     def stage(self, name):
         f = getattr(lib, "bs_" + name)

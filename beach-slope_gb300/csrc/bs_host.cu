@@ -586,12 +586,22 @@ int bs_get_matrix(bs_ctx* ctx, int32_t s, double* diag, double* off, double* rhs
     return 0;
 }
 
+int bs_set_rhs(bs_ctx* ctx, int32_t s, const double* b) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !b) return BS_E_ARG;
+    if (!ctx->assembled) return fail(ctx, BS_E_STATE, "matrix not assembled");
+    CK(cudaStreamSynchronize(ctx->stream));
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ctx->D.rhs + ctx->hpar[s].row0, b, sizeof(double) * hd.n, cudaMemcpyHostToDevice));
+    return 0;
+}
+
 // ------------------------------------------------------------------ stages
 int bs_prime(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     bs::Launch L = launch_of(ctx);
     st_search(ctx, 1, 1);
-    bs::eddy(ctx->D, L, ctx->precision, 0, 0);
+    bs::eddy(ctx->D, L, ctx->precision, 1, 0, 0);
     bs::velmag(ctx->D, L);
     bs::cell_max_timestep(ctx->D, L, 1, 1);
     bs::disp(ctx->D, L);
@@ -629,12 +639,12 @@ int bs_porosity(bs_ctx* ctx) {
 }
 int bs_eddy(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
-    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 0, 0);
+    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 1, 0, 0);
     return check_launch(ctx);
 }
 int bs_int_vel(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
-    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 1, 0);   // varts (integrator.f90:468-507)
+    bs::eddy(ctx->D, launch_of(ctx), ctx->precision, 0, 1, 0);   // varts (integrator.f90:468-507)
     bs::int_vel(ctx->D, launch_of(ctx), ctx->precision);
     return check_launch(ctx);
 }
@@ -707,7 +717,7 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
         }
         st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
         st_search(ctx, 1, 1);                // neighbour + effpor
-        bs::eddy(D, L, ctx->precision, 1, 0);  // eddyvis (+ varts of int_vel)
+        bs::eddy(D, L, ctx->precision, 1, 1, 0);  // eddyvis (+ varts of int_vel)
         bs::int_vel(D, L, ctx->precision);
         bs::assemble(D, L, ctx->precision);
         ctx->assembled = true;
@@ -720,7 +730,7 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
         bs::shift(D, L, ctx->precision);     // opt2_shift
         bs::apply_density(D, L, 1, 1);       // shift apply + densityupdate
         bs::cell_max_timestep(D, L, 0, 1);   // timestep
-        bs::eddy(D, L, ctx->precision, 0, 1);  // eddyvis (+ dispersion for the next scalar)
+        bs::eddy(D, L, ctx->precision, 1, 0, 1);  // eddyvis (+ dispersion for the next scalar)
         ctx->disp_ready = true;
         int rc = check_launch(ctx);
         if (rc) return rc;

@@ -262,7 +262,7 @@ void timer_collect(KTimer* T);
 void rebin(const Dev& D, const Launch& L, int projection, int cutoff);
 void search(const Dev& D, const Launch& L, int precision, int do_search, int do_effpor);
 void freesurf(const Dev& D, const Launch& L);
-void eddy(const Dev& D, const Launch& L, int precision, int with_varts, int with_disp);
+void eddy(const Dev& D, const Launch& L, int precision, int with_eddy, int with_varts, int with_disp);
 void int_vel(const Dev& D, const Launch& L, int precision);
 void assemble(const Dev& D, const Launch& L, int precision);
 void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_pos);

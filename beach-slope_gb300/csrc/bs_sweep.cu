@@ -193,14 +193,16 @@ __global__ void k_freesurf(Dev D) {
 // same L-corrected velocity-gradient sums) and optionally the per-particle
 // dispersion tensor used by the next scalar sub-steps (scalar.f90:276-301).
 template <typename T>
-__global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_varts, int with_disp) {
+__global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int with_varts, int with_disp) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
     const ScenePar& P = D.par[R.s];
     const int r = R.r;
     if (D.tid[r] != BS_TID_FLUID) {
-        D.nut[r] = 0.0;
-        D.tke[r] = 0.0;
+        if (with_eddy) {
+            D.nut[r] = 0.0;
+            D.tke[r] = 0.0;
+        }
         if (with_varts) D.varts[r] = 0.0;
         return;
     }
@@ -225,9 +227,12 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_varts, int 
     }
     const double cs = 0.150, cv = 0.080, ce = 1.0, dl = P.dl;
     const double t4 = sqrt(2.0 * ((double)t1 * t1 + (double)t2 * t2) + (2.0 * t3) * (2.0 * t3));
-    const double nut = ((cs * dl) * (cs * dl)) * t4;
-    D.nut[r] = nut;
-    D.tke[r] = (cv / ce) * ((dl * t4) * (dl * t4));
+    double nut = D.nut[r];
+    if (with_eddy) {
+        nut = ((cs * dl) * (cs * dl)) * t4;
+        D.nut[r] = nut;
+        D.tke[r] = (cv / ce) * ((dl * t4) * (dl * t4));
+    }
     if (with_varts) {
         double va = 0.0;
         if (D.flags[r] & BS_FLAG_FREE)
@@ -653,8 +658,8 @@ void search(const Dev& D, const Launch& L, int precision, int do_search, int do_
     BS_DISPATCH(K_SEARCH, precision, k_search, D, do_search, do_effpor);
 }
 void freesurf(const Dev& D, const Launch& L) { BS_PLAIN(K_FREESURF, k_freesurf, D); }
-void eddy(const Dev& D, const Launch& L, int precision, int with_varts, int with_disp) {
-    BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_varts, with_disp);
+void eddy(const Dev& D, const Launch& L, int precision, int with_eddy, int with_varts, int with_disp) {
+    BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_eddy, with_varts, with_disp);
 }
 void int_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_INTVEL, precision, k_intvel, D); }
 void assemble(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D); }

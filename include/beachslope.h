@@ -179,6 +179,10 @@ int bs_get_neighbours(struct bs_ctx* ctx, int32_t scene, int32_t* counts, int32_
  * aligned with the neighbour list, rhs[n]. */
 int bs_get_matrix(struct bs_ctx* ctx, int32_t scene, double* diag, double* off, double* rhs);
 
+/* Replace the assembled right-hand side (already Jacobi-scaled) of one scene,
+ * e.g. with a manufactured source; b[n] in download order. */
+int bs_set_rhs(struct bs_ctx* ctx, int32_t scene, const double* b);
+
 /* ---- one entry point per reference subroutine ----------------------------- */
 /* Warm-up: neighbour lists, porosity, eddy viscosity and timestep maxima for
  * the uploaded state (what the reference's spin-up leaves behind, main.f90:35-67). */

@@ -1,0 +1,315 @@
+"""GPU parity tests: the CUDA library (through the C-ABI) against the oracle,
+the golden fixtures and size-independent properties.
+
+Tolerances: neighbour sets, counts, cell keys and particle order are
+bit-exact; the stored pair distance is bit-exact (same IEEE expression);
+FP64 real fields agree to the stated relative tolerances (summation order
+and FMA contraction differ between the two codes).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+from _scenes import ghost_row_scene  # noqa: E402
+
+KAT_ROW = np.array([1, 4, 6, 8, 11, 14]) - 1
+KAT_COL = np.array([1, 3, 4, 2, 4, 1, 3, 2, 3, 4, 1, 2, 5]) - 1
+
+
+def relL2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_solvertest_known_answer_gpu(api):
+    rc, x, it, rr = api.bicgstab_csr(KAT_ROW, KAT_COL, np.ones(13), [8.0, 6.0, 4.0, 9.0, 8.0], np.ones(5),
+                                     tol=1e-13)
+    assert rc == 0
+    np.testing.assert_allclose(x, [1, 2, 3, 4, 5], rtol=0, atol=1e-10)
+    assert rr < 1e-12
+
+
+def _golden(name):
+    return dict(np.load(os.path.join(GOLD, name)))
+
+
+def _params_from(g):
+    from beachslope_gb300 import abi
+    p = abi.default_params()
+    for k, v in g.items():
+        if k.startswith("param_"):
+            setattr(p, k[6:], v.item())
+    return p
+
+
+def test_golden_beach_fixture(api):
+    g = _golden("beach_dx004.npz")
+    p = _params_from(g)
+    st = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    gr = {k[6:]: v for k, v in g.items() if k.startswith("grain_")}
+    ctx = api.Context([p], [st], [gr])
+    ctx.prime()
+    s = ctx.download()
+    np.testing.assert_array_equal(s["pid"], g["prime_pid"])
+    np.testing.assert_array_equal(s["cell"], g["prime_cell"])
+    np.testing.assert_array_equal(s["flags"], g["prime_flags"])
+    assert relmax(s["porosity"], g["prime_porosity"]) < 1e-13
+    assert relmax(s["coff"], g["prime_coff"]) < 1e-11
+    assert relmax(s["nut"], g["prime_nut"]) < 1e-10
+    c, idx, dist, kx, ky = ctx.neighbours()
+    np.testing.assert_array_equal(c, g["prime_nbr_count"])
+    m = np.arange(p.kmax)[None, :] < c[:, None]
+    np.testing.assert_array_equal(idx[m], g["prime_nbr_idx"])
+    np.testing.assert_array_equal(dist[m], g["prime_nbr_dist"])
+    assert relmax(kx[m], g["prime_nbr_kx"]) < 1e-13
+    ctx.step(1)
+    s = ctx.download()
+    np.testing.assert_array_equal(s["pid"], g["step1_pid"])
+    assert np.max(np.abs(s["x"] - g["step1_x"])) < 1e-13
+    assert relL2(s["p"], g["step1_p"]) < 1e-9
+    assert relL2(s["vx"], g["step1_vx"]) < 1e-9
+    ctx.step(2)
+    s = ctx.download()
+    np.testing.assert_array_equal(s["pid"], g["step3_pid"])
+    assert np.max(np.abs(s["x"] - g["step3_x"])) < 1e-12
+    assert relL2(s["p"], g["step3_p"]) < 1e-8
+    assert relL2(s["con"], g["step3_con"]) < 1e-12
+    assert ctx.info()["err_bits"] == 0
+
+
+def _pair(api, oracle, dx=0.02):
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=dx)
+    p.ppe_tol = 1e-13
+    return p, api.Context([p], [st], [gr]), oracle.Oracle(p, st, gr)
+
+
+def _cmp(g, o, fields, tol):
+    for f in fields:
+        e = relmax(g[f], o[f])
+        assert e < tol, f"{f}: {e:.3e}"
+
+
+def test_stagewise_parity(api, oracle):
+    """Each reference subroutine through its own C-ABI entry point."""
+    p, ctx, o = _pair(api, oracle)
+    ctx.prime()
+    o.stage("prime")
+    ctx.scalar_substep(); o.stage("scalar_substep")
+    _cmp(ctx.download(), o.get(), ["con", "cdiff"], 1e-9)
+    ctx.projection(); o.stage("projection")
+    ctx.cellshift(False); o.stage("cellshift"); o.stage("resetid")
+    g, r = ctx.download(), o.get()
+    np.testing.assert_array_equal(g["pid"], r["pid"])
+    np.testing.assert_array_equal(g["cell"], r["cell"])
+    assert np.array_equal(g["x"], r["x"]) and np.array_equal(g["y"], r["y"])
+    ctx.search(); o.stage("neighbour")
+    cg, ig, dg, *_ = ctx.neighbours()
+    co, io, do, *_ = o.neighbours(p.kmax)
+    np.testing.assert_array_equal(cg, co)
+    m = np.arange(p.kmax)[None, :] < co[:, None]
+    np.testing.assert_array_equal(ig[m], io[m])
+    np.testing.assert_array_equal(dg[m], do[m])
+    ctx.porosity(); o.stage("effpor")
+    _cmp(ctx.download(), o.get(), ["porosity", "rho", "resx"], 1e-12)
+    ctx.eddy(); o.stage("eddyvis")
+    _cmp(ctx.download(), o.get(), ["nut", "tke"], 1e-10)
+    ctx.int_vel(); o.stage("int_vel")
+    _cmp(ctx.download(), o.get(), ["vxs", "vys", "varts"], 1e-11)
+    ctx.ppe_assemble(); o.stage("ppe_assemble")
+    dg, og, bg = ctx.matrix()
+    do_, oo, bo = o.matrix(p.kmax)
+    assert relmax(dg, do_) < 1e-13
+    assert relmax(og[m], oo[m]) < 1e-12
+    assert relmax(bg, bo) < 1e-10
+    ctx.ppe_solve(); o.stage("ppe_solve")
+    g, r = ctx.download(), o.get()
+    assert relL2(g["p"], r["p"]) < 1e-9
+    assert ctx.info()["ppe_relres"] <= 1e-12   # true residual after a 1e-13 recurrence stop
+    ctx.comp_vel(); o.stage("comp_vel")
+    _cmp(ctx.download(), o.get(), ["vx", "vy", "vel"], 1e-8)
+    ctx.comp_pos(); o.stage("comp_pos")
+    g, r = ctx.download(), o.get()
+    assert np.max(np.abs(g["x"] - r["x"])) < 1e-13
+    ctx.cellshift(True); o.stage("cellshiftalt")
+    ctx.search(); o.stage("neighbour")
+    ctx.free_surface(); o.stage("freesurf")
+    g, r = ctx.download(), o.get()
+    np.testing.assert_array_equal(g["pid"], r["pid"])
+    np.testing.assert_array_equal(g["flags"], r["flags"])
+    ctx.porosity(); o.stage("effpor")
+    ctx.shift(); o.stage("opt2_shift")
+    g, r = ctx.download(), o.get()
+    assert np.max(np.abs(g["x"] - r["x"])) < 1e-12
+    _cmp(g, r, ["vx", "vy"], 1e-8)
+    ctx.density_update(); o.stage("densityupdate")
+    _cmp(ctx.download(), o.get(), ["oden", "mass", "rho"], 1e-14)
+    ctx.timestep(); o.stage("timestep")
+    gi, oi = ctx.info(), o.info()
+    assert gi["umax"] == pytest.approx(oi["umax"], rel=1e-9)
+    assert gi["numax"] == pytest.approx(oi["numax"], rel=1e-9)
+    assert gi["solsteps"] == oi["solsteps"]
+
+
+def test_ghost_row_leftover_entry(api, oracle):
+    p, st = ghost_row_scene()
+    ctx = api.Context([p], [st], [None])
+    o = oracle.Oracle(p, st, None)
+    for a, b in (("search", "neighbour"), ("porosity", "effpor"), ("int_vel", "int_vel"),
+                 ("ppe_assemble", "ppe_assemble")):
+        ctx.stage(a)
+        o.stage(b)
+    dg, og, bg = ctx.matrix()
+    do_, oo, bo = o.matrix(p.kmax)
+    tid = ctx.download()["tid"]
+    # the extra entry adds 1/dia (dia < 0 for these rows) to the unit diagonal
+    quirk = do_ != 1.0
+    assert quirk.any() and np.all(tid[quirk] == 2)
+    np.testing.assert_array_equal(dg != 1.0, quirk)
+    assert relmax(dg, do_) < 1e-14
+
+
+def test_full_step_parity(api, oracle):
+    p, ctx, o = _pair(api, oracle, dx=0.02)
+    ctx.prime()
+    o.stage("prime")
+    for k in range(5):
+        ctx.step(1)
+        o.step(1)
+        g, r = ctx.download(), o.get()
+        np.testing.assert_array_equal(g["pid"], r["pid"])
+        assert np.max(np.abs(g["x"] - r["x"])) < 1e-11
+        assert relL2(g["p"], r["p"]) < 1e-8
+    assert relL2(g["vx"], r["vx"]) < 1e-8
+    assert relL2(g["con"], r["con"]) < 1e-10
+    assert ctx.info()["err_bits"] == 0
+
+
+def test_lattice_small_parity_and_solve(api, oracle):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    from beachslope_gb300 import scene
+    p, st, gr = scene.lattice_scene(n=64, dx=1e-3, seed=11)
+    p.ppe_tol = 1e-12
+    ctx = api.Context([p], [st], [None])
+    o = oracle.Oracle(p, st, None)
+    for a, b in (("search", "neighbour"), ("porosity", "effpor"), ("int_vel", "int_vel"),
+                 ("ppe_assemble", "ppe_assemble")):
+        ctx.stage(a)
+        o.stage(b)
+    cg, ig, dg, *_ = ctx.neighbours()
+    co, io, do, *_ = o.neighbours(p.kmax)
+    np.testing.assert_array_equal(cg, co)
+    m = np.arange(p.kmax)[None, :] < co[:, None]
+    np.testing.assert_array_equal(ig[m], io[m])
+    np.testing.assert_array_equal(dg[m], do[m])
+    dgm, og, bg = ctx.matrix()
+    d2, oo, b2 = o.matrix(p.kmax)
+    assert relmax(og[m], oo[m]) < 1e-12 and relmax(dgm, d2) < 1e-14
+    # manufactured N(0,1) source, solved on the GPU, checked by a direct solve
+    n = len(cg)
+    b = np.random.default_rng(5).standard_normal(n)
+    ctx.set_rhs(b)
+    ctx.ppe_solve()
+    x = ctx.download()["p"]
+    rows = np.repeat(np.arange(n), cg)
+    A = sp.csr_matrix((og[m], (rows, ig[m])), shape=(n, n)) + sp.diags(dgm)
+    xd = spl.spsolve(A.tocsc(), b)
+    assert relL2(x, xd) < 1e-8
+    assert ctx.info()["ppe_relres"] <= 1e-12
+
+
+def test_lattice_1m_neighbour_sets_exact_and_solve(api):
+    """1000 x 1000 jittered lattice (the standalone search + PPE workload):
+    GPU neighbour sets equal the exact IEEE predicate evaluated by numpy on
+    candidate pairs from a k-d tree; the relation is symmetric; the PPE
+    with an N(0,1) source converges to the true residual 1e-8."""
+    from scipy.spatial import cKDTree
+    from beachslope_gb300 import scene
+    p, st, gr = scene.lattice_scene(n=1000, dx=1e-3)
+    ctx = api.Context([p], [st], [None])
+    ctx.search()
+    s = ctx.download(full=False)
+    cg, ig, dg, *_ = ctx.neighbours()
+    n = len(cg)
+    assert n == len(st["x"])
+    m = np.arange(p.kmax)[None, :] < cg[:, None]
+    gi = np.repeat(np.arange(n, dtype=np.int64), cg)
+    gj = ig[m].astype(np.int64)
+    x, y = s["x"], s["y"]
+    pairs = cKDTree(np.c_[x, y]).query_pairs(2 * p.h * (1 + 1e-6), output_type="ndarray")
+    a, b = pairs[:, 0].astype(np.int64), pairs[:, 1].astype(np.int64)
+    dx_ = x[a] - x[b]
+    dy_ = y[a] - y[b]
+    keep = np.sqrt(dx_ * dx_ + dy_ * dy_) < 2 * p.h
+    a, b = a[keep], b[keep]
+    ref = np.sort(np.concatenate([a * n + b, b * n + a]))
+    got = np.sort(gi * n + gj)
+    assert got.size == ref.size
+    assert np.array_equal(got, ref)
+    # stored distances are the exact IEEE values
+    np.testing.assert_array_equal(dg[m], np.sqrt((x[gi] - x[gj]) ** 2 + (y[gi] - y[gj]) ** 2))
+    ctx.porosity()
+    ctx.int_vel()
+    ctx.ppe_assemble()
+    b = np.random.default_rng(20261203).standard_normal(n)
+    ctx.set_rhs(b)
+    ctx.ppe_solve()
+    inf = ctx.info()
+    assert inf["ppe_relres"] <= 1e-8
+    assert inf["err_bits"] == 0
+
+
+def test_batched_scenes_equal_alone(api):
+    from beachslope_gb300 import scene
+    scenes = [scene.beach_scene(dx=d, A=a) for d, a in ((0.03, 0.05), (0.04, 0.08), (0.05, 0.03))]
+    P = [s[0] for s in scenes]
+    S = [s[1] for s in scenes]
+    G = [s[2] for s in scenes]
+    batch = api.Context(P, S, G)
+    batch.prime()
+    batch.step(3)
+    for k in range(3):
+        alone = api.Context([P[k]], [S[k]], [G[k]])
+        alone.prime()
+        alone.step(3)
+        a, b = alone.download(), batch.download(k)
+        for f in ("x", "y", "vx", "vy", "p", "con"):
+            assert np.array_equal(a[f], b[f]), f
+        assert alone.info()["ppe_iters"] == batch.info(k)["ppe_iters"]
+
+
+def test_error_paths(api):
+    from beachslope_gb300 import abi, scene
+    # neighbour capacity overflow is reported, not written past the list
+    p, st, gr = scene.beach_scene(dx=0.04)
+    p.kmax = 8
+    ctx = api.Context([p], [st], [gr])
+    ctx.search()
+    assert ctx.info()["err_bits"] & 0x01
+    c, *_ = ctx.neighbours()
+    assert c.max() == 8
+    # a particle outside the interior cell grid is rejected at upload
+    p, st, gr = scene.beach_scene(dx=0.04)
+    st["x"][0] = -1.0
+    with pytest.raises(api.BeachSlopeError):
+        api.Context([p], [st], [gr])
+    # an isolated fluid particle: zero PPE diagonal (isph.f90:436) is flagged
+    p, st, gr = scene.beach_scene(dx=0.04)
+    f = np.where(st["tid"] == 3)[0][0]
+    st["x"][f] = 3.9
+    st["y"][f] = 0.55
+    ctx = api.Context([p], [st], [gr])
+    ctx.search()
+    ctx.porosity()
+    ctx.int_vel()
+    ctx.ppe_assemble()
+    assert ctx.info()["err_bits"] & 0x02

@@ -1,0 +1,102 @@
+"""CPU tests of the host side: the C-ABI library loads and exports every
+symbol include/beachslope.h declares, the ctypes mirror matches the C
+struct layouts, and the synthetic scene generators have the named shapes.
+No GPU compute is called here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "beachslope.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(bs_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from beachslope_gb300 import build
+    lib_path = build.build_library()
+    lib = C.CDLL(lib_path)
+    syms = declared_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_struct_layouts_match_c():
+    from beachslope_gb300 import abi
+    src = r'''
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "beachslope.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(bs_params), sizeof(bs_state), sizeof(bs_grains),
+             sizeof(bs_scene_info), offsetof(bs_params, ppe_tol), offsetof(bs_state, coff),
+             offsetof(bs_scene_info, err_bits));
+      return 0; }
+    '''
+    tmp = os.path.join(ROOT, "_work")
+    os.makedirs(tmp, exist_ok=True)
+    c_file = os.path.join(tmp, "layout_check.c")
+    exe = os.path.join(tmp, "layout_check")
+    with open(c_file, "w") as f:
+        f.write(src)
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), c_file, "-o", exe])
+    vals = list(map(int, subprocess.check_output([exe]).split()))
+    assert vals == [C.sizeof(abi.Params), C.sizeof(abi.State), C.sizeof(abi.Grains), C.sizeof(abi.SceneInfo),
+                    abi.Params.ppe_tol.offset, abi.State.coff.offset, abi.SceneInfo.err_bits.offset]
+
+
+def test_beach_scene_config1_shape():
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.01)
+    fluid = int((st["tid"] == 3).sum())
+    walls = int((st["tid"] != 3).sum())
+    assert 10_000 < fluid < 13_500
+    assert 1_500 < walls < 4_000
+    assert p.h == pytest.approx(0.013) and p.dt == 1e-4 and p.ppe_tol == 1e-8
+    assert p.por == pytest.approx(0.40) and p.d50 == pytest.approx(0.005)
+    assert len(gr["x"]) > 0
+    # three wall layers, the one touching the fluid fixed (tid 1)
+    assert set(np.unique(st["tid"])) == {1, 2, 3}
+    # every particle lies inside the interior cell grid (columns/rows 2..n-1)
+    cw = 4 * p.h
+    assert st["x"].min() > 0 and st["y"].min() > 0
+    assert st["x"].max() < (p.cellx - 2) * cw and st["y"].max() < (p.celly - 2) * cw
+
+
+def test_beach_scene_pore_mass_consistent():
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.02)
+    f = st["tid"] == 3
+    phi = st["rho"][f] / st["oden"][f]
+    # m / rho = dx^2 for every fluid particle (pore fluid carries phi*rho0*dx^2)
+    np.testing.assert_allclose(st["mass"][f] / st["rho"][f], p.dl ** 2, rtol=1e-12)
+    assert phi.min() == pytest.approx(p.por, rel=1e-9) and phi.max() == 1.0
+
+
+def test_lattice_scene_shape():
+    from beachslope_gb300 import scene
+    p, st, gr = scene.lattice_scene(n=50, dx=1e-3)
+    f = st["tid"] == 3
+    assert f.sum() == 2500
+    dx = p.dl
+    X0 = 3.5 * dx
+    i = np.round((st["x"][f] - X0) / dx - 0.5)
+    assert np.max(np.abs(st["x"][f] - (X0 + (i + 0.5) * dx))) <= 0.25 * dx + 1e-15
+
+
+def test_batch_scenes_uneven():
+    from beachslope_gb300 import scene
+    out = scene.batch_scenes(count=4, seed=7, dx_range=(0.02, 0.04))
+    sizes = [len(s[1]["x"]) for s in out]
+    assert len(set(sizes)) > 1
+    slopes = [s[0].dl for s in out]
+    assert all(0.02 <= d <= 0.04 for d in slopes)
