@@ -29,6 +29,7 @@ def _load():
     i32 = C.c_int32
     sig = {
         "bs_params_default": (None, [vp]),
+        "bs_set_device": (C.c_int, [i32]),
         "bs_create": (C.c_int, [i32, vp, vp, vp, C.POINTER(vp)]),
         "bs_destroy": (C.c_int, [vp]),
         "bs_upload": (C.c_int, [vp, i32, vp, vp]),
@@ -143,6 +144,13 @@ class Context:
                                           kx.ctypes.data, ky.ctypes.data), "get_neighbours")
         return counts, idx, dist, kx, ky
 
+    def neighbour_counts(self, s=0):
+        n = self.info(s)["n"]
+        counts = np.zeros(n, np.int32)
+        self._check(lib.bs_get_neighbours(self.h, s, counts.ctypes.data, None, None, None, None),
+                    "get_neighbours")
+        return counts
+
     def matrix(self, s=0):
         n = self.info(s)["n"]
         K = self.params[s].kmax
@@ -207,6 +215,13 @@ for _name in STAGE_FUNCS:
         f.__name__ = nm
         return f
     setattr(Context, _name, _mk(_name))
+
+
+def set_device(device):
+    """Pick the CUDA device for contexts created afterwards (one rank per GPU)."""
+    rc = lib.bs_set_device(int(device))
+    if rc != 0:
+        raise BeachSlopeError(f"bs_set_device({device}) failed ({rc})")
 
 
 def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=abi.STOP_RELRES):

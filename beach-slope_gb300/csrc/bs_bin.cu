@@ -349,16 +349,22 @@ const char* const kernel_names[K_COUNT] = {
     "derive", "velmag", "projection", "mx_init", "mx_it1_spmv", "mx_it2_spmv", "mx_it3_axpy",
     "mx_residual", "mx_convert"};
 
-void timer_collect(KTimer* T) {
+// Accumulate the finished launches of the ring in order; with wait, block on
+// the oldest pending end event (used when the ring is full).
+void timer_collect(KTimer* T, bool wait) {
     if (!T || !T->ready) return;
-    for (int q = 0; q < T->used; ++q) {
+    while (T->tail < T->head) {
+        const int q = (int)(T->tail % (KTimer::NEV / 2));
+        if (wait) cudaEventSynchronize(T->ev[2 * q + 1]);
+        else if (cudaEventQuery(T->ev[2 * q + 1]) != cudaSuccess) break;
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, T->ev[2 * q], T->ev[2 * q + 1]) == cudaSuccess) {
             T->total_ms[T->id_of[q]] += ms;
             T->count[T->id_of[q]] += 1;
         }
+        ++T->tail;
+        wait = false;
     }
-    T->used = 0;
 }
 
 }  // namespace bs

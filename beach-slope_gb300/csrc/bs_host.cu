@@ -122,7 +122,7 @@ int read_solsteps(bs_ctx* ctx) {
     int mx = 1;
     for (int s = 0; s < ctx->nscene; ++s) mx = std::max(mx, ctx->h_pinned[1 + s]);
     ctx->max_solsteps = mx;
-    bs::timer_collect(&ctx->timer);
+    bs::timer_collect(&ctx->timer, false);
     return 0;
 }
 
@@ -173,6 +173,12 @@ void bs_params_default(bs_params* p) {
     p->xlcutoff = -1e300; p->ytcutoff = 1e300;
     p->ppe_tol = 1e-8; p->ppe_maxit = 5000; p->ppe_stop = BS_STOP_RELRES; p->precision = BS_PREC_FP64;
     p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 30;
+}
+
+int bs_set_device(int32_t device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return BS_E_ARG;
+    return cudaSetDevice(device) == cudaSuccess ? BS_OK : BS_E_CUDA;
 }
 
 int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity, const int32_t* grain_capacity,
@@ -820,7 +826,7 @@ int bs_kernel_timing(bs_ctx* ctx, int32_t enable) {
         for (int q = 0; q < bs::KTimer::NEV; ++q) CK(cudaEventCreate(&T.ev[q]));
         T.ready = true;
     }
-    bs::timer_collect(&T);
+    bs::timer_collect(&T, true);
     T.mask = enable == 1 ? ~0ull : (unsigned long long)(uint32_t)enable;
     if (!enable) T.mask = 0;
     for (int k = 0; k < bs::K_COUNT; ++k) {
@@ -832,7 +838,7 @@ int bs_kernel_timing(bs_ctx* ctx, int32_t enable) {
 int bs_kernel_timing_get(bs_ctx* ctx, int32_t idx, const char** name, int32_t* launches, double* total_ms) {
     if (!ctx || idx < 0 || idx >= bs::K_COUNT) return BS_E_ARG;
     CK(cudaStreamSynchronize(ctx->stream));
-    bs::timer_collect(&ctx->timer);
+    bs::timer_collect(&ctx->timer, true);
     if (name) *name = bs::kernel_names[idx];
     if (launches) *launches = (int32_t)ctx->timer.count[idx];
     if (total_ms) *total_ms = ctx->timer.total_ms[idx];

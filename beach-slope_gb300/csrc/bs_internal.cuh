@@ -230,10 +230,10 @@ enum KId {
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
     unsigned long long mask = 0;
-    static const int NEV = 4096;
+    static const int NEV = 8192;   // event pool: NEV/2 launch slots used as a ring
     cudaEvent_t ev[NEV];
     int id_of[NEV / 2];
-    int used = 0;
+    long long head = 0, tail = 0;  // slots [tail, head) are pending
     bool ready = false;
     double total_ms[K_COUNT] = {};
     long long count[K_COUNT] = {};
@@ -246,11 +246,13 @@ struct Launch {
     KTimer* timer;
 };
 // bracket one launch with timer events (no-op unless the id is enabled)
+void timer_collect(KTimer* T, bool wait);
 inline int tbegin(const Launch& L, int id) {
     *L.launches += 1;
     KTimer* T = L.timer;
-    if (!T || !T->ready || !((T->mask >> id) & 1ull) || T->used >= KTimer::NEV / 2) return -1;
-    const int q = T->used++;
+    if (!T || !T->ready || !((T->mask >> id) & 1ull)) return -1;
+    if (T->head - T->tail >= KTimer::NEV / 2) timer_collect(T, true);   // ring full: drain
+    const int q = (int)(T->head++ % (KTimer::NEV / 2));
     T->id_of[q] = id;
     cudaEventRecord(T->ev[2 * q], L.stream);
     return q;
@@ -258,7 +260,7 @@ inline int tbegin(const Launch& L, int id) {
 inline void tend(const Launch& L, int q) {
     if (q >= 0) cudaEventRecord(L.timer->ev[2 * q + 1], L.stream);
 }
-void timer_collect(KTimer* T);
+
 void rebin(const Dev& D, const Launch& L, int projection, int cutoff);
 void search(const Dev& D, const Launch& L, int precision, int do_search, int do_effpor);
 void freesurf(const Dev& D, const Launch& L);

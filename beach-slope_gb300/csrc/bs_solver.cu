@@ -285,6 +285,7 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const
         }
         // the counter copied before this chunk: decide whether to go on
         cudaEventSynchronize(ev);
+        timer_collect(L.timer, false);
         if (*h_nconv >= D.nscene) break;
     }
     q = tbegin(L, K_TRUERES);

@@ -65,15 +65,14 @@ def porosity_field(x, y, grains, h, por):
     if len(grains["x"]) == 0 or len(x) == 0:
         return phi
     from scipy.spatial import cKDTree
-    tree = cKDTree(np.c_[grains["x"], grains["y"]])
+    tg = cKDTree(np.c_[grains["x"], grains["y"]])
+    tf = cKDTree(np.c_[x, y])
+    pairs = tf.sparse_distance_matrix(tg, 2.0 * h, output_type="ndarray")
     vol = grains["mass"] / grains["rho"]
-    sf = np.zeros(len(x))
-    for i, nb in enumerate(tree.query_ball_point(np.c_[x, y], 2.0 * h)):
-        if nb:
-            nb = np.asarray(nb)
-            r = np.hypot(grains["x"][nb] - x[i], grains["y"][nb] - y[i])
-            m = r < 2.0 * h
-            sf[i] = np.sum((1.0 - por) * _wab(r[m], h) * vol[nb][m])
+    fi, gi = pairs["i"], pairs["j"]
+    r = np.hypot(x[fi] - grains["x"][gi], y[fi] - grains["y"][gi])
+    m = r < 2.0 * h
+    sf = np.bincount(fi[m], weights=(1.0 - por) * _wab(r[m], h) * vol[gi[m]], minlength=len(x))
     return 1.0 - np.minimum(sf, 1.0 - por)
 
 

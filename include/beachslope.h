@@ -156,6 +156,10 @@ typedef struct bs_scene_info {
 /* ---- lifetime ------------------------------------------------------------- */
 void bs_params_default(bs_params* p);
 
+/* Select the CUDA device for contexts created afterwards on this host thread
+ * (one process per GPU: call with the local rank before bs_create). */
+int bs_set_device(int32_t device);
+
 /* Create a context for nscenes scenes; params[s] and capacity[s] (max particles)
  * per scene.  Replaces init/memalloc/matrixid (setup.f90:10, memory.f90:10,80). */
 int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
