@@ -85,7 +85,7 @@ def default_params():
     p.precision = PREC_FP64
     p.kmax = 48
     p.mixed_inner_tol = 1e-3
-    p.mixed_max_outer = 30
+    p.mixed_max_outer = 0   # 0: the mixed mode solves the PPE with the FP64 BiCGStab
     return p
 
 

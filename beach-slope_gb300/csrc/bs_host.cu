@@ -152,7 +152,7 @@ int st_solve(bs_ctx* c) {
     bs::Launch L = launch_of(c);
     int maxit = 0;
     for (auto& p : c->prm) maxit = std::max(maxit, (int)p.ppe_maxit);
-    if (c->precision == BS_PREC_MIXED)
+    if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
         bs::solve_mixed(c->D, L, maxit, 8, c->d_nconv, c->h_pinned, c->evsync);
     else
         bs::solve_fp64(c->D, L, maxit, 8, nullptr, c->d_nconv, c->h_pinned, c->evsync);
@@ -172,7 +172,7 @@ void bs_params_default(bs_params* p) {
     p->lamfs = 0.80; p->maxdivr = 2.0; p->csh = 0.50; p->maxshift = 0.1; p->sig1 = 0.20;
     p->xlcutoff = -1e300; p->ytcutoff = 1e300;
     p->ppe_tol = 1e-8; p->ppe_maxit = 5000; p->ppe_stop = BS_STOP_RELRES; p->precision = BS_PREC_FP64;
-    p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 30;
+    p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 0;
 }
 
 int bs_set_device(int32_t device) {
@@ -266,7 +266,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     if (ctx->precision == BS_PREC_MIXED && !rc) {
         float* f;
         rc = dalloc(ctx, &f, E);
-        D.aval_lo = f;
+        D.aval32 = f;
         float** fv[] = {&D.fr, &D.fp, &D.fp2, &D.fv, &D.fv2, &D.fs, &D.ft, &D.fd, &D.frhat};
         for (auto q : fv)
             if (!rc) rc = dalloc(ctx, q, R);
@@ -279,7 +279,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     if (!rc) rc = dalloc(ctx, &dbs, blk);
     if (!rc) rc = dalloc(ctx, &dcs, cell);
     if (!rc) rc = dalloc(ctx, &dbd, nscenes);
-    if (!rc) rc = dalloc(ctx, &ctx->d_nconv, 1);
+    if (!rc) rc = dalloc(ctx, &ctx->d_nconv, 4);   // [0] inner, [1] outer converged-scene counters
     if (rc) {
         int r2 = rc;
         bs_destroy(ctx);
@@ -503,7 +503,7 @@ int bs_scene_info_get(bs_ctx* ctx, int32_t s, bs_scene_info* o) {
     o->n = hd.n;
     o->solsteps = hd.solsteps;
     o->ppe_iters = hd.iters;
-    o->ppe_outer = hd.outer;
+    o->ppe_outer = hd.outer < 0 ? -hd.outer - 1 : hd.outer;
     o->dt = hd.dt;
     o->dtsol = hd.dtsol;
     o->t = hd.t;

@@ -89,7 +89,7 @@ struct Dev {
     void *ndist, *nrinv, *nkx, *nky;   // double (FP64) or float (mixed)
     // PPE
     void* aval;                     // ELL values (double or float hi)
-    float* aval_lo;                 // mixed: lo part of the FP64 value
+    float* aval32;                  // mixed: FP32 copy of the values (inner operator)
     double *adiag, *rhs;
     double *sx, *sr, *srhat, *sp, *sp2, *sv, *sv2, *ss, *st, *sxd;  // solver vectors
     float *fr, *fp, *fp2, *fv, *fv2, *fs, *ft, *fd, *frhat;          // mixed inner vectors
@@ -225,7 +225,8 @@ enum KId {
     K_RANK = 0, K_CELLPREFIX, K_SCANCELLS, K_PERMUTE, K_SEARCH, K_FREESURF, K_EDDY, K_INTVEL,
     K_ASSEMBLE, K_COMPVEL, K_CELLMAX, K_TIMESTEP, K_SHIFT, K_APPLY, K_DISP, K_SCALAR,
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
-    K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_COUNT
+    K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
+    K_MX_UPD, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {

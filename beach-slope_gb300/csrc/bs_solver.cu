@@ -97,26 +97,48 @@ __global__ void k_init64(Dev D, int* nconv) {
     }
 }
 
-// K1: p' = r + beta (p - omega v);  v' = A p';  partial (rhat, v')
-__global__ void k_it1_64(Dev D, const double* __restrict__ p, const double* __restrict__ v, double* pn, double* vn) {
+// KP: p = r + beta (p - omega v)   (streaming; beta = 0 on the first iteration)
+__global__ void k_pupd64(Dev D) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (scene_done(D, s)) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const double beta = D.dyn[s].beta, omega = D.dyn[s].omega;
+    D.sp[r] = D.sr[r] + beta * (D.sp[r] - omega * D.sv[r]);
+}
+
+// y = A u for one row (1 DFMA per nonzero)
+__device__ __forceinline__ double spmv_row64(const Dev& D, const double* __restrict__ u, int r) {
+    const double* __restrict__ A = (const double*)D.aval;
+    const int* __restrict__ idx = D.nidx;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    double acc = D.adiag[r] * u[r];
+    long e = ell(r, 0, kmax);
+    int k = 0;
+    for (; k + 4 <= n; k += 4, e += 128) {   // four independent gathers in flight
+        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32), j2 = __ldg(idx + e + 64), j3 = __ldg(idx + e + 96);
+        const double a0 = __ldg(A + e), a1 = __ldg(A + e + 32), a2 = __ldg(A + e + 64), a3 = __ldg(A + e + 96);
+        const double u0 = u[j0], u1 = u[j1], u2 = u[j2], u3 = u[j3];
+        acc += a0 * u0;
+        acc += a1 * u1;
+        acc += a2 * u2;
+        acc += a3 * u3;
+    }
+    for (; k < n; ++k, e += 32) acc += __ldg(A + e) * u[__ldg(idx + e)];
+    return acc;
+}
+
+// K1: v = A p;  partial (rhat, v);  finisher: alpha
+__global__ void k_it1_64(Dev D) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const double beta = D.dyn[s].beta, omega = D.dyn[s].omega;
     double q[1] = {0.0};
     if (r < P.row0 + D.dyn[s].n) {
-        const double* A = (const double*)D.aval;
-        const double pi = D.sr[r] + beta * (p[r] - omega * v[r]);
-        double acc = D.adiag[r] * pi;
-        const int n = D.ncount[r];
-        for (int k = 0; k < n; ++k) {
-            const long e = ell(r, k, D.kmax);
-            const int j = D.nidx[e];
-            acc += A[e] * (D.sr[j] + beta * (p[j] - omega * v[j]));
-        }
-        pn[r] = pi;
-        vn[r] = acc;
+        const double acc = spmv_row64(D, D.sp, r);
+        D.sv[r] = acc;
         q[0] = D.srhat[r] * acc;
     }
     double tot[1];
@@ -131,26 +153,26 @@ __global__ void k_it1_64(Dev D, const double* __restrict__ p, const double* __re
     }
 }
 
-// K2: s = r - alpha v;  t = A s;  partials (t,s), (t,t)
-__global__ void k_it2_64(Dev D, const double* __restrict__ v) {
+// KS: s = r - alpha v   (streaming)
+__global__ void k_supd64(Dev D) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (scene_done(D, s)) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    D.ss[r] = D.sr[r] - D.dyn[s].alpha * D.sv[r];
+}
+
+// K2: t = A s;  partials (t,s), (t,t);  finisher: omega
+__global__ void k_it2_64(Dev D) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const double alpha = D.dyn[s].alpha;
     double q[2] = {0.0, 0.0};
     if (r < P.row0 + D.dyn[s].n) {
-        const double* A = (const double*)D.aval;
-        const double si = D.sr[r] - alpha * v[r];
-        double acc = D.adiag[r] * si;
-        const int n = D.ncount[r];
-        for (int k = 0; k < n; ++k) {
-            const long e = ell(r, k, D.kmax);
-            const int j = D.nidx[e];
-            acc += A[e] * (D.sr[j] - alpha * v[j]);
-        }
-        D.ss[r] = si;
+        const double acc = spmv_row64(D, D.ss, r);
         D.st[r] = acc;
+        const double si = D.ss[r];
         q[0] = acc * si;
         q[1] = acc * acc;
     }
@@ -162,8 +184,9 @@ __global__ void k_it2_64(Dev D, const double* __restrict__ v) {
     }
 }
 
-// K3: x += alpha p + omega s;  r = s - omega t;  partials (rhat, r), (r,r)
-__global__ void k_it3_64(Dev D, const double* __restrict__ p, int* nconv) {
+// K3: x += alpha p + omega s;  r = s - omega t;  partials (rhat, r), (r,r);
+// finisher: beta, convergence
+__global__ void k_it3_64(Dev D, int* nconv) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -174,7 +197,7 @@ __global__ void k_it3_64(Dev D, const double* __restrict__ p, int* nconv) {
     if (r < P.row0 + D.dyn[s].n) {
         const double si = D.ss[r], ti = D.st[r];
         const double xo = D.p[r];
-        const double xn = xo + alpha * p[r] + omega * si;
+        const double xn = xo + alpha * D.sp[r] + omega * si;
         D.p[r] = xn;
         const double rr = si - omega * ti;
         D.sr[r] = rr;
@@ -223,6 +246,220 @@ __global__ void k_it3_64(Dev D, const double* __restrict__ p, int* nconv) {
     }
 }
 
+// ---------------------------------------------------------------- mixed
+// Outer refinement: r64 = b - A64 x (FP64 matrix, FP64 vectors); the scene
+// is done when ||r64|| <= tol ||b||.  Otherwise the inner FP32 BiCGStab
+// solves A32 d = r64/||r64|| to inner_tol and x += ||r64|| d.
+__global__ void k_mx_res(Dev D, int* nconv) {
+    const int s = D.blk_scene[blockIdx.x];
+    const ScenePar& P = D.par[s];
+    SceneDyn& Y = D.dyn[s];
+    if (Y.outer < 0) return;   // outer-converged
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    double q[2] = {0.0, 0.0};
+    if (r < P.row0 + Y.n) {
+        const double b = D.rhs[r];
+        const double rr = b - spmv_row64(D, D.p, r);
+        D.sxd[r] = rr;
+        q[0] = rr * rr;
+        q[1] = b * b;
+    }
+    double tot[2];
+    if (scene_sum<2>(D, s, q, tot) && threadIdx.x == 0) {
+        Y.rtrue2 = tot[0];
+        Y.bnorm2 = tot[1];
+        Y.relres = (tot[1] > 0.0) ? sqrt(tot[0] / tot[1]) : sqrt(tot[0]);
+        const bool done = (tot[1] == 0.0) || (tot[0] <= P.ppe_tol * P.ppe_tol * tot[1]) || !isfinite(tot[0]);
+        if (!isfinite(tot[0])) set_err(D, s, BS_ERR_NONFINITE);
+        if (done || Y.outer >= P.max_outer) {
+            if (!done) set_err(D, s, BS_ERR_NOT_CONVERGED);
+            Y.outer = -Y.outer - 1;   // mark outer-converged, keep the count
+            Y.converged = 1;
+            atomicAdd(nconv + 1, 1);
+        } else {
+            Y.rnorm2 = tot[0];
+            Y.converged = 0;
+            Y.outer += 1;
+        }
+    }
+}
+
+// inner init: r = r64 / ||r64|| in FP32, rhat = r, p = v = d = 0
+__global__ void k_mx_init(Dev D, int* nconv) {
+    const int s = D.blk_scene[blockIdx.x];
+    const SceneDyn& Y0 = D.dyn[s];
+    if (Y0.outer < 0) return;
+    const ScenePar& P = D.par[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const double scale = 1.0 / sqrt(Y0.rnorm2);
+    double q[1] = {0.0};
+    if (r < P.row0 + Y0.n) {
+        const float rf = (float)(D.sxd[r] * scale);
+        D.fr[r] = rf;
+        D.frhat[r] = rf;
+        D.fp[r] = 0.0f;
+        D.fv[r] = 0.0f;
+        D.fd[r] = 0.0f;
+        q[0] = (double)rf * rf;
+    }
+    double tot[1];
+    if (scene_sum<1>(D, s, q, tot) && threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        Y.rho_old = tot[0];
+        Y.part_tmp = tot[0];   // inner ||r0||^2
+        Y.alpha = 1.0;
+        Y.omega = 1.0;
+        Y.beta = 0.0;
+        Y.breakdown = 0;
+        if (tot[0] == 0.0) {
+            Y.converged = 1;
+            atomicAdd(nconv, 1);
+        }
+    }
+}
+
+__device__ __forceinline__ bool inner_done(const Dev& D, int s) {
+    return D.dyn[s].outer < 0 || D.dyn[s].converged != 0;
+}
+
+// FP32 row of A32 applied to u_j = a_j + c (b_j - e g_j) evaluated on the fly
+template <int MODE>
+__device__ __forceinline__ float spmv_row32(const Dev& D, const float* __restrict__ a, const float* __restrict__ b,
+                                            const float* __restrict__ g, float c, float e2, int r, float& own) {
+    const float* __restrict__ A = (const float*)D.aval32;   // FP32 values (hi part)
+    const int* __restrict__ idx = D.nidx;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    auto val = [&](int j) -> float {
+        if (MODE == 0) return a[j] + c * (b[j] - e2 * g[j]);   // p = r + beta (p - omega v)
+        return a[j] - c * b[j];                              // s = r - alpha v
+    };
+    own = val(r);
+    float acc = (float)D.adiag[r] * own;
+    long e = ell(r, 0, kmax);
+    int k = 0;
+    for (; k + 4 <= n; k += 4, e += 128) {
+        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32), j2 = __ldg(idx + e + 64), j3 = __ldg(idx + e + 96);
+        const float a0 = __ldg(A + e), a1 = __ldg(A + e + 32), a2 = __ldg(A + e + 64), a3 = __ldg(A + e + 96);
+        const float u0 = val(j0), u1 = val(j1), u2 = val(j2), u3 = val(j3);
+        acc = fmaf(a0, u0, acc);
+        acc = fmaf(a1, u1, acc);
+        acc = fmaf(a2, u2, acc);
+        acc = fmaf(a3, u3, acc);
+    }
+    for (; k < n; ++k, e += 32) acc = fmaf(__ldg(A + e), val(__ldg(idx + e)), acc);
+    return acc;
+}
+
+__global__ void k_mx_it1(Dev D, const float* __restrict__ p, const float* __restrict__ v, float* pn, float* vn) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (inner_done(D, s)) return;
+    const ScenePar& P = D.par[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const float beta = (float)D.dyn[s].beta, omega = (float)D.dyn[s].omega;
+    double q[1] = {0.0};
+    if (r < P.row0 + D.dyn[s].n) {
+        float pi;
+        const float acc = spmv_row32<0>(D, D.fr, p, v, beta, omega, r, pi);
+        pn[r] = pi;
+        vn[r] = acc;
+        q[0] = (double)D.frhat[r] * acc;
+    }
+    double tot[1];
+    if (scene_sum<1>(D, s, q, tot) && threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        if (tot[0] == 0.0 || !isfinite(tot[0])) {
+            Y.breakdown = 1;
+            Y.alpha = 0.0;
+        } else {
+            Y.alpha = Y.rho_old / tot[0];
+        }
+    }
+}
+
+__global__ void k_mx_it2(Dev D, const float* __restrict__ v) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (inner_done(D, s)) return;
+    const ScenePar& P = D.par[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const float alpha = (float)D.dyn[s].alpha;
+    double q[2] = {0.0, 0.0};
+    if (r < P.row0 + D.dyn[s].n) {
+        float si;
+        const float acc = spmv_row32<1>(D, D.fr, v, v, alpha, 0.0f, r, si);
+        D.fs[r] = si;
+        D.ft[r] = acc;
+        q[0] = (double)acc * si;
+        q[1] = (double)acc * acc;
+    }
+    double tot[2];
+    if (scene_sum<2>(D, s, q, tot) && threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        Y.omega = (tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
+        if (tot[1] == 0.0) Y.breakdown = 1;
+    }
+}
+
+__global__ void k_mx_it3(Dev D, const float* __restrict__ p, int* nconv) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (inner_done(D, s)) return;
+    const ScenePar& P = D.par[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const float alpha = (float)D.dyn[s].alpha, omega = (float)D.dyn[s].omega;
+    double q[2] = {0.0, 0.0};
+    if (r < P.row0 + D.dyn[s].n) {
+        const float si = D.fs[r], ti = D.ft[r];
+        D.fd[r] = D.fd[r] + alpha * p[r] + omega * si;
+        const float rr = si - omega * ti;
+        D.fr[r] = rr;
+        q[0] = (double)D.frhat[r] * rr;
+        q[1] = (double)rr * rr;
+    }
+    double tot[2];
+    if (scene_sum<2>(D, s, q, tot) && threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        const double rho_new = tot[0];
+        Y.beta = (rho_new / Y.rho_old) * ((double)alpha / (double)omega);
+        Y.rho_old = rho_new;
+        Y.iters += 1;
+        bool conv = tot[1] <= P.inner_tol * P.inner_tol * Y.part_tmp;
+        if (!isfinite(tot[1]) || Y.breakdown) conv = true;
+        if (Y.iters >= P.maxit) conv = true;
+        if (conv) {
+            Y.converged = 1;
+            atomicAdd(nconv, 1);
+        }
+    }
+}
+
+// x += ||r64|| d
+__global__ void k_mx_update(Dev D) {
+    const int s = D.blk_scene[blockIdx.x];
+    const SceneDyn& Y = D.dyn[s];
+    if (Y.outer < 0) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + Y.n) return;
+    D.p[r] = D.p[r] + sqrt(Y.rnorm2) * (double)D.fd[r];
+}
+
+// FP32 copy of the assembled FP64 matrix values (inner operator)
+__global__ void k_mx_convert(Dev D) {
+    const int s = D.blk_scene[blockIdx.x];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == D.par[s].row0) {
+        D.dyn[s].outer = 0;
+        D.dyn[s].iters = 0;
+    }
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const double* A = (const double*)D.aval;
+    float* F = D.aval32;
+    const int n = D.ncount[r];
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, D.kmax);
+        F[e] = (float)A[e];
+    }
+}
+
 // true FP64 residual ||b - A x|| / ||b|| for every scene (no early exit)
 __global__ void k_true_res64(Dev D) {
     const int s = D.blk_scene[blockIdx.x];
@@ -255,35 +492,35 @@ __global__ void k_true_res64(Dev D) {
 namespace bs {
 
 // Host driver of the FP64 solve.  Checks the converged-scene counter every
-// `check_every` iterations (one event sync), so the host never waits per
-// iteration.
+// `check_every` iterations with one event sync, one chunk behind the launches
+// so the GPU never idles on the host.
 void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const int*, int* d_nconv,
                 int* h_nconv, cudaEvent_t ev) {
     cudaMemsetAsync(d_nconv, 0, sizeof(int), L.stream);
     int q = tbegin(L, K_BICG_INIT);
     k_init64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
     tend(L, q);
-    double *p = D.sp, *v = D.sv, *p2 = D.sp2, *v2 = D.sv2;
     int it = 0;
     while (it < maxit) {
         cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
         cudaEventRecord(ev, L.stream);
-        const int chunk = check_every;
-        for (int c = 0; c < chunk && it < maxit; ++c, ++it) {
+        for (int c = 0; c < check_every && it < maxit; ++c, ++it) {
+            q = tbegin(L, K_BICG_PUPD);
+            k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            tend(L, q);
             q = tbegin(L, K_BICG_IT1);
-            k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p, v, p2, v2);
+            k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            tend(L, q);
+            q = tbegin(L, K_BICG_SUPD);
+            k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
             tend(L, q);
             q = tbegin(L, K_BICG_IT2);
-            k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, v2);
+            k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
             tend(L, q);
             q = tbegin(L, K_BICG_IT3);
-            k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p2, d_nconv);
+            k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
             tend(L, q);
-            double* t;
-            t = p; p = p2; p2 = t;
-            t = v; v = v2; v2 = t;
         }
-        // the counter copied before this chunk: decide whether to go on
         cudaEventSynchronize(ev);
         timer_collect(L.timer, false);
         if (*h_nconv >= D.nscene) break;
@@ -293,10 +530,57 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const
     tend(L, q);
 }
 
+// Mixed solve: outer FP64 refinement around an FP32 BiCGStab.
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_nconv, int* h_nconv,
                  cudaEvent_t ev) {
-    // mixed precision solver: added with the FP32 inner iteration
-    solve_fp64(D, L, maxit, check_every, nullptr, d_nconv, h_nconv, ev);
+    int q = tbegin(L, K_MX_CONV);
+    k_mx_convert<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    tend(L, q);
+    cudaMemsetAsync(d_nconv, 0, 2 * sizeof(int), L.stream);
+    int max_outer = 0;
+    cudaMemcpyAsync(h_nconv + 2, &D.par[0].max_outer, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+    cudaStreamSynchronize(L.stream);
+    max_outer = h_nconv[2];
+    for (int outer = 0; outer <= max_outer; ++outer) {
+        float *p = D.fp, *v = D.fv, *p2 = D.fp2, *v2 = D.fv2;   // k_mx_init zeroes fp, fv
+        q = tbegin(L, K_MX_RES);
+        k_mx_res<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+        tend(L, q);
+        cudaMemcpyAsync(h_nconv, d_nconv, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+        cudaStreamSynchronize(L.stream);
+        if (h_nconv[1] >= D.nscene) break;
+        cudaMemsetAsync(d_nconv, 0, sizeof(int), L.stream);
+        // inner-converged counter starts with the outer-converged scenes
+        cudaMemcpyAsync(d_nconv, d_nconv + 1, sizeof(int), cudaMemcpyDeviceToDevice, L.stream);
+        q = tbegin(L, K_MX_INIT);
+        k_mx_init<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+        tend(L, q);
+        int it = 0;
+        while (it < maxit) {
+            cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+            cudaEventRecord(ev, L.stream);
+            for (int c = 0; c < check_every && it < maxit; ++c, ++it) {
+                q = tbegin(L, K_MX_IT1);
+                k_mx_it1<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p, v, p2, v2);
+                tend(L, q);
+                q = tbegin(L, K_MX_IT2);
+                k_mx_it2<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, v2);
+                tend(L, q);
+                q = tbegin(L, K_MX_IT3);
+                k_mx_it3<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p2, d_nconv);
+                tend(L, q);
+                float* t;
+                t = p; p = p2; p2 = t;
+                t = v; v = v2; v2 = t;
+            }
+            cudaEventSynchronize(ev);
+            timer_collect(L.timer, false);
+            if (*h_nconv >= D.nscene) break;
+        }
+        q = tbegin(L, K_MX_UPD);
+        k_mx_update<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        tend(L, q);
+    }
 }
 
 }  // namespace bs

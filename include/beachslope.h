@@ -110,7 +110,8 @@ typedef struct bs_params {
     int32_t ppe_stop;  /* BS_STOP_*                                                   */
     int32_t precision; /* BS_PREC_*                                                   */
     int32_t kmax;      /* neighbour-list capacity per particle (<= 64)                */
-    /* mixed precision: inner FP32 BiCGStab tolerance per refinement sweep */
+    /* mixed precision: FP32 inner BiCGStab tolerance per refinement sweep and
+     * the number of FP64 refinement sweeps (0: solve with the FP64 BiCGStab) */
     double mixed_inner_tol;
     int32_t mixed_max_outer;
     int32_t pad0;
