@@ -45,11 +45,11 @@ class Params(C.Structure):
         ("lamfs", _d), ("maxdivr", _d), ("csh", _d), ("maxshift", _d), ("sig1", _d),
         ("xlcutoff", _d), ("ytcutoff", _d),
         ("ppe_tol", _d), ("ppe_maxit", _i), ("ppe_stop", _i), ("precision", _i),
-        ("kmax", _i), ("mixed_inner_tol", _d), ("mixed_max_outer", _i), ("pad0", _i),
+        ("kmax", _i), ("mixed_inner_tol", _d), ("mixed_max_outer", _i), ("ppe_precond", _i),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad0"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def default_params():
@@ -86,6 +86,7 @@ def default_params():
     p.kmax = 48
     p.mixed_inner_tol = 1e-3
     p.mixed_max_outer = 0   # 0: the mixed mode solves the PPE with the FP64 BiCGStab
+    p.ppe_precond = 1       # multigrid V-cycle preconditioner
     return p
 
 

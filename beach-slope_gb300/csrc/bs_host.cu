@@ -155,7 +155,8 @@ int st_solve(bs_ctx* c) {
     if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
         bs::solve_mixed(c->D, L, maxit, 8, c->d_nconv, c->h_pinned, c->evsync);
     else
-        bs::solve_fp64(c->D, L, maxit, 8, nullptr, c->d_nconv, c->h_pinned, c->evsync);
+        bs::solve_fp64(c->D, L, maxit, c->prm[0].ppe_precond ? 4 : 8, c->prm[0].ppe_precond, c->precision,
+                       c->d_nconv, c->h_pinned, c->evsync);
     return 0;
 }
 
@@ -270,6 +271,58 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         float** fv[] = {&D.fr, &D.fp, &D.fp2, &D.fv, &D.fv2, &D.fs, &D.ft, &D.fd, &D.frhat};
         for (auto q : fv)
             if (!rc) rc = dalloc(ctx, q, R);
+    }
+    // multigrid levels: level 1 = the cell grid of every scene, then 2x2
+    // coarsening until every scene has at most 256 coarse cells
+    if (!rc) {
+        MgDev& M = D.mg;
+        std::memset(&M, 0, sizeof(M));
+        M.omega = 0.7;
+        M.cscale = 1.0;
+        M.coarse_sweeps = 40;
+        std::vector<int> nx(nscenes), ny(nscenes);
+        for (int s = 0; s < nscenes; ++s) { nx[s] = params[s].cellx; ny[s] = params[s].celly; }
+        const size_t tw = (ctx->precision == BS_PREC_MIXED) ? sizeof(float) : sizeof(double);
+        int l = 1;
+        while (true) {
+            std::vector<int> off(nscenes), sc;
+            int tot = 0, mx = 0;
+            for (int s = 0; s < nscenes; ++s) {
+                off[s] = tot;
+                tot += nx[s] * ny[s];
+                mx = std::max(mx, nx[s] * ny[s]);
+                for (int q = 0; q < nx[s] * ny[s]; ++q) sc.push_back(s);
+            }
+            M.n[l] = tot;
+            int *doff, *dnx, *dny, *dsc;
+            char *A, *dinv, *rr, *zz;
+            if (!rc) rc = dalloc(ctx, &doff, nscenes);
+            if (!rc) rc = dalloc(ctx, &dnx, nscenes);
+            if (!rc) rc = dalloc(ctx, &dny, nscenes);
+            if (!rc) rc = dalloc(ctx, &dsc, tot);
+            if (!rc) rc = dalloc(ctx, &A, 9 * (size_t)tot * tw);
+            if (!rc) rc = dalloc(ctx, &dinv, (size_t)tot * tw);
+            if (!rc) rc = dalloc(ctx, &rr, (size_t)tot * tw);
+            if (!rc) rc = dalloc(ctx, &zz, (size_t)tot * tw);
+            if (rc) break;
+            cudaMemcpy(doff, off.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
+            cudaMemcpy(dnx, nx.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
+            cudaMemcpy(dny, ny.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
+            cudaMemcpy(dsc, sc.data(), sizeof(int) * tot, cudaMemcpyHostToDevice);
+            M.off[l] = doff; M.nx[l] = dnx; M.ny[l] = dny; M.scene_of[l] = dsc;
+            M.A[l] = A; M.dinv[l] = dinv; M.r[l] = rr; M.z[l] = zz;
+            M.nlev = l;
+            M.coarse_max = mx;
+            if (mx <= 256 || l == BS_MG_MAXL) break;
+            for (int s = 0; s < nscenes; ++s) { nx[s] = (nx[s] + 1) / 2; ny[s] = (ny[s] + 1) / 2; }
+            ++l;
+        }
+        char* d0;
+        if (!rc) rc = dalloc(ctx, &d0, R * tw);
+        if (!rc) M.dinv0 = d0;
+    }
+    if (!rc && ctx->precision != BS_PREC_MIXED) {   // FP32 matrix copy for an FP32 V-cycle is mixed-only
+        D.aval32 = nullptr;
     }
     ScenePar* dpar = nullptr;
     SceneDyn* ddyn = nullptr;
@@ -793,7 +846,7 @@ int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const
     CK(cudaMemcpy(D.nidx, idx.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(D.aval, aval.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
     ctx->assembled = true;
-    bs::solve_fp64(D, launch_of(ctx), maxit, 1, nullptr, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
+    bs::solve_fp64(D, launch_of(ctx), maxit, 1, 0, BS_PREC_FP64, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
     rc = bs_sync(ctx);
     if (!rc) {
         CK(cudaMemcpy(x, D.p, sizeof(double) * n, cudaMemcpyDeviceToHost));

@@ -61,6 +61,26 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     double part_tmp;
 };
 
+// Aggregation multigrid over the cell grid (level 1 = the cells, one
+// aggregate per cell; level l+1 = 2x2 boxes of level l), 9-point Galerkin
+// stencils stored per offset k = (dj+1)*3 + (di+1): A[k*n + c].
+#define BS_MG_MAXL 16
+struct MgDev {
+    int nlev;                         // coarsest level index (levels 1..nlev)
+    int n[BS_MG_MAXL + 1];            // cells of level l over all scenes
+    void* A[BS_MG_MAXL + 1];          // 9*n[l] (double or float)
+    void* dinv[BS_MG_MAXL + 1];       // 1/diag (0 for empty rows)
+    void* r[BS_MG_MAXL + 1];
+    void* z[BS_MG_MAXL + 1];
+    const int* scene_of[BS_MG_MAXL + 1];
+    const int* off[BS_MG_MAXL + 1];   // per scene: first cell of the scene in level l
+    const int* nx[BS_MG_MAXL + 1];    // per scene
+    const int* ny[BS_MG_MAXL + 1];
+    void* dinv0;                      // level 0: 1/adiag per particle row
+    double omega, cscale;
+    int coarse_sweeps, coarse_max;
+};
+
 // device pointers of one context (passed by value to kernels)
 struct Dev {
     // particle fields (current buffer)
@@ -112,6 +132,7 @@ struct Dev {
     int ncell_total, nrow_total, nblk_total, nscene;
     int kmax;
     unsigned* err_word;
+    MgDev mg;
 };
 
 // ------------------------------------------------------------ helpers
@@ -226,7 +247,7 @@ enum KId {
     K_ASSEMBLE, K_COMPVEL, K_CELLMAX, K_TIMESTEP, K_SHIFT, K_APPLY, K_DISP, K_SCALAR,
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
-    K_MX_UPD, K_COUNT
+    K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -276,8 +297,11 @@ void scalar(const Dev& D, const Launch& L, int precision, int substep);
 void advance_time(const Dev& D, const Launch& L);
 void derive_fields(const Dev& D, const Launch& L);
 // solver
-void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const int* h_conv_flag,
+void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_precision,
                 int* d_all_conv, int* h_all_conv_pinned, cudaEvent_t ev);
+// multigrid preconditioner (bs_mg.cu)
+void mg_setup(const Dev& D, const Launch& L, int mg_precision);
+void mg_apply(const Dev& D, const Launch& L, int mg_precision, const double* in, double* out);
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_all_conv,
                  int* h_all_conv_pinned, cudaEvent_t ev);
 }  // namespace bs

@@ -129,15 +129,16 @@ __device__ __forceinline__ double spmv_row64(const Dev& D, const double* __restr
     return acc;
 }
 
-// K1: v = A p;  partial (rhat, v);  finisher: alpha
-__global__ void k_it1_64(Dev D) {
+// K1: v = A u (u = p, or M^-1 p when preconditioned);  partial (rhat, v);
+// finisher: alpha
+__global__ void k_it1_64(Dev D, const double* __restrict__ u) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     double q[1] = {0.0};
     if (r < P.row0 + D.dyn[s].n) {
-        const double acc = spmv_row64(D, D.sp, r);
+        const double acc = spmv_row64(D, u, r);
         D.sv[r] = acc;
         q[0] = D.srhat[r] * acc;
     }
@@ -162,15 +163,15 @@ __global__ void k_supd64(Dev D) {
     D.ss[r] = D.sr[r] - D.dyn[s].alpha * D.sv[r];
 }
 
-// K2: t = A s;  partials (t,s), (t,t);  finisher: omega
-__global__ void k_it2_64(Dev D) {
+// K2: t = A u (u = s, or M^-1 s);  partials (t,s), (t,t);  finisher: omega
+__global__ void k_it2_64(Dev D, const double* __restrict__ u) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     double q[2] = {0.0, 0.0};
     if (r < P.row0 + D.dyn[s].n) {
-        const double acc = spmv_row64(D, D.ss, r);
+        const double acc = spmv_row64(D, u, r);
         D.st[r] = acc;
         const double si = D.ss[r];
         q[0] = acc * si;
@@ -184,9 +185,9 @@ __global__ void k_it2_64(Dev D) {
     }
 }
 
-// K3: x += alpha p + omega s;  r = s - omega t;  partials (rhat, r), (r,r);
+// K3: x += alpha pu + omega su;  r = s - omega t;  partials (rhat, r), (r,r);
 // finisher: beta, convergence
-__global__ void k_it3_64(Dev D, int* nconv) {
+__global__ void k_it3_64(Dev D, const double* __restrict__ pu, const double* __restrict__ su, int* nconv) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -197,7 +198,7 @@ __global__ void k_it3_64(Dev D, int* nconv) {
     if (r < P.row0 + D.dyn[s].n) {
         const double si = D.ss[r], ti = D.st[r];
         const double xo = D.p[r];
-        const double xn = xo + alpha * D.sp[r] + omega * si;
+        const double xn = xo + alpha * pu[r] + omega * su[r];
         D.p[r] = xn;
         const double rr = si - omega * ti;
         D.sr[r] = rr;
@@ -494,10 +495,21 @@ namespace bs {
 // Host driver of the FP64 solve.  Checks the converged-scene counter every
 // `check_every` iterations with one event sync, one chunk behind the launches
 // so the GPU never idles on the host.
-void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const int*, int* d_nconv,
+void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec, int* d_nconv,
                 int* h_nconv, cudaEvent_t ev) {
+    int q;
+    if (precond) {
+        if (mg_prec == BS_PREC_MIXED) {
+            q = tbegin(L, K_MX_CONV);
+            k_mx_convert<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            tend(L, q);
+        }
+        mg_setup(D, L, mg_prec);
+    }
+    const double* pu = precond ? D.sp2 : D.sp;   // M^-1 p
+    const double* su = precond ? D.sv2 : D.ss;   // M^-1 s
     cudaMemsetAsync(d_nconv, 0, sizeof(int), L.stream);
-    int q = tbegin(L, K_BICG_INIT);
+    q = tbegin(L, K_BICG_INIT);
     k_init64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
     tend(L, q);
     int it = 0;
@@ -508,17 +520,19 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const
             q = tbegin(L, K_BICG_PUPD);
             k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
             tend(L, q);
+            if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
             q = tbegin(L, K_BICG_IT1);
-            k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu);
             tend(L, q);
             q = tbegin(L, K_BICG_SUPD);
             k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
             tend(L, q);
+            if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
             q = tbegin(L, K_BICG_IT2);
-            k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, su);
             tend(L, q);
             q = tbegin(L, K_BICG_IT3);
-            k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+            k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu, su, d_nconv);
             tend(L, q);
         }
         cudaEventSynchronize(ev);
@@ -533,6 +547,8 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, const
 // Mixed solve: outer FP64 refinement around an FP32 BiCGStab.
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_nconv, int* h_nconv,
                  cudaEvent_t ev) {
+    // FP32-inner iterative refinement (kept for systems whose condition number
+    // times the FP32 unit round-off is well below one)
     int q = tbegin(L, K_MX_CONV);
     k_mx_convert<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
     tend(L, q);

@@ -114,7 +114,9 @@ typedef struct bs_params {
      * the number of FP64 refinement sweeps (0: solve with the FP64 BiCGStab) */
     double mixed_inner_tol;
     int32_t mixed_max_outer;
-    int32_t pad0;
+    /* PPE preconditioner: 0 none (the reference's plain BiCGStab), 1 cell-grid
+     * aggregation multigrid V-cycle (FP64 in BS_PREC_FP64, FP32 in BS_PREC_MIXED) */
+    int32_t ppe_precond;
 } bs_params;
 
 /*
