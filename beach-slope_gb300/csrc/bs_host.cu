@@ -280,18 +280,36 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.omega = 0.7;
         M.cscale = 1.0;
         M.coarse_sweeps = 40;
-        std::vector<int> nx(nscenes), ny(nscenes);
-        for (int s = 0; s < nscenes; ++s) { nx[s] = params[s].cellx; ny[s] = params[s].celly; }
+        // each scene coarsens on its own until it has at most 256 cells, so
+        // its V-cycle is the same alone and inside any batch
+        std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
+        int L = 1;
+        for (int s = 0; s < nscenes; ++s) {
+            int nx = params[s].cellx, ny = params[s].celly;
+            dims[s].push_back({nx, ny});
+            while (nx * ny > 256 && (int)dims[s].size() < BS_MG_MAXL) {
+                nx = (nx + 1) / 2;
+                ny = (ny + 1) / 2;
+                dims[s].push_back({nx, ny});
+            }
+            ctx->hpar[s].mg_lev = (int)dims[s].size();
+            L = std::max(L, (int)dims[s].size());
+        }
         const size_t tw = (ctx->precision == BS_PREC_MIXED) ? sizeof(float) : sizeof(double);
-        int l = 1;
-        while (true) {
-            std::vector<int> off(nscenes), sc;
-            int tot = 0, mx = 0;
+        M.nlev = L;
+        M.coarse_max = 1;
+        for (int s = 0; s < nscenes; ++s)
+            M.coarse_max = std::max(M.coarse_max, dims[s].back().first * dims[s].back().second);
+        for (int l = 1; l <= L && !rc; ++l) {
+            std::vector<int> off(nscenes, -1), nxv(nscenes, 0), nyv(nscenes, 0), sc;
+            int tot = 0;
             for (int s = 0; s < nscenes; ++s) {
+                if ((int)dims[s].size() < l) continue;
                 off[s] = tot;
-                tot += nx[s] * ny[s];
-                mx = std::max(mx, nx[s] * ny[s]);
-                for (int q = 0; q < nx[s] * ny[s]; ++q) sc.push_back(s);
+                nxv[s] = dims[s][l - 1].first;
+                nyv[s] = dims[s][l - 1].second;
+                tot += nxv[s] * nyv[s];
+                for (int q = 0; q < nxv[s] * nyv[s]; ++q) sc.push_back(s);
             }
             M.n[l] = tot;
             int *doff, *dnx, *dny, *dsc;
@@ -306,16 +324,11 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
             if (!rc) rc = dalloc(ctx, &zz, (size_t)tot * tw);
             if (rc) break;
             cudaMemcpy(doff, off.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
-            cudaMemcpy(dnx, nx.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
-            cudaMemcpy(dny, ny.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
-            cudaMemcpy(dsc, sc.data(), sizeof(int) * tot, cudaMemcpyHostToDevice);
+            cudaMemcpy(dnx, nxv.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
+            cudaMemcpy(dny, nyv.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice);
+            if (tot) cudaMemcpy(dsc, sc.data(), sizeof(int) * tot, cudaMemcpyHostToDevice);
             M.off[l] = doff; M.nx[l] = dnx; M.ny[l] = dny; M.scene_of[l] = dsc;
             M.A[l] = A; M.dinv[l] = dinv; M.r[l] = rr; M.z[l] = zz;
-            M.nlev = l;
-            M.coarse_max = mx;
-            if (mx <= 256 || l == BS_MG_MAXL) break;
-            for (int s = 0; s < nscenes; ++s) { nx[s] = (nx[s] + 1) / 2; ny[s] = (ny[s] + 1) / 2; }
-            ++l;
         }
         char* d0;
         if (!rc) rc = dalloc(ctx, &d0, R * tw);

@@ -46,7 +46,7 @@ struct ScenePar {                 // per-scene constants
     int cellx, celly, ncell, cell0;   // grid dims and first global cell
     int row0, cap, kmax, maxit;
     int adaptive_dt, scalar_on, precision, stop_rule;
-    int nblk, blk0, max_outer, pad;
+    int nblk, blk0, max_outer, mg_lev;   // mg_lev: this scene's coarsest multigrid level
 };
 
 struct SceneDyn {                 // per-scene dynamic state (device)

@@ -207,7 +207,7 @@ __global__ void k_mg_coarse(Dev D) {
     const int s = blockIdx.x;
     if (mg_skip(D, s)) return;
     const MgDev& M = D.mg;
-    const int L = M.nlev;
+    const int L = D.par[s].mg_lev;
     const LevelView<T> C = view<T>(M, L, s);
     const int m = C.nx * C.ny;
     extern __shared__ unsigned char smem[];
@@ -244,7 +244,7 @@ __global__ void k_mg_up(Dev D, int l) {
     const MgDev& M = D.mg;
     if (c >= M.n[l]) return;
     const int s = M.scene_of[l][c];
-    if (mg_skip(D, s)) return;
+    if (mg_skip(D, s) || l >= D.par[s].mg_lev) return;   // the coarse solve wrote this level
     const LevelView<T> F = view<T>(M, l, s);
     const int q = c - F.off;
     const int i = q % F.ny, j = q / F.ny;
