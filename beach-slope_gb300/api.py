@@ -59,6 +59,7 @@ def _load():
         "bs_timestep": (C.c_int, [vp]),
         "bs_step": (C.c_int, [vp, i32]),
         "bs_bicgstab_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, vp, vp]),
+        "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
         "bs_kernel_timing": (C.c_int, [vp, i32]),
@@ -236,3 +237,14 @@ def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=abi.STOP_
     rc = lib.bs_bicgstab_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data, b.ctypes.data,
                              x.ctypes.data, tol, maxit, rule, C.byref(it), C.byref(rr))
     return rc, x, it.value, rr.value
+
+
+def bicgstab_csr_noalloc(n, d_row_ptr, d_col, d_val, d_b, d_x, tol=1e-12, maxit=1000, stream=None):
+    """BiCGStab on a CSR system already in device memory (integer device
+    addresses), allocating nothing; see bs_bicgstab_csr_noalloc in
+    include/beachslope.h for the limits.  Returns (status, iterations, relres)."""
+    it = C.c_int32()
+    rr = C.c_double()
+    rc = lib.bs_bicgstab_csr_noalloc(int(n), d_row_ptr, d_col, d_val, d_b, d_x, float(tol), int(maxit), stream,
+                                     C.byref(it), C.byref(rr))
+    return rc, it.value, rr.value

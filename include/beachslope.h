@@ -220,6 +220,23 @@ int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const
                     const double* b, double* x, double tol, int32_t maxit, int32_t stop_rule,
                     int32_t* iters, double* relres);
 
+/* No counterpart in the reference.  The same BiCGStab as bs_bicgstab_csr, but
+ * on a CSR system already in device memory (0-based d_row_ptr[n+1], d_col,
+ * d_val, d_b; d_x holds the initial guess and receives the solution) and
+ * without allocating: for callers that cannot let a library call cudaMalloc
+ * or cudaFree (hosts whose device memory belongs to their own pool allocator,
+ * or code that must not stall on the implicit synchronisation of those
+ * calls).  All solver scratch lives in a fixed ~3.2 MB device array inside the
+ * library, which every GPU that loads the library holds until exit.  At most
+ * 65,536 rows (larger n returns BS_E_CAPACITY).  The array is shared by all
+ * calls: calls whose GPU work overlaps race, so serialise them.  The first call
+ * on each device looks up the array's address (cudaGetSymbolAddress, that
+ * device current); make it before any stream capture.  `stream` is a
+ * cudaStream_t (NULL: the default stream). */
+int bs_bicgstab_csr_noalloc(int32_t n, const int32_t* d_row_ptr, const int32_t* d_col, const double* d_val,
+                            const double* d_b, double* d_x, double tol, int32_t maxit, void* stream,
+                            int32_t* iters, double* relres);
+
 /* ---- timing: CUDA events recorded on the context's stream ------------------ */
 int bs_event_record(struct bs_ctx* ctx, int32_t slot);
 int bs_event_elapsed_ms(struct bs_ctx* ctx, int32_t slot0, int32_t slot1, float* ms);
