@@ -62,7 +62,7 @@ def _load():
         "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
-        "bs_kernel_timing": (C.c_int, [vp, i32]),
+        "bs_kernel_timing": (C.c_int, [vp, C.c_uint64]),
         "bs_kernel_timing_get": (C.c_int, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(i32),
                                            C.POINTER(C.c_double)]),
         "bs_launch_count": (C.c_int64, [vp]),
@@ -190,7 +190,7 @@ class Context:
         self._check(lib.bs_event_elapsed_ms(self.h, a, b, C.byref(ms)), "event_elapsed")
         return ms.value
 
-    def kernel_timing(self, mask=1):
+    def kernel_timing(self, mask=(1 << 64) - 1):
         self._check(lib.bs_kernel_timing(self.h, mask), "kernel_timing")
 
     def kernel_times(self):
@@ -203,6 +203,16 @@ class Context:
                 break
             if cnt.value:
                 out[name.value.decode()] = (cnt.value, ms.value)
+        return out
+
+    def kernel_ids(self):
+        """name -> id of every kernel the per-kernel timer knows."""
+        out = {}
+        for k in range(256):
+            name = C.c_char_p()
+            if lib.bs_kernel_timing_get(self.h, k, C.byref(name), None, None) != 0:
+                break
+            out[name.value.decode()] = k
         return out
 
     def launch_count(self):

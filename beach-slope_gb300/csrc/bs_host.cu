@@ -37,6 +37,7 @@ struct bs_ctx {
     bool disp_ready = false;
     int max_solsteps = 1;
     bs::KTimer timer;
+    bs::IterGraph graph;
 };
 
 namespace {
@@ -71,6 +72,7 @@ bs::Launch launch_of(bs_ctx* c) {
     L.ncell_total = c->ncell_total;
     L.launches = &c->launches;
     L.timer = &c->timer;
+    L.graph = &c->graph;
     return L;
 }
 
@@ -396,6 +398,7 @@ int bs_destroy(bs_ctx* ctx) {
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->timer.ready)
         for (auto& e : ctx->timer.ev) cudaEventDestroy(e);
+    if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BS_OK;
@@ -884,7 +887,7 @@ int bs_event_elapsed_ms(bs_ctx* ctx, int32_t a, int32_t b, float* ms) {
     return 0;
 }
 // enable: bit mask of kernel ids to bracket with events (0 disables); resets totals
-int bs_kernel_timing(bs_ctx* ctx, int32_t enable) {
+int bs_kernel_timing(bs_ctx* ctx, uint64_t enable) {
     if (!ctx) return BS_E_ARG;
     CK(cudaStreamSynchronize(ctx->stream));
     bs::KTimer& T = ctx->timer;
@@ -893,8 +896,7 @@ int bs_kernel_timing(bs_ctx* ctx, int32_t enable) {
         T.ready = true;
     }
     bs::timer_collect(&T, true);
-    T.mask = enable == 1 ? ~0ull : (unsigned long long)(uint32_t)enable;
-    if (!enable) T.mask = 0;
+    T.mask = (unsigned long long)enable;
     for (int k = 0; k < bs::K_COUNT; ++k) {
         T.total_ms[k] = 0.0;
         T.count[k] = 0;

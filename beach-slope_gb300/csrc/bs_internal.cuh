@@ -260,12 +260,21 @@ struct KTimer {
     double total_ms[K_COUNT] = {};
     long long count[K_COUNT] = {};
 };
+// One captured BiCGStab iteration, re-used while the device pointers match.
+struct IterGraph {
+    cudaGraphExec_t exec = nullptr;
+    Dev key;
+    int precond = -1, prec = -1;
+    int64_t nkernels = 0;
+    bool valid = false;
+};
 struct Launch {
     cudaStream_t stream;
     int nblk_rows;      // total row blocks
     int ncell_total;
     int64_t* launches;  // launch counter
     KTimer* timer;
+    IterGraph* graph;   // nullptr: launch kernels one by one
 };
 // bracket one launch with timer events (no-op unless the id is enabled)
 void timer_collect(KTimer* T, bool wait);

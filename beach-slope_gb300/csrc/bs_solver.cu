@@ -12,6 +12,8 @@
 // inner iteration runs on FP32 vectors and FP32 matrix values; the outer
 // loop recomputes the true residual with the FP64 matrix and corrects x
 // (iterative refinement), with FP64 dots throughout.
+#include <cstring>
+
 #include "bs_internal.cuh"
 
 namespace {
@@ -512,28 +514,62 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     q = tbegin(L, K_BICG_INIT);
     k_init64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
     tend(L, q);
+    auto iteration = [&]() {
+        int q2 = tbegin(L, K_BICG_PUPD);
+        k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        tend(L, q2);
+        if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
+        q2 = tbegin(L, K_BICG_IT1);
+        k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu);
+        tend(L, q2);
+        q2 = tbegin(L, K_BICG_SUPD);
+        k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        tend(L, q2);
+        if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
+        q2 = tbegin(L, K_BICG_IT2);
+        k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, su);
+        tend(L, q2);
+        q2 = tbegin(L, K_BICG_IT3);
+        k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu, su, d_nconv);
+        tend(L, q2);
+    };
+    // capture one iteration as a CUDA graph (not while per-kernel events are on)
+    IterGraph* G = L.graph;
+    bool use_graph = G && !(L.timer && L.timer->mask);
+    if (use_graph && !(G->valid && G->precond == precond && G->prec == mg_prec &&
+                       std::memcmp(&G->key, &D, sizeof(Dev)) == 0)) {
+        if (G->exec) cudaGraphExecDestroy(G->exec);
+        G->exec = nullptr;
+        G->valid = false;
+        const int64_t before = *L.launches;
+        cudaGraph_t gr = nullptr;
+        if (cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            iteration();
+            if (cudaStreamEndCapture(L.stream, &gr) == cudaSuccess && gr &&
+                cudaGraphInstantiate(&G->exec, gr, 0) == cudaSuccess) {
+                G->valid = true;
+                G->key = D;
+                G->precond = precond;
+                G->prec = mg_prec;
+                G->nkernels = *L.launches - before;
+            }
+            if (gr) cudaGraphDestroy(gr);
+        }
+        *L.launches = before;
+        cudaGetLastError();
+        use_graph = G->valid;
+    }
     int it = 0;
     while (it < maxit) {
         cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
         cudaEventRecord(ev, L.stream);
         for (int c = 0; c < check_every && it < maxit; ++c, ++it) {
-            q = tbegin(L, K_BICG_PUPD);
-            k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
-            tend(L, q);
-            if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
-            q = tbegin(L, K_BICG_IT1);
-            k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu);
-            tend(L, q);
-            q = tbegin(L, K_BICG_SUPD);
-            k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
-            tend(L, q);
-            if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
-            q = tbegin(L, K_BICG_IT2);
-            k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, su);
-            tend(L, q);
-            q = tbegin(L, K_BICG_IT3);
-            k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu, su, d_nconv);
-            tend(L, q);
+            if (use_graph) {
+                cudaGraphLaunch(G->exec, L.stream);
+                *L.launches += G->nkernels;
+            } else {
+                iteration();
+            }
         }
         cudaEventSynchronize(ev);
         timer_collect(L.timer, false);

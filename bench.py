@@ -135,26 +135,31 @@ def peaks():
 
 
 # ------------------------------------------------------------- our arm
-SPMV_KERNELS = {"bicg_it1_spmv": 17, "bicg_it2_spmv": 18, "mx_it1_spmv": 26, "mx_it2_spmv": 27}
+# Kernels bracketed by CUDA events during the timed region (the candidates for
+# the dominant kernel).
+TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down", "mg_l0_up")
 
 
-def spmv_algorithmic_bytes(ctx, P, kernel):
-    """Compulsory bytes of one SpMV-type BiCGStab launch over all scenes:
-    per row its neighbour entries (column index 4 B + value w_A), diagonal,
-    count, and the row's own vector reads/writes; neighbour vector gathers
-    are counted as on-chip hits."""
+def algorithmic_bytes(ctx, kernel, precision):
+    """Compulsory HBM bytes of one launch over all scenes (neighbour-vector
+    gathers counted as on-chip hits; every other operand read or written once).
+    w = width of the per-pair and matrix values (8 FP64, 4 mixed)."""
+    w = 4 if precision == "mixed" else 8
     tot = 0.0
     for s in range(ctx.nscenes):
         c = ctx.neighbour_counts(s)
-        nnz = float(c.sum())
-        n = float(len(c))
-        if kernel.startswith("bicg"):
-            wa, wv = 8, 8
-            vec = (3 * wv + 2 * wv + wv) if "it1" in kernel else (2 * wv + 2 * wv)
-        else:
-            wa, wv = 4, 4
-            vec = (3 * wv + 2 * wv + wv) if "it1" in kernel else (2 * wv + 2 * wv)
-        tot += nnz * (4 + wa) + n * (8 + 4 + vec)
+        nnz, n = float(c.sum()), float(len(c))
+        if kernel in ("bicg_it1_spmv", "bicg_it2_spmv"):
+            # values (FP64) + column index per nonzero; diag, count, input, output, dot operand per row
+            tot += nnz * (8 + 4) + n * (8 + 4 + 8 + 8 + 8)
+        elif kernel == "mg_l0_down":
+            tot += nnz * (w + 4) + n * (8 + 4 + w + 8) + n / 27.0 * w
+        elif kernel == "mg_l0_up":
+            tot += nnz * (w + 4) + n * (8 + 4 + w + 8 + 4 + 8)
+        elif kernel == "search_effpor":
+            # own position, vol, flags, cell; list (index + dist, 1/(r2+lam), gradW x,y);
+            # coff, gradvx, flags, count; effpor reads/writes
+            tot += n * (16 + 8 + 2 + 4) + nnz * (4 + 4 * w) + n * (32 + 8 + 1 + 4) + n * (32 + 40)
     return tot
 
 
@@ -169,8 +174,8 @@ def run_ours(args, D):
     for _ in range(args.warmup):
         ctx.step(1)
     ctx.sync()
-    # per-kernel events only on the SpMV kernels (the dominant ones)
-    mask = sum(1 << k for k in SPMV_KERNELS.values())
+    ids = ctx.kernel_ids()
+    mask = sum(1 << ids[k] for k in TIMED_KERNELS)
     ctx.kernel_timing(mask)
     clocks = ClockSampler(D.local)
     D.barrier()
@@ -189,26 +194,21 @@ def run_ours(args, D):
     ms_max = D.allreduce(ms, "max")
     parts = D.allreduce(n_particles, "sum")
     info = [ctx.info(s) for s in range(ctx.nscenes)]
-    iters = float(np.mean([i["ppe_iters"] for i in info]))
     out = {
         "value": parts * args.steps / (ms_max / 1e3),
         "ms_per_step": ms_max / args.steps,
         "particles": n_particles,
         "gpu_launches": int(l1 - l0),
         "clocks": ck,
-        "ppe_iters_last": iters,
+        "ppe_iters_last": float(np.mean([i["ppe_iters"] for i in info])),
         "ppe_relres_last": max(i["ppe_relres"] for i in info),
         "err_bits": int(np.bitwise_or.reduce([i["err_bits"] for i in info])),
     }
-    # roofline of the dominant kernel (SpMV of the Krylov loop)
-    best = None
-    for name, (cnt, tms) in kt.items():
-        if name in SPMV_KERNELS and cnt:
-            if best is None or tms > best[2]:
-                best = (name, cnt, tms)
-    if best:
-        name, cnt, tms = best
-        alg = spmv_algorithmic_bytes(ctx, P, name)
+    # roofline of the dominant kernel (largest event-timed total)
+    cands = [(k, v[0], v[1]) for k, v in kt.items() if k in TIMED_KERNELS and v[0]]
+    if cands:
+        name, cnt, tms = max(cands, key=lambda t: t[2])
+        alg = algorithmic_bytes(ctx, name, args.precision)
         avg_s = tms / cnt / 1e3
         pk, src = peaks()
         achieved = alg / avg_s / 1e9
@@ -216,14 +216,58 @@ def run_ours(args, D):
                            "peak_source": src, "unit": "GB/s", "frac": round(achieved / pk, 4),
                            "traffic": None, "algorithmic_bytes_per_launch": alg,
                            "avg_launch_us": round(avg_s * 1e6, 2), "launches": cnt,
-                           "share_of_step": round(sum(v[1] for k, v in kt.items() if k in SPMV_KERNELS)
-                                                  / ms, 3)}
+                           "share_of_step": round(tms / ms, 3),
+                           "timed_kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in kt.items()}}
+    state = ctx.download(0)
     ctx.close()
-    # e2e through the C-ABI with host buffers: upload + prime inside the timed
-    # region, every step followed by a device->host read of the output fields
     if not args.no_e2e:
         out["e2e"] = run_e2e(args, D, P, S, G)
+    if args.precision == "mixed" and not args.no_fp64:
+        out["fp64"] = run_fp64_and_accuracy(args, P, S, G, state)
     return out
+
+
+def run_fp64_and_accuracy(args, P, S, G, state):
+    """The plain FP64 path on the same workload (same steps), and the per-step
+    pressure error of the mixed form against it from one common state:
+    both restart from the mixed run's final state and take one step, once at
+    the configured PPE tolerance and once at 1e-12 (which isolates the
+    precision of the sweeps and V-cycle from the solver tolerance)."""
+    from beachslope_gb300 import abi, api
+    P64 = [abi.Params.from_buffer_copy(p) for p in P]
+    for p in P64:
+        p.precision = abi.PREC_FP64
+    c = api.Context(P64, S, G)
+    c.prime()
+    for _ in range(args.warmup):
+        c.step(1)
+    c.sync()
+    c.record(0)
+    c.step(args.steps)
+    c.record(1)
+    ms = c.elapsed_ms(0, 1)
+    n = sum(len(s["x"]) for s in S)
+    res = {"value": n * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+           "ppe_iters_last": c.info(0)["ppe_iters"]}
+    c.close()
+    keys = ["x", "y", "vx", "vy", "p", "mass", "rho", "oden", "ovol", "con", "tid", "pid", "flags"]
+    st = {k: state[k] for k in keys}
+    for tol, tag in ((P[0].ppe_tol, "p_rel_l2_vs_fp64"), (1e-12, "p_rel_l2_vs_fp64_tol1e-12")):
+        outs = []
+        for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+            q = abi.Params.from_buffer_copy(P[0])
+            q.precision = prec
+            q.ppe_tol = tol
+            q.ppe_maxit = 20000
+            cc = api.Context([q], [st], [G[0]])
+            cc.prime()
+            cc.step(1)
+            outs.append(cc.download(0))
+            cc.close()
+        a, b = outs
+        if np.array_equal(a["pid"], b["pid"]):
+            res[tag] = float(np.linalg.norm(b["p"] - a["p"]) / np.linalg.norm(a["p"]))
+    return res
 
 
 def run_e2e(args, D, P, S, G):
@@ -301,13 +345,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beach_dx0.00125", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     D = Dist()
     config = {"workload": args.workload, "description": WORKLOADS[args.workload], "dt": 1e-4,
               "ppe_tol": 1e-8, "precision": args.precision, "scenes_per_gpu": 1,
+              "ppe_solver": "BiCGStab, multigrid V-cycle right preconditioner",
               "l2": "state larger than L2, streamed every step (no flush)"}
     base = {"metric": METRIC, "unit": UNIT, "n_gpus": D.world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
@@ -327,7 +373,7 @@ def main():
     if D.rank == 0:
         line = dict(base)
         line.update({"value": out["value"], "ms_per_step": out["ms_per_step"], "dtype": dtype_of(args.precision)})
-        for k in ("roofline", "e2e", "gpu_launches", "clocks"):
+        for k in ("roofline", "e2e", "gpu_launches", "clocks", "fp64"):
             if k in out:
                 line[k] = out[k]
         line["config"]["particles_per_gpu"] = out["particles"]

@@ -240,8 +240,9 @@ int bs_bicgstab_csr_noalloc(int32_t n, const int32_t* d_row_ptr, const int32_t* 
 /* ---- timing: CUDA events recorded on the context's stream ------------------ */
 int bs_event_record(struct bs_ctx* ctx, int32_t slot);
 int bs_event_elapsed_ms(struct bs_ctx* ctx, int32_t slot0, int32_t slot1, float* ms);
-/* per-kernel timing of bs_step: enable, then read {name, launches, total ms} */
-int bs_kernel_timing(struct bs_ctx* ctx, int32_t enable);
+/* per-kernel timing: mask = one bit per kernel id (bs_kernel_timing_get
+ * gives the name of each id), ~0 for all, 0 to stop; totals are reset. */
+int bs_kernel_timing(struct bs_ctx* ctx, uint64_t mask);
 int bs_kernel_timing_get(struct bs_ctx* ctx, int32_t idx, const char** name, int32_t* launches,
                          double* total_ms);
 /* count of kernels launched by the library since context creation */
