@@ -41,6 +41,8 @@ def _load():
         "bs_get_neighbours": (C.c_int, [vp, i32, vp, vp, vp, vp, vp]),
         "bs_get_matrix": (C.c_int, [vp, i32, vp, vp, vp]),
         "bs_set_rhs": (C.c_int, [vp, i32, vp]),
+        "bs_set_option": (C.c_int, [vp, C.c_char_p, C.c_double]),
+        "bs_get_option": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
         "bs_prime": (C.c_int, [vp]),
         "bs_scalar_substep": (C.c_int, [vp]),
         "bs_projection": (C.c_int, [vp]),
@@ -84,7 +86,7 @@ STAGE_FUNCS = ["prime", "scalar_substep", "projection", "search", "porosity", "e
 class Context:
     """A batch of scenes resident on the GPU."""
 
-    def __init__(self, params, states, grains=None, capacity=None):
+    def __init__(self, params, states, grains=None, capacity=None, tuning=None):
         if not isinstance(params, (list, tuple)):
             params, states, grains = [params], [states], [grains]
         n = len(params)
@@ -103,6 +105,14 @@ class Context:
         self.h = h
         for s in range(n):
             self.upload(s, states[s], grains[s])
+        self.tuning = None
+        if tuning == "auto":   # solver options picked by the autotuner for this size class
+            from . import autotune
+            self.tuning = autotune.apply(self, params[0].precision, sum(caps))
+        elif isinstance(tuning, dict):
+            for k, v in tuning.items():
+                self.set_option(k, v)
+            self.tuning = tuning
 
     def close(self):
         if getattr(self, "h", None):
@@ -161,6 +171,14 @@ class Context:
         self._check(lib.bs_get_matrix(self.h, s, diag.ctypes.data, off.ctypes.data, rhs.ctypes.data),
                     "get_matrix")
         return diag, off, rhs
+
+    def set_option(self, name, value):
+        self._check(lib.bs_set_option(self.h, name.encode(), float(value)), "set_option " + name)
+
+    def get_option(self, name):
+        v = C.c_double()
+        self._check(lib.bs_get_option(self.h, name.encode(), C.byref(v)), "get_option " + name)
+        return v.value
 
     def set_rhs(self, b, s=0):
         b = np.ascontiguousarray(b, np.float64)

@@ -1,0 +1,130 @@
+"""Autotuner for the PPE solver's multigrid V-cycle.
+
+Measures ms/step of the real workload (CUDA events on the context's stream)
+for a small staged grid of V-cycle shapes -- pre-smoothing on the particle
+and cell levels, Jacobi damping, coarse-correction scale, coarsest sweeps --
+and keeps the fastest configuration whose solves converged without error
+bits.  The result is written to tuning.json next to this file, keyed by
+precision and a particle-count bucket; Context(..., tuning="auto") applies it.
+
+    python -m beachslope_gb300.autotune   (via __graft_entry__.load_package())
+"""
+import json
+import math
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CACHE = os.path.join(HERE, "tuning.json")
+OPTIONS = ("mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
+
+
+def bucket(n_particles):
+    """Size class of a workload: powers of 4 of the particle count."""
+    return str(int(round(math.log(max(n_particles, 1), 4))))
+
+
+def key(precision, n_particles):
+    return f"prec{precision}_n4^{bucket(n_particles)}"
+
+
+def load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def lookup(precision, n_particles):
+    return load().get(key(precision, n_particles))
+
+
+def _measure(ctx, steps):
+    ctx.sync()
+    ctx.record(2)
+    ctx.step(steps)
+    ctx.record(3)
+    ms = ctx.elapsed_ms(2, 3) / steps
+    info = [ctx.info(s) for s in range(ctx.nscenes)]
+    ok = all(i["err_bits"] == 0 for i in info)
+    iters = sum(i["ppe_iters"] for i in info) / len(info)
+    return ms, ok, iters
+
+
+def tune(ctx, steps=2, verbose=True):
+    """Staged search on a primed context; returns (best options, table)."""
+    table = []
+
+    def run(opts):
+        for k, v in opts.items():
+            ctx.set_option(k, v)
+        ctx.clear_errors()
+        ms, ok, iters = _measure(ctx, steps)
+        table.append({"options": dict(opts), "ms_per_step": ms, "ok": ok, "ppe_iters": iters})
+        if verbose:
+            print(f"  {opts} -> {ms:.2f} ms/step, iters {iters:.0f}{'' if ok else ' (errors)'}", flush=True)
+        return ms if ok else math.inf
+
+    base = {"mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.7, "mg_cscale": 1.0, "mg_coarse_sweeps": 40}
+    best, best_ms = dict(base), run(base)
+    stages = [
+        [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
+        [{"mg_cscale": c} for c in (1.0, 1.3, 1.6, 1.9)],
+        [{"mg_omega": w} for w in (0.6, 0.7, 0.8, 0.9)],
+        [{"mg_coarse_sweeps": c} for c in (10, 20, 40, 80)],
+    ]
+    for stage in stages:
+        stage_best, stage_ms = best, best_ms
+        for delta in stage:
+            cand = dict(best)
+            cand.update(delta)
+            if cand == best:
+                continue
+            ms = run(cand)
+            if ms < stage_ms:
+                stage_best, stage_ms = cand, ms
+        best, best_ms = stage_best, stage_ms
+    for k, v in best.items():
+        ctx.set_option(k, v)
+    return best, best_ms, table
+
+
+def save(precision, n_particles, best, best_ms, workload):
+    d = load()
+    d[key(precision, n_particles)] = {"options": best, "ms_per_step": best_ms, "workload": workload}
+    with open(CACHE, "w") as f:
+        json.dump(d, f, indent=1, sort_keys=True)
+
+
+def apply(ctx, precision, n_particles):
+    t = lookup(precision, n_particles)
+    if t:
+        for k, v in t["options"].items():
+            ctx.set_option(k, v)
+    return t
+
+
+def main():
+    import argparse
+    from . import abi, api, scene
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dx", type=float, nargs="+", default=[0.00125, 0.0025, 0.01])
+    ap.add_argument("--precision", nargs="+", default=["mixed", "fp64"])
+    args = ap.parse_args()
+    for prec_name in args.precision:
+        prec = abi.PREC_MIXED if prec_name == "mixed" else abi.PREC_FP64
+        for dx in args.dx:
+            p, st, gr = scene.beach_scene(dx=dx, precision=prec)
+            ctx = api.Context([p], [st], [gr])
+            ctx.prime()
+            ctx.step(2)
+            n = len(st["x"])
+            print(f"{prec_name} dx={dx} n={n}", flush=True)
+            best, ms, _ = tune(ctx)
+            print(f"  best {best} {ms:.2f} ms/step", flush=True)
+            save(prec, n, best, ms, f"beach dx={dx}")
+            ctx.close()
+
+
+if __name__ == "__main__":
+    main()

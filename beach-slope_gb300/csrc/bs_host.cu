@@ -282,6 +282,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.omega = 0.7;
         M.cscale = 1.0;
         M.coarse_sweeps = 40;
+        M.pre0 = 1;
+        M.prec = 1;
         // each scene coarsens on its own until it has at most 256 cells, so
         // its V-cycle is the same alone and inside any batch
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
@@ -658,6 +660,38 @@ int bs_get_matrix(bs_ctx* ctx, int32_t s, double* diag, double* off, double* rhs
         for (int r = 0; r < n; ++r)
             for (int k = 0; k < cnt[r]; ++k) off[(size_t)r * K + k] = v[((size_t)(r >> 5) * K + k) * 32 + (r & 31)];
     }
+    return 0;
+}
+
+// Tunables of the solver (set by the autotuner, autotune.py).
+int bs_set_option(bs_ctx* ctx, const char* name, double value) {
+    if (!ctx || !name) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    MgDev& M = ctx->D.mg;
+    const std::string k(name);
+    if (k == "mg_omega" && value > 0 && value < 2) M.omega = value;
+    else if (k == "mg_cscale" && value > 0 && value < 4) M.cscale = value;
+    else if (k == "mg_pre0") M.pre0 = value != 0;
+    else if (k == "mg_prec") M.prec = value != 0;
+    else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
+    else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
+    else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
+    ctx->graph.valid = false;   // the captured iteration holds the old values
+    return 0;
+}
+
+int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
+    if (!ctx || !name || !value) return BS_E_ARG;
+    const MgDev& M = ctx->D.mg;
+    const std::string k(name);
+    if (k == "mg_omega") *value = M.omega;
+    else if (k == "mg_cscale") *value = M.cscale;
+    else if (k == "mg_pre0") *value = M.pre0;
+    else if (k == "mg_prec") *value = M.prec;
+    else if (k == "mg_coarse_sweeps") *value = M.coarse_sweeps;
+    else if (k == "mg_levels") *value = M.nlev;
+    else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
+    else return BS_E_ARG;
     return 0;
 }
 

@@ -79,6 +79,7 @@ struct MgDev {
     void* dinv0;                      // level 0: 1/adiag per particle row
     double omega, cscale;
     int coarse_sweeps, coarse_max;
+    int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
 };
 
 // device pointers of one context (passed by value to kernels)
@@ -159,6 +160,38 @@ __device__ __forceinline__ double bs_W(double r, const ScenePar& P) {
         t2 = t1;
     }
     return P.cn1 * t1 + P.cn2 * t2;
+}
+
+__device__ __forceinline__ float bs_Wf(float r, const ScenePar& P) {
+    const float q = r * (float)P.inv_h;
+    float t1, t2;
+    if (r < (float)P.h) {
+        t1 = 4.0f - 6.0f * q * q + 3.0f * q * q * q;
+        t2 = q * q * q - 6.0f * q + 6.0f;
+    } else {
+        const float a = 2.0f - q;
+        t1 = a * a * a;
+        t2 = t1;
+    }
+    return (float)P.cn1 * t1 + (float)P.cn2 * t2;
+}
+
+// r = sqrt(s) and 1/r in FP64 from an FP32 rsqrt seed and two Newton steps
+// (relative error ~1e-16, not correctly rounded): used where the exact IEEE
+// sqrt is not required (mixed-mode pair quantities, grain distances).
+__device__ __forceinline__ void fast_r64(double s, double& r, double& ir) {
+    double y = (double)rsqrtf((float)s);
+    y = y * (1.5 - 0.5 * s * y * y);
+    y = y * (1.5 - 0.5 * s * y * y);
+    ir = y;
+    r = s * y;
+}
+// 1/d in FP64 from an FP32 reciprocal seed and two Newton steps
+__device__ __forceinline__ double fast_rcp64(double d) {
+    double y = (double)__frcp_rn((float)d);
+    y = y * (2.0 - d * y);
+    y = y * (2.0 - d * y);
+    return y;
 }
 
 // Radial factor F(r) of the hybrid-kernel gradient: grad_i W_ij = F(r) (r_i - r_j)

@@ -132,17 +132,21 @@ __global__ void k_mg_l0_down(Dev D, const double* __restrict__ in) {
     const T* A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
     T sum = 0;
-    for (int r = r0 + lane; r < r1; r += 32) {
-        const T x = (T)in[r];
-        const T zr = w * x * di0[r];
-        T ax = (T)D.adiag[r] * zr;
-        const int n = D.ncount[r];
-        for (int k = 0; k < n; ++k) {
-            const long e = ell(r, k, D.kmax);
-            const int j = D.nidx[e];
-            ax += A[e] * (w * (T)in[j] * di0[j]);
+    if (!D.mg.pre0) {   // no pre-smoothing: restrict the input itself
+        for (int r = r0 + lane; r < r1; r += 32) sum += (T)in[r];
+    } else {
+        for (int r = r0 + lane; r < r1; r += 32) {
+            const T x = (T)in[r];
+            const T zr = w * x * di0[r];
+            T ax = (T)D.adiag[r] * zr;
+            const int n = D.ncount[r];
+            for (int k = 0; k < n; ++k) {
+                const long e = ell(r, k, D.kmax);
+                const int j = D.nidx[e];
+                ax += A[e] * (w * (T)in[j] * di0[j]);
+            }
+            sum += x - ax;
         }
-        sum += x - ax;
     }
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if (lane == 0) ((T*)D.mg.r[1])[c] = sum;
@@ -188,6 +192,10 @@ __global__ void k_mg_down(Dev D, int l) {
             const int fi = 2 * I + a, fj = 2 * J + b;
             if (fi >= F.ny || fj >= F.nx) continue;
             const int c = F.off + fj * F.ny + fi;
+            if (!M.prec) {
+                sum += F.r[c];
+                continue;
+            }
             T ax = 0;
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
@@ -251,9 +259,10 @@ __global__ void k_mg_up(Dev D, int l) {
     const int nyc = M.ny[l + 1][s], oc = M.off[l + 1][s];
     const T* e = (const T*)M.z[l + 1];
     const T w = (T)M.omega, cs = (T)M.cscale;
+    const T wp = M.prec ? w : (T)0;
     auto zval = [&](int ii, int jj) -> T {
         const int nb = F.off + jj * F.ny + ii;
-        return w * F.r[nb] * F.dinv[nb] + cs * e[oc + (jj / 2) * nyc + (ii / 2)];
+        return wp * F.r[nb] * F.dinv[nb] + cs * e[oc + (jj / 2) * nyc + (ii / 2)];
     };
     const T zc = zval(i, j);
     T ax = 0;
@@ -278,14 +287,15 @@ __global__ void k_mg_l0_up(Dev D, const double* __restrict__ in, double* __restr
     const T* di0 = (const T*)D.mg.dinv0;
     const T* e1 = (const T*)D.mg.z[1];
     const T* A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
+    const T wp = D.mg.pre0 ? w : (T)0;
     const T x = (T)in[r];
-    const T zr = w * x * di0[r] + cs * e1[D.cell[r]];
+    const T zr = wp * x * di0[r] + cs * e1[D.cell[r]];
     T ax = (T)D.adiag[r] * zr;
     const int n = D.ncount[r];
     for (int k = 0; k < n; ++k) {
         const long e = ell(r, k, D.kmax);
         const int j = D.nidx[e];
-        ax += A[e] * (w * (T)in[j] * di0[j] + cs * e1[D.cell[j]]);
+        ax += A[e] * (wp * (T)in[j] * di0[j] + cs * e1[D.cell[j]]);
     }
     out[r] = (double)(zr + w * di0[r] * (x - ax));
 }

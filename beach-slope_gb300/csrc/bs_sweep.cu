@@ -73,38 +73,86 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
     if (do_search) {
         const int kmax = D.kmax;
         const double twoh = P.twoh;
-        const float thr_hi = (float)(twoh * twoh) * (1.0f + 1e-5f);
+        // FP32 prefilter of the squared distance: outside [lo, hi] the exact
+        // FP64 test cannot disagree (rounding of d^2 in FP32 is < 3 ulp)
+        const float t2f = (float)(twoh * twoh);
+        const float thr_hi = t2f * (1.0f + 1e-5f), thr_lo = t2f * (1.0f - 1e-5f);
         double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
         int cnt = 0;
+        auto accept = [&](int rj, double dx, double dy, float d2f) {
+            if (cnt < kmax) {
+                const long e = ell(r, cnt, kmax);
+                D.nidx[e] = rj;
+                double kx, ky;
+                if (sizeof(T) == 4) {
+                    // mixed: pair quantities computed in FP64 without IEEE
+                    // sqrt/division (Newton from FP32 seeds), stored in FP32;
+                    // the gradient-correction sums below stay FP64-accurate
+                    (void)d2f;
+                    const double s2 = dx * dx + dy * dy;
+                    double rad, ir;
+                    fast_r64(s2, rad, ir);
+                    double F;
+                    if (rad < P.h) {
+                        F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
+                    } else {
+                        const double a = 2.0 - rad * P.inv_h;
+                        F = -(P.cn1 + P.cn2) * (3.0 * P.inv_h * ir) * a * a;
+                    }
+                    kx = F * (-dx);
+                    ky = F * (-dy);
+                    st<T>(D.ndist, e, (T)rad);
+                    st<T>(D.nrinv, e, (T)fast_rcp64(s2 + P.lam));
+                    st<T>(D.nkx, e, (T)kx);
+                    st<T>(D.nky, e, (T)ky);
+                } else {
+                    const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                    const double ir = 1.0 / rad;
+                    double F;
+                    if (rad < P.h) {
+                        F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
+                    } else {
+                        const double a = 2.0 - rad * P.inv_h;
+                        F = -(P.cn1 + P.cn2) * (3.0 * P.inv_h * ir) * a * a;
+                    }
+                    kx = F * (-dx);
+                    ky = F * (-dy);
+                    st<T>(D.ndist, e, (T)rad);
+                    st<T>(D.nrinv, e, (T)(1.0 / (rad * rad + P.lam)));
+                    st<T>(D.nkx, e, (T)kx);
+                    st<T>(D.nky, e, (T)ky);
+                }
+                const double vj = D.vol[rj];
+                const double res1 = vj * dx, res3 = vj * dy;
+                a00 += kx * res1;
+                a01 += ky * res1;
+                a10 += kx * res3;
+                a11 += ky * res3;
+            }
+            ++cnt;
+        };
+        auto test = [&](int rj, double dx, double dy) {
+            const float fx = (float)dx, fy = (float)dy;
+            const float d2f = fx * fx + fy * fy;
+            if (d2f > thr_hi) return;
+            if (d2f >= thr_lo || sizeof(T) == 8) {
+                // exact test as functions.f90:38 / search.f90:59, no FMA
+                const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                if (!(rad < twoh)) return;
+            }
+            accept(rj, dx, dy, d2f);
+        };
         if (ok) {
             for (int q = 0; q < 4; ++q) {
                 const int r1 = D.cell_end[cc[q]];
-                for (int rj = D.cell_start[cc[q]]; rj < r1; ++rj) {
-                    if (rj == r) continue;   // (tid, matid) self-exclusion
-                    const double dx = D.x[rj] - xi, dy = D.y[rj] - yi;
-                    const float fx = (float)dx, fy = (float)dy;
-                    if (fx * fx + fy * fy > thr_hi) continue;
-                    // exact test as functions.f90:38 / search.f90:59, no FMA
-                    const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                    if (!(rad < twoh)) continue;
-                    if (cnt < kmax) {
-                        const double F = bs_F(rad, P);
-                        const double kx = F * (-dx), ky = F * (-dy);   // grad_i W = F (r_i - r_j)
-                        const long e = ell(r, cnt, kmax);
-                        D.nidx[e] = rj;
-                        st<T>(D.ndist, e, (T)rad);
-                        st<T>(D.nrinv, e, (T)(1.0 / (rad * rad + P.lam)));
-                        st<T>(D.nkx, e, (T)kx);
-                        st<T>(D.nky, e, (T)ky);
-                        const double vj = D.vol[rj];
-                        const double res1 = vj * dx, res3 = vj * dy;
-                        a00 += kx * res1;
-                        a01 += ky * res1;
-                        a10 += kx * res3;
-                        a11 += ky * res3;
-                    }
-                    ++cnt;
+                int rj = D.cell_start[cc[q]];
+                for (; rj + 1 < r1; rj += 2) {   // two independent candidate loads in flight
+                    const double x0 = __ldg(D.x + rj), y0 = __ldg(D.y + rj);
+                    const double x1 = __ldg(D.x + rj + 1), y1 = __ldg(D.y + rj + 1);
+                    if (rj != r) test(rj, x0 - xi, y0 - yi);   // (tid, matid) self-exclusion
+                    if (rj + 1 != r) test(rj + 1, x1 - xi, y1 - yi);
                 }
+                if (rj < r1 && rj != r) test(rj, __ldg(D.x + rj) - xi, __ldg(D.y + rj) - yi);
             }
         }
         if (cnt > kmax) set_err(D, R.s, BS_ERR_NBR_OVERFLOW);
@@ -118,10 +166,11 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             const double det = a00 * a11 - a01 * a10;
             double c0 = 1.0, c1 = 0.0, c2 = 0.0, c3 = 1.0;
             if (fabs(det) >= BS_SP1EM5 && isfinite(det)) {
-                c0 = a11 / det;
-                c1 = -a01 / det;
-                c2 = -a10 / det;
-                c3 = a00 / det;
+                const double id = 1.0 / det;
+                c0 = a11 * id;
+                c1 = -a01 * id;
+                c2 = -a10 * id;
+                c3 = a00 * id;
             }
             D.c0[r] = c0; D.c1[r] = c1; D.c2[r] = c2; D.c3[r] = c3;
             if ((gv <= P.freethr) && !(fl & BS_FLAG_BUFFER)) fl |= BS_FLAG_FREE;
@@ -146,8 +195,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                     const int g1 = D.gcell_end[ord[q]];
                     for (int g = D.gcell_start[ord[q]]; g < g1; ++g) {
                         const double dx = xi - D.gx[g], dy = yi - D.gy[g];
-                        const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                        if (rad < P.twoh) sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
+                        if (sizeof(T) == 4) {   // mixed: Newton sqrt (W(2h) = 0: the cut needs no exact test)
+                            const double s2 = dx * dx + dy * dy;
+                            if (s2 < P.twoh * P.twoh) {
+                                double rad = 0.0, ir;   // grains may coincide with pore particles
+                                if (s2 > 0.0) fast_r64(s2, rad, ir);
+                                sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
+                            }
+                        } else {
+                            const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                            if (rad < P.twoh) sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
+                        }
                     }
                 }
             }

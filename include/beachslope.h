@@ -186,6 +186,13 @@ int bs_get_neighbours(struct bs_ctx* ctx, int32_t scene, int32_t* counts, int32_
  * aligned with the neighbour list, rhs[n]. */
 int bs_get_matrix(struct bs_ctx* ctx, int32_t scene, double* diag, double* off, double* rhs);
 
+/* Solver tunables, set by the project autotuner (beach-slope_gb300/autotune.py):
+ * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
+ * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),
+ * "mg_coarse_sweeps", "ppe_precond"; bs_get_option also reads "mg_levels". */
+int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
+int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);
+
 /* Replace the assembled right-hand side (already Jacobi-scaled) of one scene,
  * e.g. with a manufactured source; b[n] in download order. */
 int bs_set_rhs(struct bs_ctx* ctx, int32_t scene, const double* b);

@@ -287,6 +287,37 @@ def test_batched_scenes_equal_alone(api):
         assert alone.info()["ppe_iters"] == batch.info(k)["ppe_iters"]
 
 
+def test_mixed_precision_against_fp64(api):
+    """The mixed form (FP32 pair storage and sweeps, FP32 V-cycle, FP64
+    Krylov) from the same state as the FP64 drop-in: identical neighbour sets
+    and particle order, pressure within rel-L2 1e-6 when both solve to 1e-12."""
+    from beachslope_gb300 import abi, scene
+    p, st, gr = scene.beach_scene(dx=0.01)
+    p.ppe_tol = 1e-12
+    p.ppe_maxit = 20000
+    pm = abi.Params.from_buffer_copy(p)
+    pm.precision = abi.PREC_MIXED
+    a = api.Context([p], [st], [gr])
+    b = api.Context([pm], [st], [gr])
+    a.prime()
+    b.prime()
+    ca, ia, *_ = a.neighbours()
+    cb, ib, *_ = b.neighbours()
+    np.testing.assert_array_equal(ca, cb)
+    m = np.arange(p.kmax)[None, :] < ca[:, None]
+    np.testing.assert_array_equal(ia[m], ib[m])
+    a.step(1)
+    b.step(1)
+    ga, gb = a.download(), b.download()
+    # compare by particle id: a still particle sitting on a cell boundary of
+    # the lattice may end the step on either side in the two precisions
+    oa, ob = np.argsort(ga["pid"]), np.argsort(gb["pid"])
+    np.testing.assert_array_equal(ga["pid"][oa], gb["pid"][ob])
+    assert relL2(gb["p"][ob], ga["p"][oa]) < 1e-6
+    assert relL2(gb["vx"][ob], ga["vx"][oa]) < 1e-6
+    assert b.info()["ppe_relres"] <= 1e-11 and b.info()["err_bits"] == 0
+
+
 def test_error_paths(api):
     from beachslope_gb300 import abi, scene
     # neighbour capacity overflow is reported, not written past the list
