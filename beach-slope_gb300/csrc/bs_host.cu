@@ -334,9 +334,19 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
             M.off[l] = doff; M.nx[l] = dnx; M.ny[l] = dny; M.scene_of[l] = dsc;
             M.A[l] = A; M.dinv[l] = dinv; M.r[l] = rr; M.z[l] = zz;
         }
-        char* d0;
+        char *d0, *ad, *xi, *uu, *zz;
         if (!rc) rc = dalloc(ctx, &d0, R * tw);
-        if (!rc) M.dinv0 = d0;
+        if (!rc) rc = dalloc(ctx, &ad, R * tw);
+        if (!rc) rc = dalloc(ctx, &xi, R * tw);
+        if (!rc) rc = dalloc(ctx, &uu, R * tw);
+        if (!rc) rc = dalloc(ctx, &zz, R * tw);
+        if (!rc) {
+            M.dinv0 = d0;
+            M.adiagT = ad;
+            M.xin = xi;
+            M.u = uu;
+            M.zz = zz;
+        }
     }
     if (!rc && ctx->precision != BS_PREC_MIXED) {   // FP32 matrix copy for an FP32 V-cycle is mixed-only
         D.aval32 = nullptr;

@@ -77,6 +77,10 @@ struct MgDev {
     const int* nx[BS_MG_MAXL + 1];    // per scene
     const int* ny[BS_MG_MAXL + 1];
     void* dinv0;                      // level 0: 1/adiag per particle row
+    void* adiagT;                     // level 0: adiag in the V-cycle's precision
+    void* xin;                        // level 0: V-cycle input in its precision
+    void* u;                          // level 0: w * xin / adiag (pre-smoothing from zero)
+    void* zz;                         // level 0: u + cscale * e1[cell]  (after the coarse correction)
     double omega, cscale;
     int coarse_sweeps, coarse_max;
     int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
@@ -280,7 +284,8 @@ enum KId {
     K_ASSEMBLE, K_COMPVEL, K_CELLMAX, K_TIMESTEP, K_SHIFT, K_APPLY, K_DISP, K_SCALAR,
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
-    K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_COUNT
+    K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
+    K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -344,6 +349,12 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
 // multigrid preconditioner (bs_mg.cu)
 void mg_setup(const Dev& D, const Launch& L, int mg_precision);
 void mg_apply(const Dev& D, const Launch& L, int mg_precision, const double* in, double* out);
+// the level-0 input of the V-cycle, written by the Krylov streams (x = p or s)
+template <typename T>
+__device__ __forceinline__ void mg_put_input(const Dev& D, int r, double x) {
+    ((T*)D.mg.xin)[r] = (T)x;
+    ((T*)D.mg.u)[r] = (T)D.mg.omega * (T)x * ((const T*)D.mg.dinv0)[r];
+}
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_all_conv,
                  int* h_all_conv_pinned, cudaEvent_t ev);
 }  // namespace bs

@@ -35,6 +35,7 @@ __global__ void k_mg_dinv0(Dev D) {
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
     const double d = D.adiag[r];
     ((T*)D.mg.dinv0)[r] = (d != 0.0 && isfinite(d)) ? (T)(1.0 / d) : (T)0;
+    ((T*)D.mg.adiagT)[r] = (T)d;
 }
 
 // level 1 = P^T A0 P: one warp per cell
@@ -121,35 +122,43 @@ __global__ void k_mg_galc(Dev D, int l) {
 // Level 0 pre-smooth from zero (z0 = w D^-1 in), residual, restriction to
 // the cells: r1[c] = sum_{i in c} (in_i - (A0 z0)_i).  One warp per cell.
 template <typename T>
-__global__ void k_mg_l0_down(Dev D, const double* __restrict__ in) {
+__global__ void k_mg_l0_down(Dev D) {
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (c >= D.ncell_total) return;
     const int s = D.cell_scene[c];
     if (mg_skip(D, s)) return;
-    const T w = (T)D.mg.omega;
-    const T* di0 = (const T*)D.mg.dinv0;
-    const T* A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
+    const T* __restrict__ xin = (const T*)D.mg.xin;
+    const T* __restrict__ u = (const T*)D.mg.u;
+    const T* __restrict__ ad = (const T*)D.mg.adiagT;
+    const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
+    const int* __restrict__ idx = D.nidx;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
     T sum = 0;
     if (!D.mg.pre0) {   // no pre-smoothing: restrict the input itself
-        for (int r = r0 + lane; r < r1; r += 32) sum += (T)in[r];
+        for (int r = r0 + lane; r < r1; r += 32) sum += xin[r];
     } else {
         for (int r = r0 + lane; r < r1; r += 32) {
-            const T x = (T)in[r];
-            const T zr = w * x * di0[r];
-            T ax = (T)D.adiag[r] * zr;
+            T ax = ad[r] * u[r];
             const int n = D.ncount[r];
-            for (int k = 0; k < n; ++k) {
-                const long e = ell(r, k, D.kmax);
-                const int j = D.nidx[e];
-                ax += A[e] * (w * (T)in[j] * di0[j]);
-            }
-            sum += x - ax;
+            long e = ell(r, 0, D.kmax);
+            for (int k = 0; k < n; ++k, e += 32) ax += __ldg(A + e) * u[__ldg(idx + e)];
+            sum += xin[r] - ax;
         }
     }
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if (lane == 0) ((T*)D.mg.r[1])[c] = sum;
+}
+
+// zz = u + cscale * e1[cell]: the level-0 value after the coarse correction
+template <typename T>
+__global__ void k_mg_l0_prolong(Dev D) {
+    const int s = D.blk_scene[blockIdx.x];
+    if (mg_skip(D, s)) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const T pre = D.mg.pre0 ? ((const T*)D.mg.u)[r] : (T)0;
+    ((T*)D.mg.zz)[r] = pre + (T)D.mg.cscale * ((const T*)D.mg.z[1])[D.cell[r]];
 }
 
 template <typename T>
@@ -275,29 +284,31 @@ __global__ void k_mg_up(Dev D, int l) {
     ((T*)M.z[l])[c] = zc + w * F.dinv[c] * (F.r[c] - ax);
 }
 
-// Level 1 -> 0: prolongation to the particle rows + one post-sweep; writes
-// the preconditioned vector (FP64).
+// Level 0 post-sweep after the prolongation; writes the preconditioned
+// vector (FP64).
 template <typename T>
-__global__ void k_mg_l0_up(Dev D, const double* __restrict__ in, double* __restrict__ out) {
+__global__ void k_mg_l0_up(Dev D, double* __restrict__ out) {
     const int s = D.blk_scene[blockIdx.x];
     if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
-    const T w = (T)D.mg.omega, cs = (T)D.mg.cscale;
-    const T* di0 = (const T*)D.mg.dinv0;
-    const T* e1 = (const T*)D.mg.z[1];
-    const T* A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
-    const T wp = D.mg.pre0 ? w : (T)0;
-    const T x = (T)in[r];
-    const T zr = wp * x * di0[r] + cs * e1[D.cell[r]];
-    T ax = (T)D.adiag[r] * zr;
+    const T* __restrict__ zz = (const T*)D.mg.zz;
+    const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
+    const int* __restrict__ idx = D.nidx;
+    const T zr = zz[r];
+    T ax = ((const T*)D.mg.adiagT)[r] * zr;
     const int n = D.ncount[r];
-    for (int k = 0; k < n; ++k) {
-        const long e = ell(r, k, D.kmax);
-        const int j = D.nidx[e];
-        ax += A[e] * (wp * (T)in[j] * di0[j] + cs * e1[D.cell[j]]);
+    long e = ell(r, 0, D.kmax);
+    int k = 0;
+    for (; k + 2 <= n; k += 2, e += 64) {
+        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32);
+        const T a0 = __ldg(A + e), a1 = __ldg(A + e + 32);
+        ax += a0 * zz[j0];
+        ax += a1 * zz[j1];
     }
-    out[r] = (double)(zr + w * di0[r] * (x - ax));
+    if (k < n) ax += __ldg(A + e) * zz[__ldg(idx + e)];
+    const T x = ((const T*)D.mg.xin)[r];
+    out[r] = (double)(zr + (T)D.mg.omega * ((const T*)D.mg.dinv0)[r] * (x - ax));
 }
 
 inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }
@@ -318,8 +329,9 @@ void setup_t(const Dev& D, const Launch& L) {
 
 template <typename T>
 void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
+    (void)in;   // the Krylov stream already wrote the input (mg_put_input)
     int q = tbegin(L, K_MG_L0DOWN);
-    k_mg_l0_down<T><<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D, in);
+    k_mg_l0_down<T><<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
     tend(L, q);
     for (int l = 1; l < D.mg.nlev; ++l) {
         q = tbegin(L, K_MG_DOWN);
@@ -334,8 +346,11 @@ void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
         k_mg_up<T><<<gdiv(D.mg.n[l], 128), 128, 0, L.stream>>>(D, l);
         tend(L, q);
     }
+    q = tbegin(L, K_MG_PROLONG);
+    k_mg_l0_prolong<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    tend(L, q);
     q = tbegin(L, K_MG_L0UP);
-    k_mg_l0_up<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, in, out);
+    k_mg_l0_up<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, out);
     tend(L, q);
 }
 

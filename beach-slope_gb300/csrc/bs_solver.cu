@@ -99,14 +99,18 @@ __global__ void k_init64(Dev D, int* nconv) {
     }
 }
 
-// KP: p = r + beta (p - omega v)   (streaming; beta = 0 on the first iteration)
-__global__ void k_pupd64(Dev D) {
+// KP: p = r + beta (p - omega v)   (streaming; beta = 0 on the first iteration);
+// also writes the V-cycle input (mgmode 1: FP64, 2: FP32)
+__global__ void k_pupd64(Dev D, int mgmode) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
     const double beta = D.dyn[s].beta, omega = D.dyn[s].omega;
-    D.sp[r] = D.sr[r] + beta * (D.sp[r] - omega * D.sv[r]);
+    const double p = D.sr[r] + beta * (D.sp[r] - omega * D.sv[r]);
+    D.sp[r] = p;
+    if (mgmode == 1) bs::mg_put_input<double>(D, r, p);
+    else if (mgmode == 2) bs::mg_put_input<float>(D, r, p);
 }
 
 // y = A u for one row (1 DFMA per nonzero)
@@ -156,13 +160,16 @@ __global__ void k_it1_64(Dev D, const double* __restrict__ u) {
     }
 }
 
-// KS: s = r - alpha v   (streaming)
-__global__ void k_supd64(Dev D) {
+// KS: s = r - alpha v   (streaming), plus the V-cycle input as in KP
+__global__ void k_supd64(Dev D, int mgmode) {
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
-    D.ss[r] = D.sr[r] - D.dyn[s].alpha * D.sv[r];
+    const double v = D.sr[r] - D.dyn[s].alpha * D.sv[r];
+    D.ss[r] = v;
+    if (mgmode == 1) bs::mg_put_input<double>(D, r, v);
+    else if (mgmode == 2) bs::mg_put_input<float>(D, r, v);
 }
 
 // K2: t = A u (u = s, or M^-1 s);  partials (t,s), (t,t);  finisher: omega
@@ -514,16 +521,17 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     q = tbegin(L, K_BICG_INIT);
     k_init64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
     tend(L, q);
+    const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
     auto iteration = [&]() {
         int q2 = tbegin(L, K_BICG_PUPD);
-        k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, mgmode);
         tend(L, q2);
         if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
         q2 = tbegin(L, K_BICG_IT1);
         k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu);
         tend(L, q2);
         q2 = tbegin(L, K_BICG_SUPD);
-        k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, mgmode);
         tend(L, q2);
         if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
         q2 = tbegin(L, K_BICG_IT2);

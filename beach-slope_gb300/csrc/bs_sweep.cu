@@ -73,74 +73,25 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
     if (do_search) {
         const int kmax = D.kmax;
         const double twoh = P.twoh;
-        // FP32 prefilter of the squared distance: outside [lo, hi] the exact
-        // FP64 test cannot disagree (rounding of d^2 in FP32 is < 3 ulp)
+        // Phase 1 (divergent candidate scan): FP32 prefilter of the squared
+        // distance -- outside [lo, hi] the exact FP64 test cannot disagree
+        // (FP32 rounding of d^2 is < 3 ulp) -- and the exact test of
+        // functions.f90:38 / search.f90:59 (IEEE sqrt, no FMA) inside it.
+        // Only indices are appended, so the warp's divergence is cheap.
         const float t2f = (float)(twoh * twoh);
         const float thr_hi = t2f * (1.0f + 1e-5f), thr_lo = t2f * (1.0f - 1e-5f);
-        double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
         int cnt = 0;
-        auto accept = [&](int rj, double dx, double dy, float d2f) {
-            if (cnt < kmax) {
-                const long e = ell(r, cnt, kmax);
-                D.nidx[e] = rj;
-                double kx, ky;
-                if (sizeof(T) == 4) {
-                    // mixed: pair quantities computed in FP64 without IEEE
-                    // sqrt/division (Newton from FP32 seeds), stored in FP32;
-                    // the gradient-correction sums below stay FP64-accurate
-                    (void)d2f;
-                    const double s2 = dx * dx + dy * dy;
-                    double rad, ir;
-                    fast_r64(s2, rad, ir);
-                    double F;
-                    if (rad < P.h) {
-                        F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
-                    } else {
-                        const double a = 2.0 - rad * P.inv_h;
-                        F = -(P.cn1 + P.cn2) * (3.0 * P.inv_h * ir) * a * a;
-                    }
-                    kx = F * (-dx);
-                    ky = F * (-dy);
-                    st<T>(D.ndist, e, (T)rad);
-                    st<T>(D.nrinv, e, (T)fast_rcp64(s2 + P.lam));
-                    st<T>(D.nkx, e, (T)kx);
-                    st<T>(D.nky, e, (T)ky);
-                } else {
-                    const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                    const double ir = 1.0 / rad;
-                    double F;
-                    if (rad < P.h) {
-                        F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
-                    } else {
-                        const double a = 2.0 - rad * P.inv_h;
-                        F = -(P.cn1 + P.cn2) * (3.0 * P.inv_h * ir) * a * a;
-                    }
-                    kx = F * (-dx);
-                    ky = F * (-dy);
-                    st<T>(D.ndist, e, (T)rad);
-                    st<T>(D.nrinv, e, (T)(1.0 / (rad * rad + P.lam)));
-                    st<T>(D.nkx, e, (T)kx);
-                    st<T>(D.nky, e, (T)ky);
-                }
-                const double vj = D.vol[rj];
-                const double res1 = vj * dx, res3 = vj * dy;
-                a00 += kx * res1;
-                a01 += ky * res1;
-                a10 += kx * res3;
-                a11 += ky * res3;
-            }
-            ++cnt;
-        };
-        auto test = [&](int rj, double dx, double dy) {
+        auto test = [&](int rj, double xj, double yj) {
+            const double dx = xj - xi, dy = yj - yi;
             const float fx = (float)dx, fy = (float)dy;
             const float d2f = fx * fx + fy * fy;
             if (d2f > thr_hi) return;
-            if (d2f >= thr_lo || sizeof(T) == 8) {
-                // exact test as functions.f90:38 / search.f90:59, no FMA
+            if (d2f >= thr_lo) {
                 const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (!(rad < twoh)) return;
             }
-            accept(rj, dx, dy, d2f);
+            if (cnt < kmax) D.nidx[ell(r, cnt, kmax)] = rj;
+            ++cnt;
         };
         if (ok) {
             for (int q = 0; q < 4; ++q) {
@@ -149,14 +100,53 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 for (; rj + 1 < r1; rj += 2) {   // two independent candidate loads in flight
                     const double x0 = __ldg(D.x + rj), y0 = __ldg(D.y + rj);
                     const double x1 = __ldg(D.x + rj + 1), y1 = __ldg(D.y + rj + 1);
-                    if (rj != r) test(rj, x0 - xi, y0 - yi);   // (tid, matid) self-exclusion
-                    if (rj + 1 != r) test(rj + 1, x1 - xi, y1 - yi);
+                    if (rj != r) test(rj, x0, y0);   // (tid, matid) self-exclusion
+                    if (rj + 1 != r) test(rj + 1, x1, y1);
                 }
-                if (rj < r1 && rj != r) test(rj, __ldg(D.x + rj) - xi, __ldg(D.y + rj) - yi);
+                if (rj < r1 && rj != r) test(rj, __ldg(D.x + rj), __ldg(D.y + rj));
             }
         }
         if (cnt > kmax) set_err(D, R.s, BS_ERR_NBR_OVERFLOW);
-        D.ncount[r] = cnt < kmax ? cnt : kmax;
+        const int n = cnt < kmax ? cnt : kmax;
+        D.ncount[r] = n;
+        // Phase 2 (uniform over the accepted neighbours): pair quantities and
+        // the gradient-correction sums (search.f90:61-85).
+        double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, kmax);
+            const int rj = D.nidx[e];
+            const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
+            double rad, ir, rinv;
+            if (sizeof(T) == 4) {
+                // mixed: r and 1/r from Newton steps (no IEEE sqrt/division);
+                // stored in FP32, sums below stay FP64-accurate
+                const double s2 = dx * dx + dy * dy;
+                fast_r64(s2, rad, ir);
+                rinv = fast_rcp64(s2 + P.lam);
+            } else {
+                rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                ir = 1.0 / rad;
+                rinv = 1.0 / (rad * rad + P.lam);
+            }
+            double F;
+            if (rad < P.h) {
+                F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
+            } else {
+                const double a = 2.0 - rad * P.inv_h;
+                F = -(P.cn1 + P.cn2) * (3.0 * P.inv_h * ir) * a * a;
+            }
+            const double kx = F * (-dx), ky = F * (-dy);   // grad_i W = F (r_i - r_j)
+            st<T>(D.ndist, e, (T)rad);
+            st<T>(D.nrinv, e, (T)rinv);
+            st<T>(D.nkx, e, (T)kx);
+            st<T>(D.nky, e, (T)ky);
+            const double vj = D.vol[rj];
+            const double res1 = vj * dx, res3 = vj * dy;
+            a00 += kx * res1;
+            a01 += ky * res1;
+            a10 += kx * res3;
+            a11 += ky * res3;
+        }
         fl &= ~BS_FLAG_FREE;
         double gv = 0.0;
         if (tid == BS_TID_FLUID) {
