@@ -1,8 +1,9 @@
 """Autotuner for the PPE solver's multigrid V-cycle.
 
 Measures ms/step of the real workload (CUDA events on the context's stream)
-for a small staged grid of V-cycle shapes -- pre-smoothing on the particle
-and cell levels, Jacobi damping, coarse-correction scale, coarsest sweeps --
+for a small staged grid of multigrid cycle shapes -- W-cycle depth,
+pre-smoothing on the particle and cell levels, Jacobi damping,
+coarse-correction scale, coarsest sweeps --
 and keeps the fastest configuration whose solves converged without error
 bits.  The result is written to tuning.json next to this file, keyed by
 precision and a particle-count bucket; Context(..., tuning="auto") applies it.
@@ -15,7 +16,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
-OPTIONS = ("mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
+OPTIONS = ("mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
 
 
 def bucket(n_particles):
@@ -46,32 +47,49 @@ def _measure(ctx, steps):
     ctx.record(3)
     ms = ctx.elapsed_ms(2, 3) / steps
     info = [ctx.info(s) for s in range(ctx.nscenes)]
-    ok = all(i["err_bits"] == 0 for i in info)
+    ok = all(i["err_bits"] == 0 and i["ppe_iters"] > 0 for i in info)
     iters = sum(i["ppe_iters"] for i in info) / len(info)
     return ms, ok, iters
 
 
-def tune(ctx, steps=2, verbose=True):
-    """Staged search on a primed context; returns (best options, table)."""
+def tune(ctx, grains, steps=2, verbose=True):
+    """Staged search on a primed context; returns (best options, table).
+
+    Every candidate starts from the same snapshot of the scenes (re-uploaded
+    and primed, then one untimed step that also captures the solver graph),
+    so a candidate that diverges does not leave its state to the next one."""
     table = []
+    snap = [ctx.download(s) for s in range(ctx.nscenes)]
+
+    def restore():
+        for s in range(ctx.nscenes):
+            ctx.upload(s, snap[s], grains[s])
+        ctx.clear_errors()
+        ctx.prime()
 
     def run(opts):
         for k, v in opts.items():
             ctx.set_option(k, v)
-        ctx.clear_errors()
-        ms, ok, iters = _measure(ctx, steps)
+        try:
+            restore()
+            ctx.step(1)
+            ms, ok, iters = _measure(ctx, steps)
+        except RuntimeError:
+            ms, ok, iters = math.inf, False, 0
         table.append({"options": dict(opts), "ms_per_step": ms, "ok": ok, "ppe_iters": iters})
         if verbose:
             print(f"  {opts} -> {ms:.2f} ms/step, iters {iters:.0f}{'' if ok else ' (errors)'}", flush=True)
         return ms if ok else math.inf
 
-    base = {"mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.7, "mg_cscale": 1.0, "mg_coarse_sweeps": 40}
+    base = {"mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
+            "mg_coarse_sweeps": 10}
     best, best_ms = dict(base), run(base)
     stages = [
+        [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
-        [{"mg_cscale": c} for c in (1.0, 1.3, 1.6, 1.9)],
-        [{"mg_omega": w} for w in (0.6, 0.7, 0.8, 0.9)],
-        [{"mg_coarse_sweeps": c} for c in (10, 20, 40, 80)],
+        [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
+        [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],
+        [{"mg_coarse_sweeps": c} for c in (5, 10, 20)],
     ]
     for stage in stages:
         stage_best, stage_ms = best, best_ms
@@ -86,6 +104,7 @@ def tune(ctx, steps=2, verbose=True):
         best, best_ms = stage_best, stage_ms
     for k, v in best.items():
         ctx.set_option(k, v)
+    restore()
     return best, best_ms, table
 
 
@@ -120,7 +139,7 @@ def main():
             ctx.step(2)
             n = len(st["x"])
             print(f"{prec_name} dx={dx} n={n}", flush=True)
-            best, ms, _ = tune(ctx)
+            best, ms, _ = tune(ctx, [gr])
             print(f"  best {best} {ms:.2f} ms/step", flush=True)
             save(prec, n, best, ms, f"beach dx={dx}")
             ctx.close()

@@ -38,6 +38,8 @@ struct bs_ctx {
     int max_solsteps = 1;
     bs::KTimer timer;
     bs::IterGraph graph;
+    std::vector<MgLevel> mglev;          // multigrid level tables (kernel arguments), index = level
+    std::vector<unsigned char> mgneed;   // per level: which launches some scene needs (Launch::mgneed)
 };
 
 namespace {
@@ -73,6 +75,8 @@ bs::Launch launch_of(bs_ctx* c) {
     L.launches = &c->launches;
     L.timer = &c->timer;
     L.graph = &c->graph;
+    L.mglev = c->mglev.empty() ? nullptr : c->mglev.data();
+    L.mgneed = c->mgneed.empty() ? nullptr : c->mgneed.data();
     return L;
 }
 
@@ -187,6 +191,7 @@ int bs_set_device(int32_t device) {
 int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity, const int32_t* grain_capacity,
               bs_ctx** out) {
     if (nscenes <= 0 || !params || !capacity || !out) return BS_E_ARG;
+    if (nscenes > BS_MG_MAXS) return BS_E_CAPACITY;   // multigrid level tables hold BS_MG_MAXS scenes
     bs_ctx* ctx = new bs_ctx();
     ctx->nscene = nscenes;
     ctx->prm.assign(params, params + nscenes);
@@ -274,22 +279,24 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         for (auto q : fv)
             if (!rc) rc = dalloc(ctx, q, R);
     }
-    // multigrid levels: level 1 = the cell grid of every scene, then 2x2
-    // coarsening until every scene has at most 256 coarse cells
+    // multigrid levels: level 1 = the half-cell grid of every scene (2 x 2
+    // per search cell), level 2 = the cells, then 2x2 coarsening until every
+    // scene has at most 256 coarse cells
     if (!rc) {
         MgDev& M = D.mg;
         std::memset(&M, 0, sizeof(M));
-        M.omega = 0.7;
-        M.cscale = 1.0;
-        M.coarse_sweeps = 40;
+        M.omega = 0.9;
+        M.cscale = 1.5;
+        M.coarse_sweeps = 10;
         M.pre0 = 1;
         M.prec = 1;
+        M.wlev = 2;
         // each scene coarsens on its own until it has at most 256 cells, so
         // its V-cycle is the same alone and inside any batch
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
         int L = 1;
         for (int s = 0; s < nscenes; ++s) {
-            int nx = params[s].cellx, ny = params[s].celly;
+            int nx = 2 * params[s].cellx, ny = 2 * params[s].celly;
             dims[s].push_back({nx, ny});
             while (nx * ny > 256 && (int)dims[s].size() < BS_MG_MAXL) {
                 nx = (nx + 1) / 2;
@@ -335,6 +342,32 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
             M.A[l] = A; M.dinv[l] = dinv; M.r[l] = rr; M.z[l] = zz;
         }
         char *d0, *ad, *xi, *uu, *zz;
+        if (!rc) rc = dalloc(ctx, &M.sub, R);
+        if (!rc) rc = dalloc(ctx, &M.agg1, R);
+        // level tables for the level kernels' arguments, and the levels
+        // that need launches at all
+        ctx->mglev.assign(L + 2, MgLevel{});
+        ctx->mgneed.assign(L + 2, 0);
+        for (int l = 1; l <= L; ++l) {
+            MgLevel& G = ctx->mglev[l];
+            G.l = l;
+            G.n = M.n[l];
+            G.ns = nscenes;
+            int o = 0;
+            for (int s = 0; s < nscenes; ++s) {
+                G.off[s] = o;
+                const int Lc = (int)dims[s].size();
+                const bool has = Lc >= l;
+                G.nx[s] = has ? dims[s][l - 1].first : 0;
+                G.ny[s] = has ? dims[s][l - 1].second : 0;
+                G.lev[s] = Lc;
+                o += G.nx[s] * G.ny[s];
+                if (l <= Lc) ctx->mgneed[l] |= 1;
+                if (l < Lc) ctx->mgneed[l] |= 2;
+                if (l == Lc) ctx->mgneed[l] |= 4;
+            }
+            G.off[nscenes] = o;
+        }
         if (!rc) rc = dalloc(ctx, &d0, R * tw);
         if (!rc) rc = dalloc(ctx, &ad, R * tw);
         if (!rc) rc = dalloc(ctx, &xi, R * tw);
@@ -684,6 +717,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_pre0") M.pre0 = value != 0;
     else if (k == "mg_prec") M.prec = value != 0;
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
+    else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
     ctx->graph.valid = false;   // the captured iteration holds the old values
@@ -699,6 +733,7 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "mg_pre0") *value = M.pre0;
     else if (k == "mg_prec") *value = M.prec;
     else if (k == "mg_coarse_sweeps") *value = M.coarse_sweeps;
+    else if (k == "mg_wlev") *value = M.wlev;
     else if (k == "mg_levels") *value = M.nlev;
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
     else return BS_E_ARG;

@@ -61,9 +61,11 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     double part_tmp;
 };
 
-// Aggregation multigrid over the cell grid (level 1 = the cells, one
-// aggregate per cell; level l+1 = 2x2 boxes of level l), 9-point Galerkin
-// stencils stored per offset k = (dj+1)*3 + (di+1): A[k*n + c].
+// Aggregation multigrid over the cell grid.  Level 1 = half-cells (2h x 2h,
+// the four quadrants of a search cell: one aggregate of ~7 rows), level 2 =
+// the cells, level l+1 = 2x2 boxes of level l; 9-point Galerkin stencils
+// stored per offset k = (dj+1)*3 + (di+1): A[k*n + c].  Levels 1..wlev
+// visit the next level twice (W-cycle), deeper levels once (V-cycle).
 #define BS_MG_MAXL 16
 struct MgDev {
     int nlev;                         // coarsest level index (levels 1..nlev)
@@ -84,6 +86,20 @@ struct MgDev {
     double omega, cscale;
     int coarse_sweeps, coarse_max;
     int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
+    int wlev;                         // levels 1..wlev recurse twice
+    uint8_t* sub;                     // level 0: quadrant of the row in its cell (bit0 lower, bit1 right)
+    int* agg1;                        // level 0: global level-1 index of the row's half-cell
+};
+
+// One cell level's per-scene tables, passed to the level kernels by value
+// (__grid_constant__): scene k owns cells [off[k], off[k+1]) of the level, a
+// nx[k] x ny[k] grid (empty range if the scene is coarser than the level).
+#define BS_MG_MAXS 64
+struct MgLevel {
+    int l, n, ns;              // level, cells over all scenes, scenes
+    int off[BS_MG_MAXS + 1];
+    int nx[BS_MG_MAXS], ny[BS_MG_MAXS];
+    int lev[BS_MG_MAXS];       // the scene's coarsest level
 };
 
 // device pointers of one context (passed by value to kernels)
@@ -285,7 +301,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_COUNT
+    K_MG_RESID, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -298,11 +314,11 @@ struct KTimer {
     double total_ms[K_COUNT] = {};
     long long count[K_COUNT] = {};
 };
-// One captured BiCGStab iteration, re-used while the device pointers match.
+// A captured chunk of BiCGStab iterations, re-used while the device data match.
 struct IterGraph {
     cudaGraphExec_t exec = nullptr;
     Dev key;
-    int precond = -1, prec = -1;
+    int precond = -1, prec = -1, chunk = 0;
     int64_t nkernels = 0;
     bool valid = false;
 };
@@ -313,7 +329,35 @@ struct Launch {
     int64_t* launches;  // launch counter
     KTimer* timer;
     IterGraph* graph;   // nullptr: launch kernels one by one
+    const MgLevel* mglev;          // host tables of the multigrid levels, indexed by level
+    const unsigned char* mgneed;   // per level: bit0 some scene visits it, bit1 restriction and
+                                   // prolongation to the next level, bit2 coarsest-level solve
 };
+// Programmatic dependent launch: a kernel launched by launch_pdl may be
+// scheduled while its predecessor in the stream still runs.  Its first
+// statement must be BS_PDL_ENTRY(): wait for the predecessor grid to finish
+// (its memory visible), then allow the successor to be scheduled.  Without
+// the launch attribute both instructions are no-ops.
+#define BS_PDL_ENTRY()                                                  \
+    do {                                                                \
+        asm volatile("griddepcontrol.wait;" ::: "memory");              \
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); \
+    } while (0)
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(const Launch& L, void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                       Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = L.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 // bracket one launch with timer events (no-op unless the id is enabled)
 void timer_collect(KTimer* T, bool wait);
 inline int tbegin(const Launch& L, int id) {

@@ -2,19 +2,26 @@
 //
 // The reference solves the Jacobi-scaled PPE with unpreconditioned FGMRES /
 // BiCGStab (solver.f90:129-350); the iteration count then grows with the
-// number of particles across the domain.  This V-cycle is applied as a right
-// preconditioner; the Krylov recurrence, dots and the stopping test stay
-// FP64, so the converged pressure is the solution of the same FP64 system.
+// number of particles across the domain.  This multigrid cycle is applied as
+// a right preconditioner; the Krylov recurrence, dots and the stopping test
+// stay FP64, so the converged pressure is the solution of the same FP64
+// system.
 //
 // Level 0: particle rows (the sliced-ELL PPE).  Level 1: one aggregate per
-// cell of the search grid -- the rows of a cell are contiguous, so the
-// Galerkin product P^T A P (P = cell indicator) is a warp reduction per
-// cell, and because every neighbour lies in one of the 3x3 surrounding cells
-// the coarse operator is a 9-point stencil on the cell grid.  Level l+1:
-// 2x2 boxes of level l, again a 9-point Galerkin stencil.  Smoother: damped
-// Jacobi, one pre-sweep from zero and one post-sweep; coarsest level: Jacobi
-// sweeps by one block per scene.  All kernels skip converged scenes.
-// T = double (FP64 mode) or float (mixed mode, FP32 V-cycle).
+// half-cell -- the four 2h x 2h quadrants of a search cell (~7 rows each).
+// The rows of a cell are contiguous, so the Galerkin product P^T A P
+// (P = half-cell indicator) is a warp reduction per cell, and because every
+// neighbour lies within 2h the coarse operator is a 9-point stencil on the
+// half-cell grid.  Level 2: the cells; level l+1: 2x2 boxes of level l,
+// again 9-point Galerkin stencils.  Smoother: damped Jacobi, one pre-sweep
+// from zero and one post-sweep; coarse corrections scaled by cscale (over-
+// correction for the piecewise-constant prolongation); levels 1..wlev visit
+// the next level twice (the second time on the updated residual), so the
+// cycle is a W-cycle at the top and a V-cycle below; coarsest level: Jacobi
+// sweeps by one block per scene.  Every scene coarsens on its own, so its
+// cycle is the same alone and inside a batch.  The particle-level kernels
+// skip converged scenes.  T = double (FP64 mode) or float (mixed mode, FP32
+// cycle).
 #include "bs_internal.cuh"
 
 using namespace bs;
@@ -23,64 +30,105 @@ namespace {
 
 __device__ __forceinline__ bool mg_skip(const Dev& D, int s) { return D.dyn[s].converged != 0; }
 
-template <typename T>
-__device__ __forceinline__ const T* Ap(const Dev& D, int l) { return (const T*)D.mg.A[l]; }
-
 // ------------------------------------------------------------ setup
-// level 0: 1/adiag per row
+// level 0: 1/adiag per row, and the row's half-cell (quadrant of its cell,
+// split at the cell's mid-lines as the quadrant search does, search.f90:328)
 template <typename T>
 __global__ void k_mg_dinv0(Dev D) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const ScenePar& P = D.par[s];
+    if (r >= P.row0 + D.dyn[s].n) return;
     const double d = D.adiag[r];
     ((T*)D.mg.dinv0)[r] = (d != 0.0 && isfinite(d)) ? (T)(1.0 / d) : (T)0;
     ((T*)D.mg.adiagT)[r] = (T)d;
+    const int lc = D.cell[r] - P.cell0;
+    const int i0 = lc % P.celly, j0 = lc / P.celly;
+    const double xl = cell_xleft(P, j0 + 1), xr = cell_xright(P, j0 + 1);
+    const double yb = cell_ybot(P, i0 + 1), yt = cell_ytop(P, i0 + 1);
+    const int lower = D.y[r] <= yb + fabs((yt - yb) / 2.0);
+    const int right = D.x[r] > xl + fabs((xl - xr) / 2.0);
+    D.mg.sub[r] = (uint8_t)(lower | (right << 1));
+    D.mg.agg1[r] = D.mg.off[1][s] + (2 * j0 + right) * (2 * P.celly) + 2 * i0 + lower;
 }
 
-// level 1 = P^T A0 P: one warp per cell
+// level 1 = P^T A0 P over the half-cells: one warp per cell, a lane per row
+// accumulating the row's 9 stencil entries, then one masked warp reduction
+// per (half-cell, entry); lane m keeps entry m and m+32 of the 36 results.
+// An offset beyond one half-cell (a pair split by rounding at a mid-line)
+// is clamped into the stencil.
 template <typename T>
 __global__ void k_mg_gal0(Dev D) {
+    BS_PDL_ENTRY();
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (c >= D.ncell_total) return;
     const int s = D.cell_scene[c];
-    const int celly = D.par[s].celly;
+    const ScenePar& P = D.par[s];
+    const int celly = P.celly;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
     const double* A = (const double*)D.aval;
-    double acc[9];
+    const uint8_t* sub = D.mg.sub;
+    double mine0 = 0.0, mine1 = 0.0;
+    for (int base = r0; base < r1; base += 32) {
+        const int r = base + lane;
+        double acc[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
-    for (int r = r0 + lane; r < r1; r += 32) {
-        acc[4] += D.adiag[r];
-        const int n = D.ncount[r];
-        for (int k = 0; k < n; ++k) {
-            const long e = ell(r, k, D.kmax);
-            const int d = D.cell[D.nidx[e]] - c;
-            const int dj = (d + celly + 1) / celly - 1;
-            const int di = d - dj * celly;
-            const int q = (dj + 1) * 3 + (di + 1);
-            const double v = A[e];
+        for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+        int sb = -1;
+        if (r < r1) {
+            sb = sub[r];
+            const int si = sb & 1, sj = sb >> 1;
+            acc[4] += D.adiag[r];
+            const int n = D.ncount[r];
+            for (int k = 0; k < n; ++k) {
+                const long e = ell(r, k, D.kmax);
+                const int col = D.nidx[e];
+                const int d = D.cell[col] - c;
+                const int dj = (d + celly + 1) / celly - 1;
+                const int di = d - dj * celly;
+                const int s2 = sub[col];
+                const int dI = min(max(2 * di + (s2 & 1) - si, -1), 1);
+                const int dJ = min(max(2 * dj + (s2 >> 1) - sj, -1), 1);
+                const int q = (dJ + 1) * 3 + (dI + 1);
+                const double v = A[e];
 #pragma unroll
-            for (int t = 0; t < 9; ++t)
-                if (t == q) acc[t] += v;
+                for (int t = 0; t < 9; ++t)
+                    if (t == q) acc[t] += v;
+            }
         }
-    }
 #pragma unroll
-    for (int k = 0; k < 9; ++k)
-        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-    if (lane == 0) {
-        T* Al = (T*)D.mg.A[1];
-        const int n1 = D.mg.n[1];
+        for (int t = 0; t < 4; ++t)
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Al[(long)k * n1 + c] = (T)acc[k];
-        ((T*)D.mg.dinv[1])[c] = (acc[4] != 0.0 && isfinite(acc[4])) ? (T)(1.0 / acc[4]) : (T)0;
+            for (int k = 0; k < 9; ++k) {
+                double v = (sb == t) ? acc[k] : 0.0;
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                const int m = t * 9 + k;
+                if (m < 32) { if (lane == m) mine0 += v; }
+                else if (lane == m - 32) mine1 += v;
+            }
     }
+    T* Al = (T*)D.mg.A[1];
+    T* dl = (T*)D.mg.dinv[1];
+    const int n1 = D.mg.n[1];
+    const int lc = c - P.cell0;
+    const int i0 = lc % celly, j0 = lc / celly;
+    const int o1 = D.mg.off[1][s], ny1 = 2 * celly;
+    auto put = [&](int m, double v) {
+        const int t = m / 9, k = m - 9 * (m / 9);
+        const int Q = o1 + (2 * j0 + (t >> 1)) * ny1 + 2 * i0 + (t & 1);
+        Al[(long)k * n1 + Q] = (T)v;
+        if (k == 4) dl[Q] = (v != 0.0 && isfinite(v)) ? (T)(1.0 / v) : (T)0;
+    };
+    put(lane, mine0);
+    if (lane < 4) put(lane + 32, mine1);
 }
 
 // level l+1 from level l: one thread per coarse cell
 template <typename T>
 __global__ void k_mg_galc(Dev D, int l) {
+    BS_PDL_ENTRY();
     const int Q = blockIdx.x * blockDim.x + threadIdx.x;
     const MgDev& M = D.mg;
     if (Q >= M.n[l + 1]) return;
@@ -118,11 +166,14 @@ __global__ void k_mg_galc(Dev D, int l) {
     ((T*)M.dinv[l + 1])[Q] = (acc[4] != 0.0 && isfinite(acc[4])) ? (T)(1.0 / acc[4]) : (T)0;
 }
 
-// ------------------------------------------------------------ V-cycle
+// ------------------------------------------------------------ cycle
 // Level 0 pre-smooth from zero (z0 = w D^-1 in), residual, restriction to
-// the cells: r1[c] = sum_{i in c} (in_i - (A0 z0)_i).  One warp per cell.
+// the half-cells: r1[h] = sum_{i in h} (in_i - (A0 z0)_i).  One warp per
+// cell, four sums (one per quadrant); every half-cell is written, empty
+// ones with 0.
 template <typename T>
 __global__ void k_mg_l0_down(Dev D) {
+    BS_PDL_ENTRY();
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (c >= D.ncell_total) return;
@@ -133,161 +184,219 @@ __global__ void k_mg_l0_down(Dev D) {
     const T* __restrict__ ad = (const T*)D.mg.adiagT;
     const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
     const int* __restrict__ idx = D.nidx;
+    const uint8_t* __restrict__ sub = D.mg.sub;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
-    T sum = 0;
-    if (!D.mg.pre0) {   // no pre-smoothing: restrict the input itself
-        for (int r = r0 + lane; r < r1; r += 32) sum += xin[r];
-    } else {
-        for (int r = r0 + lane; r < r1; r += 32) {
+    T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+    for (int r = r0 + lane; r < r1; r += 32) {
+        T v = xin[r];
+        if (D.mg.pre0) {
             T ax = ad[r] * u[r];
             const int n = D.ncount[r];
             long e = ell(r, 0, D.kmax);
             for (int k = 0; k < n; ++k, e += 32) ax += __ldg(A + e) * u[__ldg(idx + e)];
-            sum += xin[r] - ax;
+            v -= ax;
         }
+        const int t = sub[r];
+        q0 += (t == 0) ? v : (T)0;
+        q1 += (t == 1) ? v : (T)0;
+        q2 += (t == 2) ? v : (T)0;
+        q3 += (t == 3) ? v : (T)0;
     }
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (lane == 0) ((T*)D.mg.r[1])[c] = sum;
+    for (int o = 16; o > 0; o >>= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+        q3 += __shfl_xor_sync(0xffffffffu, q3, o);
+    }
+    if (lane < 4) {
+        const ScenePar& P = D.par[s];
+        const int lc = c - P.cell0;
+        const int i0 = lc % P.celly, j0 = lc / P.celly;
+        const int Q = D.mg.off[1][s] + (2 * j0 + (lane >> 1)) * (2 * P.celly) + 2 * i0 + (lane & 1);
+        ((T*)D.mg.r[1])[Q] = lane == 0 ? q0 : lane == 1 ? q1 : lane == 2 ? q2 : q3;
+    }
 }
 
-// zz = u + cscale * e1[cell]: the level-0 value after the coarse correction
+// zz = u + cscale * e1[half-cell]: the level-0 value after the coarse correction
 template <typename T>
 __global__ void k_mg_l0_prolong(Dev D) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
     const T pre = D.mg.pre0 ? ((const T*)D.mg.u)[r] : (T)0;
-    ((T*)D.mg.zz)[r] = pre + (T)D.mg.cscale * ((const T*)D.mg.z[1])[D.cell[r]];
+    ((T*)D.mg.zz)[r] = pre + (T)D.mg.cscale * ((const T*)D.mg.z[1])[D.mg.agg1[r]];
 }
 
-template <typename T>
-struct LevelView {
-    const T* A;
-    const T* dinv;
-    const T* r;
-    int n, off, nx, ny;
-};
+// ---- level operations on the cell levels (l >= 1), one cell per thread.
+// The level's per-scene tables arrive as a kernel argument (MgLevel, in the
+// constant bank), so a cell's scene, offsets and grid size cost no memory
+// round trip; on these small levels the kernels are bound by the latency of
+// their dependent loads, not by bandwidth.  Converged scenes are not
+// skipped here (their cells are few and the result is unused).
 
-template <typename T>
-__device__ __forceinline__ LevelView<T> view(const MgDev& M, int l, int s) {
-    LevelView<T> v;
-    v.A = (const T*)M.A[l];
-    v.dinv = (const T*)M.dinv[l];
-    v.r = (const T*)M.r[l];
-    v.n = M.n[l];
-    v.off = M.off[l][s];
-    v.nx = M.nx[l][s];
-    v.ny = M.ny[l][s];
-    return v;
+// largest scene index k with G.off[k] <= c (scenes absent from the level
+// have empty ranges)
+__device__ __forceinline__ int scene_at(const MgLevel& G, int c) {
+    int lo = 0, hi = G.ns - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (G.off[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
-// Levels l -> l+1: pre-smooth from zero, residual, restriction (2x2 sum).
+// Levels l -> l+1 for coarse cell Q: pre-smooth from zero, residual,
+// restriction (2x2 sum).
 template <typename T>
-__global__ void k_mg_down(Dev D, int l) {
+__global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C) {
+    BS_PDL_ENTRY();
     const int Q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (Q >= C.n) return;
     const MgDev& M = D.mg;
-    if (Q >= M.n[l + 1]) return;
-    const int s = M.scene_of[l + 1][Q];
-    if (mg_skip(D, s)) return;
-    const int q = Q - M.off[l + 1][s];
-    const int nyc = M.ny[l + 1][s];
+    const int k = scene_at(C, Q);
+    const int q = Q - C.off[k];
+    const int nyc = C.ny[k];
     const int I = q % nyc, J = q / nyc;
-    const LevelView<T> F = view<T>(M, l, s);
+    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
+    const T* __restrict__ A = (const T*)M.A[F.l];
+    const T* __restrict__ dinv = (const T*)M.dinv[F.l];
+    const T* __restrict__ r = (const T*)M.r[F.l];
     const T w = (T)M.omega;
     T sum = 0;
     for (int b = 0; b < 2; ++b)
         for (int a = 0; a < 2; ++a) {
             const int fi = 2 * I + a, fj = 2 * J + b;
-            if (fi >= F.ny || fj >= F.nx) continue;
-            const int c = F.off + fj * F.ny + fi;
+            if (fi >= fny || fj >= fnx) continue;
+            const int c = fo + fj * fny + fi;
+            const T rc = r[c];
             if (!M.prec) {
-                sum += F.r[c];
+                sum += rc;
                 continue;
             }
             T ax = 0;
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                const int ni = fi + (k % 3) - 1, nj = fj + (k / 3) - 1;
-                if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-                const int nb = F.off + nj * F.ny + ni;
-                ax += F.A[(long)k * F.n + c] * (w * F.r[nb] * F.dinv[nb]);
+            for (int t = 0; t < 9; ++t) {
+                const int ni = fi + (t % 3) - 1, nj = fj + (t / 3) - 1;
+                if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
+                const int nb = fo + nj * fny + ni;
+                ax += __ldg(A + (long)t * F.n + c) * (w * r[nb] * __ldg(dinv + nb));
             }
-            sum += F.r[c] - ax;
+            sum += rc - ax;
         }
-    ((T*)M.r[l + 1])[Q] = sum;
+    ((T*)M.r[C.l])[Q] = sum;
 }
 
-// Coarsest level: damped Jacobi sweeps from zero, one block per scene.
+// In-place residual on level l, cell c: r = r - A z (between the two visits
+// of a W-cycle level; reads its own r and the z of its stencil).
 template <typename T>
-__global__ void k_mg_coarse(Dev D) {
-    const int s = blockIdx.x;
-    if (mg_skip(D, s)) return;
+__global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
+    BS_PDL_ENTRY();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F.n) return;
     const MgDev& M = D.mg;
-    const int L = D.par[s].mg_lev;
-    const LevelView<T> C = view<T>(M, L, s);
-    const int m = C.nx * C.ny;
+    const int k = scene_at(F, c);
+    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
+    const int q = c - fo;
+    const int i = q % fny, j = q / fny;
+    const T* __restrict__ A = (const T*)M.A[F.l];
+    const T* z = (const T*)M.z[F.l];
+    T* r = (T*)M.r[F.l];
+    T ax = 0;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+        if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
+        ax += __ldg(A + (long)t * F.n + c) * z[fo + nj * fny + ni];
+    }
+    r[c] = r[c] - ax;
+}
+
+// Levels l+1 -> l for cell c: prolongation (constant per box, scaled) + one
+// post-sweep; with acc the result is added to z (second visit).
+template <typename T>
+__global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C, int acc) {
+    BS_PDL_ENTRY();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F.n) return;
+    const MgDev& M = D.mg;
+    const int k = scene_at(F, c);
+    if (F.l >= F.lev[k]) return;   // the coarse solve wrote this level
+    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
+    const int q = c - fo;
+    const int i = q % fny, j = q / fny;
+    const int nyc = C.ny[k], oc = C.off[k];
+    const T* __restrict__ A = (const T*)M.A[F.l];
+    const T* __restrict__ dinv = (const T*)M.dinv[F.l];
+    const T* __restrict__ r = (const T*)M.r[F.l];
+    const T* __restrict__ e = (const T*)M.z[C.l];
+    const T w = (T)M.omega, cs = (T)M.cscale;
+    const T wp = M.prec ? w : (T)0;
+    auto zval = [&](int ii, int jj) -> T {
+        const int nb = fo + jj * fny + ii;
+        return wp * r[nb] * __ldg(dinv + nb) + cs * e[oc + (jj / 2) * nyc + (ii / 2)];
+    };
+    const T zc = zval(i, j);
+    T ax = 0;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+        if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
+        ax += __ldg(A + (long)t * F.n + c) * (t == 4 ? zc : zval(ni, nj));
+    }
+    const T v = zc + w * __ldg(dinv + c) * (r[c] - ax);
+    T* zo = (T*)M.z[F.l];
+    zo[c] = acc ? zo[c] + v : v;
+}
+
+// Coarsest level: damped Jacobi sweeps from zero in shared memory, one
+// block per scene whose coarsest level is F.l; with acc the result is added
+// to z (second visit).
+template <typename T>
+__global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
+    BS_PDL_ENTRY();
+    const int k = blockIdx.x;
+    if (F.lev[k] != F.l) return;
+    const MgDev& M = D.mg;
     extern __shared__ unsigned char smem[];
     T* z = (T*)smem;
     T* z2 = z + M.coarse_max;
+    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
+    const int m = fnx * fny;
+    const T* __restrict__ A = (const T*)M.A[F.l];
+    const T* __restrict__ dinv = (const T*)M.dinv[F.l];
+    const T* __restrict__ r = (const T*)M.r[F.l];
     const T w = (T)M.omega;
     for (int q = threadIdx.x; q < m; q += blockDim.x) z[q] = 0;
     __syncthreads();
     for (int it = 0; it < M.coarse_sweeps; ++it) {
         for (int q = threadIdx.x; q < m; q += blockDim.x) {
-            const int i = q % C.ny, j = q / C.ny;
-            const int c = C.off + q;
+            const int i = q % fny, j = q / fny;
+            const int c = fo + q;
             T ax = 0;
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                const int ni = i + (k % 3) - 1, nj = j + (k / 3) - 1;
-                if (ni < 0 || nj < 0 || ni >= C.ny || nj >= C.nx) continue;
-                ax += C.A[(long)k * C.n + c] * z[nj * C.ny + ni];
+            for (int t = 0; t < 9; ++t) {
+                const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+                if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
+                ax += __ldg(A + (long)t * F.n + c) * z[nj * fny + ni];
             }
-            z2[q] = z[q] + w * C.dinv[c] * (C.r[c] - ax);
+            z2[q] = z[q] + w * __ldg(dinv + c) * (r[c] - ax);
         }
         __syncthreads();
         for (int q = threadIdx.x; q < m; q += blockDim.x) z[q] = z2[q];
         __syncthreads();
     }
-    T* out = (T*)M.z[L];
-    for (int q = threadIdx.x; q < m; q += blockDim.x) out[C.off + q] = z[q];
-}
-
-// Levels l+1 -> l: prolongation (constant per box, scaled) + one post-sweep.
-template <typename T>
-__global__ void k_mg_up(Dev D, int l) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const MgDev& M = D.mg;
-    if (c >= M.n[l]) return;
-    const int s = M.scene_of[l][c];
-    if (mg_skip(D, s) || l >= D.par[s].mg_lev) return;   // the coarse solve wrote this level
-    const LevelView<T> F = view<T>(M, l, s);
-    const int q = c - F.off;
-    const int i = q % F.ny, j = q / F.ny;
-    const int nyc = M.ny[l + 1][s], oc = M.off[l + 1][s];
-    const T* e = (const T*)M.z[l + 1];
-    const T w = (T)M.omega, cs = (T)M.cscale;
-    const T wp = M.prec ? w : (T)0;
-    auto zval = [&](int ii, int jj) -> T {
-        const int nb = F.off + jj * F.ny + ii;
-        return wp * F.r[nb] * F.dinv[nb] + cs * e[oc + (jj / 2) * nyc + (ii / 2)];
-    };
-    const T zc = zval(i, j);
-    T ax = 0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        const int ni = i + (k % 3) - 1, nj = j + (k / 3) - 1;
-        if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-        ax += F.A[(long)k * F.n + c] * (k == 4 ? zc : zval(ni, nj));
-    }
-    ((T*)M.z[l])[c] = zc + w * F.dinv[c] * (F.r[c] - ax);
+    T* out = (T*)M.z[F.l];
+    for (int q = threadIdx.x; q < m; q += blockDim.x) out[fo + q] = acc ? out[fo + q] + z[q] : z[q];
 }
 
 // Level 0 post-sweep after the prolongation; writes the preconditioned
 // vector (FP64).
 template <typename T>
 __global__ void k_mg_l0_up(Dev D, double* __restrict__ out) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -316,41 +425,59 @@ inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }
 template <typename T>
 void setup_t(const Dev& D, const Launch& L) {
     int q = tbegin(L, K_MG_GAL0);
-    k_mg_dinv0<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
-    k_mg_gal0<T><<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
+    launch_pdl(L, k_mg_dinv0<T>, L.nblk_rows, BS_THREADS, 0, D);
+    launch_pdl(L, k_mg_gal0<T>, gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, D);
     tend(L, q);
     *L.launches += 1;
     for (int l = 1; l < D.mg.nlev; ++l) {
         q = tbegin(L, K_MG_GALC);
-        k_mg_galc<T><<<gdiv(D.mg.n[l + 1], 128), 128, 0, L.stream>>>(D, l);
+        launch_pdl(L, k_mg_galc<T>, gdiv(D.mg.n[l + 1], 128), 128, 0, D, l);
         tend(L, q);
     }
+}
+
+// Cycle on level l >= 1 (input r[l], output z[l]); acc: add to z[l].
+// Levels 1..wlev visit level l+1 twice (W), deeper levels once (V).
+// Levels no scene needs launch nothing.
+template <typename T>
+void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
+    const MgLevel* G = L.mglev;
+    const unsigned char need = L.mgneed[l];
+    if (!(need & 1)) return;
+    int q;
+    if (need & 4) {
+        q = tbegin(L, K_MG_COARSE);
+        launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
+        tend(L, q);
+    }
+    if (!(need & 2)) return;
+    q = tbegin(L, K_MG_DOWN);
+    launch_pdl(L, k_mg_down<T>, gdiv(D.mg.n[l + 1], 128), 128, 0, D, G[l], G[l + 1]);
+    tend(L, q);
+    cycle_t<T>(D, L, l + 1, 0);
+    if (l <= D.mg.wlev) {
+        q = tbegin(L, K_MG_RESID);
+        launch_pdl(L, k_mg_resid<T>, gdiv(D.mg.n[l + 1], 128), 128, 0, D, G[l + 1]);
+        tend(L, q);
+        cycle_t<T>(D, L, l + 1, 1);
+    }
+    q = tbegin(L, K_MG_UP);
+    launch_pdl(L, k_mg_up<T>, gdiv(D.mg.n[l], 128), 128, 0, D, G[l], G[l + 1], acc);
+    tend(L, q);
 }
 
 template <typename T>
 void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
     (void)in;   // the Krylov stream already wrote the input (mg_put_input)
     int q = tbegin(L, K_MG_L0DOWN);
-    k_mg_l0_down<T><<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
+    launch_pdl(L, k_mg_l0_down<T>, gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, D);
     tend(L, q);
-    for (int l = 1; l < D.mg.nlev; ++l) {
-        q = tbegin(L, K_MG_DOWN);
-        k_mg_down<T><<<gdiv(D.mg.n[l + 1], 128), 128, 0, L.stream>>>(D, l);
-        tend(L, q);
-    }
-    q = tbegin(L, K_MG_COARSE);
-    k_mg_coarse<T><<<D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), L.stream>>>(D);
-    tend(L, q);
-    for (int l = D.mg.nlev - 1; l >= 1; --l) {
-        q = tbegin(L, K_MG_UP);
-        k_mg_up<T><<<gdiv(D.mg.n[l], 128), 128, 0, L.stream>>>(D, l);
-        tend(L, q);
-    }
+    cycle_t<T>(D, L, 1, 0);
     q = tbegin(L, K_MG_PROLONG);
-    k_mg_l0_prolong<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    launch_pdl(L, k_mg_l0_prolong<T>, L.nblk_rows, BS_THREADS, 0, D);
     tend(L, q);
     q = tbegin(L, K_MG_L0UP);
-    k_mg_l0_up<T><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, out);
+    launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out);
     tend(L, q);
 }
 

@@ -59,6 +59,7 @@ __device__ __forceinline__ bool scene_done(const Dev& D, int s) { return D.dyn[s
 
 // ---------------------------------------------------------------- FP64
 __global__ void k_init64(Dev D, int* nconv) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,6 +103,7 @@ __global__ void k_init64(Dev D, int* nconv) {
 // KP: p = r + beta (p - omega v)   (streaming; beta = 0 on the first iteration);
 // also writes the V-cycle input (mgmode 1: FP64, 2: FP32)
 __global__ void k_pupd64(Dev D, int mgmode) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -138,6 +140,7 @@ __device__ __forceinline__ double spmv_row64(const Dev& D, const double* __restr
 // K1: v = A u (u = p, or M^-1 p when preconditioned);  partial (rhat, v);
 // finisher: alpha
 __global__ void k_it1_64(Dev D, const double* __restrict__ u) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -162,6 +165,7 @@ __global__ void k_it1_64(Dev D, const double* __restrict__ u) {
 
 // KS: s = r - alpha v   (streaming), plus the V-cycle input as in KP
 __global__ void k_supd64(Dev D, int mgmode) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -174,6 +178,7 @@ __global__ void k_supd64(Dev D, int mgmode) {
 
 // K2: t = A u (u = s, or M^-1 s);  partials (t,s), (t,t);  finisher: omega
 __global__ void k_it2_64(Dev D, const double* __restrict__ u) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -197,6 +202,7 @@ __global__ void k_it2_64(Dev D, const double* __restrict__ u) {
 // K3: x += alpha pu + omega su;  r = s - omega t;  partials (rhat, r), (r,r);
 // finisher: beta, convergence
 __global__ void k_it3_64(Dev D, const double* __restrict__ pu, const double* __restrict__ su, int* nconv) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (scene_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -261,6 +267,7 @@ __global__ void k_it3_64(Dev D, const double* __restrict__ pu, const double* __r
 // is done when ||r64|| <= tol ||b||.  Otherwise the inner FP32 BiCGStab
 // solves A32 d = r64/||r64|| to inner_tol and x += ||r64|| d.
 __global__ void k_mx_res(Dev D, int* nconv) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const ScenePar& P = D.par[s];
     SceneDyn& Y = D.dyn[s];
@@ -296,6 +303,7 @@ __global__ void k_mx_res(Dev D, int* nconv) {
 
 // inner init: r = r64 / ||r64|| in FP32, rhat = r, p = v = d = 0
 __global__ void k_mx_init(Dev D, int* nconv) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const SceneDyn& Y0 = D.dyn[s];
     if (Y0.outer < 0) return;
@@ -362,6 +370,7 @@ __device__ __forceinline__ float spmv_row32(const Dev& D, const float* __restric
 }
 
 __global__ void k_mx_it1(Dev D, const float* __restrict__ p, const float* __restrict__ v, float* pn, float* vn) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (inner_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -388,6 +397,7 @@ __global__ void k_mx_it1(Dev D, const float* __restrict__ p, const float* __rest
 }
 
 __global__ void k_mx_it2(Dev D, const float* __restrict__ v) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (inner_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -411,6 +421,7 @@ __global__ void k_mx_it2(Dev D, const float* __restrict__ v) {
 }
 
 __global__ void k_mx_it3(Dev D, const float* __restrict__ p, int* nconv) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (inner_done(D, s)) return;
     const ScenePar& P = D.par[s];
@@ -444,6 +455,7 @@ __global__ void k_mx_it3(Dev D, const float* __restrict__ p, int* nconv) {
 
 // x += ||r64|| d
 __global__ void k_mx_update(Dev D) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const SceneDyn& Y = D.dyn[s];
     if (Y.outer < 0) return;
@@ -454,6 +466,7 @@ __global__ void k_mx_update(Dev D) {
 
 // FP32 copy of the assembled FP64 matrix values (inner operator)
 __global__ void k_mx_convert(Dev D) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r == D.par[s].row0) {
@@ -472,6 +485,7 @@ __global__ void k_mx_convert(Dev D) {
 
 // true FP64 residual ||b - A x|| / ||b|| for every scene (no early exit)
 __global__ void k_true_res64(Dev D) {
+    BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     const ScenePar& P = D.par[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -510,7 +524,7 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     if (precond) {
         if (mg_prec == BS_PREC_MIXED) {
             q = tbegin(L, K_MX_CONV);
-            k_mx_convert<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+            launch_pdl(L, k_mx_convert, L.nblk_rows, BS_THREADS, 0, D);
             tend(L, q);
         }
         mg_setup(D, L, mg_prec);
@@ -519,32 +533,34 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     const double* su = precond ? D.sv2 : D.ss;   // M^-1 s
     cudaMemsetAsync(d_nconv, 0, sizeof(int), L.stream);
     q = tbegin(L, K_BICG_INIT);
-    k_init64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+    launch_pdl(L, k_init64, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
     tend(L, q);
     const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
     auto iteration = [&]() {
         int q2 = tbegin(L, K_BICG_PUPD);
-        k_pupd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, mgmode);
+        launch_pdl(L, k_pupd64, L.nblk_rows, BS_THREADS, 0, D, mgmode);
         tend(L, q2);
         if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
         q2 = tbegin(L, K_BICG_IT1);
-        k_it1_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu);
+        launch_pdl(L, k_it1_64, L.nblk_rows, BS_THREADS, 0, D, pu);
         tend(L, q2);
         q2 = tbegin(L, K_BICG_SUPD);
-        k_supd64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, mgmode);
+        launch_pdl(L, k_supd64, L.nblk_rows, BS_THREADS, 0, D, mgmode);
         tend(L, q2);
         if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
         q2 = tbegin(L, K_BICG_IT2);
-        k_it2_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, su);
+        launch_pdl(L, k_it2_64, L.nblk_rows, BS_THREADS, 0, D, su);
         tend(L, q2);
         q2 = tbegin(L, K_BICG_IT3);
-        k_it3_64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, pu, su, d_nconv);
+        launch_pdl(L, k_it3_64, L.nblk_rows, BS_THREADS, 0, D, pu, su, d_nconv);
         tend(L, q2);
     };
-    // capture one iteration as a CUDA graph (not while per-kernel events are on)
+    // capture one convergence-check chunk (check_every iterations; an
+    // iteration of a converged scene returns at once) as a CUDA graph, not
+    // while per-kernel events are on
     IterGraph* G = L.graph;
     bool use_graph = G && !(L.timer && L.timer->mask);
-    if (use_graph && !(G->valid && G->precond == precond && G->prec == mg_prec &&
+    if (use_graph && !(G->valid && G->precond == precond && G->prec == mg_prec && G->chunk == check_every &&
                        std::memcmp(&G->key, &D, sizeof(Dev)) == 0)) {
         if (G->exec) cudaGraphExecDestroy(G->exec);
         G->exec = nullptr;
@@ -552,13 +568,14 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
         const int64_t before = *L.launches;
         cudaGraph_t gr = nullptr;
         if (cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-            iteration();
+            for (int c = 0; c < check_every; ++c) iteration();
             if (cudaStreamEndCapture(L.stream, &gr) == cudaSuccess && gr &&
                 cudaGraphInstantiate(&G->exec, gr, 0) == cudaSuccess) {
                 G->valid = true;
                 G->key = D;
                 G->precond = precond;
                 G->prec = mg_prec;
+                G->chunk = check_every;
                 G->nkernels = *L.launches - before;
             }
             if (gr) cudaGraphDestroy(gr);
@@ -571,20 +588,19 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     while (it < maxit) {
         cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
         cudaEventRecord(ev, L.stream);
-        for (int c = 0; c < check_every && it < maxit; ++c, ++it) {
-            if (use_graph) {
-                cudaGraphLaunch(G->exec, L.stream);
-                *L.launches += G->nkernels;
-            } else {
-                iteration();
-            }
+        if (use_graph) {
+            cudaGraphLaunch(G->exec, L.stream);
+            *L.launches += G->nkernels;
+            it += check_every;
+        } else {
+            for (int c = 0; c < check_every && it < maxit; ++c, ++it) iteration();
         }
         cudaEventSynchronize(ev);
         timer_collect(L.timer, false);
         if (*h_nconv >= D.nscene) break;
     }
     q = tbegin(L, K_TRUERES);
-    k_true_res64<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    launch_pdl(L, k_true_res64, L.nblk_rows, BS_THREADS, 0, D);
     tend(L, q);
 }
 
@@ -594,7 +610,7 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
     // FP32-inner iterative refinement (kept for systems whose condition number
     // times the FP32 unit round-off is well below one)
     int q = tbegin(L, K_MX_CONV);
-    k_mx_convert<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+    launch_pdl(L, k_mx_convert, L.nblk_rows, BS_THREADS, 0, D);
     tend(L, q);
     cudaMemsetAsync(d_nconv, 0, 2 * sizeof(int), L.stream);
     int max_outer = 0;
@@ -604,7 +620,7 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
     for (int outer = 0; outer <= max_outer; ++outer) {
         float *p = D.fp, *v = D.fv, *p2 = D.fp2, *v2 = D.fv2;   // k_mx_init zeroes fp, fv
         q = tbegin(L, K_MX_RES);
-        k_mx_res<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+        launch_pdl(L, k_mx_res, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
         tend(L, q);
         cudaMemcpyAsync(h_nconv, d_nconv, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
         cudaStreamSynchronize(L.stream);
@@ -613,7 +629,7 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
         // inner-converged counter starts with the outer-converged scenes
         cudaMemcpyAsync(d_nconv, d_nconv + 1, sizeof(int), cudaMemcpyDeviceToDevice, L.stream);
         q = tbegin(L, K_MX_INIT);
-        k_mx_init<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, d_nconv);
+        launch_pdl(L, k_mx_init, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
         tend(L, q);
         int it = 0;
         while (it < maxit) {
@@ -621,13 +637,13 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
             cudaEventRecord(ev, L.stream);
             for (int c = 0; c < check_every && it < maxit; ++c, ++it) {
                 q = tbegin(L, K_MX_IT1);
-                k_mx_it1<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p, v, p2, v2);
+                launch_pdl(L, k_mx_it1, L.nblk_rows, BS_THREADS, 0, D, p, v, p2, v2);
                 tend(L, q);
                 q = tbegin(L, K_MX_IT2);
-                k_mx_it2<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, v2);
+                launch_pdl(L, k_mx_it2, L.nblk_rows, BS_THREADS, 0, D, v2);
                 tend(L, q);
                 q = tbegin(L, K_MX_IT3);
-                k_mx_it3<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, p2, d_nconv);
+                launch_pdl(L, k_mx_it3, L.nblk_rows, BS_THREADS, 0, D, p2, d_nconv);
                 tend(L, q);
                 float* t;
                 t = p; p = p2; p2 = t;
@@ -638,7 +654,7 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
             if (*h_nconv >= D.nscene) break;
         }
         q = tbegin(L, K_MX_UPD);
-        k_mx_update<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D);
+        launch_pdl(L, k_mx_update, L.nblk_rows, BS_THREADS, 0, D);
         tend(L, q);
     }
 }

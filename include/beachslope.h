@@ -189,7 +189,9 @@ int bs_get_matrix(struct bs_ctx* ctx, int32_t scene, double* diag, double* off, 
 /* Solver tunables, set by the project autotuner (beach-slope_gb300/autotune.py):
  * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
  * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),
- * "mg_coarse_sweeps", "ppe_precond"; bs_get_option also reads "mg_levels". */
+ * "mg_coarse_sweeps", "mg_wlev" (coarse levels 1..mg_wlev visit the next
+ * level twice: W-cycle on top, V-cycle below), "ppe_precond";
+ * bs_get_option also reads "mg_levels". */
 int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
 int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);
 
