@@ -259,6 +259,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(bucket, C * BS_NCAT); A(cell_total, C); A(coderank, R);
     A(cell_maxvel, C); A(cell_maxeddy, C);
     A(gx, (size_t)gr); A(gy, (size_t)gr); A(gv, (size_t)gr); A(gcell_start, C); A(gcell_end, C);
+    A(gxr, (size_t)gr); A(gyr, (size_t)gr); A(xr, R); A(yr, R);
     A(part, (size_t)blk * BS_MAXDOT);
     A(err_word, 1);
 #undef A
@@ -524,12 +525,16 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
         std::stable_sort(gk.begin(), gk.end());
         const int m = (int)gk.size();
         std::vector<double> gx(m), gy(m), gv(m);
+        std::vector<float> gxr(m), gyr(m);
         std::vector<int> gs(P.ncell, 0), ge(P.ncell, 0), cnt(P.ncell, 0);
         for (int q = 0; q < m; ++q) {
             const int k = gk[q].second;
             gx[q] = gr->x[k];
             gy[q] = gr->y[k];
             gv[q] = gr->mass[k] / gr->rho[k];
+            const int cj = gk[q].first / p.celly + 1, ci = gk[q].first % p.celly + 1;
+            gxr[q] = (float)(gx[q] - xleft_of(p, cj));
+            gyr[q] = (float)(gy[q] - ybot_of(p, ci));
             cnt[gk[q].first]++;
         }
         int acc = ctx->grain0[s];
@@ -543,6 +548,8 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
             CK(cudaMemcpy(D.gx + g0, gx.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
             CK(cudaMemcpy(D.gy + g0, gy.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
             CK(cudaMemcpy(D.gv + g0, gv.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(D.gxr + g0, gxr.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(D.gyr + g0, gyr.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
         }
         CK(cudaMemcpy(D.gcell_start + P.cell0, gs.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(D.gcell_end + P.cell0, ge.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));

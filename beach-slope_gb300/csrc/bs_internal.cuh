@@ -106,6 +106,7 @@ struct MgLevel {
 struct Dev {
     // particle fields (current buffer)
     double *x, *y, *xs, *ys, *vx, *vy, *vxs, *vys, *p, *mass, *rho, *oden, *ovol, *con;
+    float *xr, *yr;                 // position relative to the row's cell corner (xleft, ybot), FP32
     double *vol, *nu;               // derived: m/rho, vis(oden)/oden
     int8_t* tid;
     uint8_t* flags;
@@ -149,6 +150,7 @@ struct Dev {
     double *cell_maxvel, *cell_maxeddy;
     // grains (static, sorted by cell)
     double *gx, *gy, *gv;           // gv = mass/density
+    float *gxr, *gyr;               // grain position relative to its cell corner, FP32
     int *gcell_start, *gcell_end;
     int ncell_total, nrow_total, nblk_total, nscene;
     int kmax;
@@ -196,20 +198,19 @@ __device__ __forceinline__ float bs_Wf(float r, const ScenePar& P) {
     return (float)P.cn1 * t1 + (float)P.cn2 * t2;
 }
 
-// r = sqrt(s) and 1/r in FP64 from an FP32 rsqrt seed and two Newton steps
-// (relative error ~1e-16, not correctly rounded): used where the exact IEEE
-// sqrt is not required (mixed-mode pair quantities, grain distances).
+// r = sqrt(s) and 1/r in FP64 from an FP32 rsqrt seed and one Newton step
+// (relative error ~1e-13: far below the FP32 rounding of the stored pair
+// values, not correctly rounded): used where the exact IEEE sqrt is not
+// required (mixed-mode pair quantities, grain distances).
 __device__ __forceinline__ void fast_r64(double s, double& r, double& ir) {
     double y = (double)rsqrtf((float)s);
-    y = y * (1.5 - 0.5 * s * y * y);
     y = y * (1.5 - 0.5 * s * y * y);
     ir = y;
     r = s * y;
 }
-// 1/d in FP64 from an FP32 reciprocal seed and two Newton steps
+// 1/d in FP64 from an FP32 reciprocal seed and one Newton step (~1e-14)
 __device__ __forceinline__ double fast_rcp64(double d) {
     double y = (double)__frcp_rn((float)d);
-    y = y * (2.0 - d * y);
     y = y * (2.0 - d * y);
     return y;
 }
@@ -301,7 +302,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_COUNT
+    K_MG_RESID, K_RELPOS, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {

@@ -52,6 +52,29 @@ __device__ __forceinline__ bool quad_cells(const ScenePar& P, int c, double xi, 
     return true;
 }
 
+// corner of cell cq relative to the corner of cell c (both global indices),
+// rounded to FP32 once
+__device__ __forceinline__ void cell_offset(const ScenePar& P, int c, int cq, float& ox, float& oy) {
+    const int l = c - P.cell0, lq = cq - P.cell0;
+    const int i = l % P.celly + 1, j = l / P.celly + 1;
+    const int iq = lq % P.celly + 1, jq = lq / P.celly + 1;
+    ox = (float)(cell_xleft(P, jq) - cell_xleft(P, j));
+    oy = (float)(cell_ybot(P, iq) - cell_ybot(P, i));
+}
+
+// FP32 position of every row relative to its cell's corner (the search's
+// candidate prefilter reads 8 bytes per candidate and no FP64)
+__global__ void k_relpos(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const int lc = D.cell[r] - P.cell0;
+    const int i = lc % P.celly + 1, j = lc / P.celly + 1;
+    D.xr[r] = (float)(D.x[r] - cell_xleft(P, j));
+    D.yr[r] = (float)(D.y[r] - cell_ybot(P, i));
+}
+
 template <typename T>
 __device__ __forceinline__ T ld(const void* p, long e) { return ((const T*)p)[e]; }
 template <typename T>
@@ -74,19 +97,20 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         const int kmax = D.kmax;
         const double twoh = P.twoh;
         // Phase 1 (divergent candidate scan): FP32 prefilter of the squared
-        // distance -- outside [lo, hi] the exact FP64 test cannot disagree
-        // (FP32 rounding of d^2 is < 3 ulp) -- and the exact test of
-        // functions.f90:38 / search.f90:59 (IEEE sqrt, no FMA) inside it.
-        // Only indices are appended, so the warp's divergence is cheap.
+        // distance from positions relative to the cell corners (rounding
+        // error of d^2 below 2e-6 relative for coordinates within a cell) --
+        // outside [lo, hi] the exact FP64 test cannot disagree -- and the
+        // exact test of functions.f90:38 / search.f90:59 (IEEE sqrt, no FMA,
+        // FP64 positions) inside it.  Only indices are appended, so the
+        // warp's divergence is cheap.
         const float t2f = (float)(twoh * twoh);
         const float thr_hi = t2f * (1.0f + 1e-5f), thr_lo = t2f * (1.0f - 1e-5f);
         int cnt = 0;
-        auto test = [&](int rj, double xj, double yj) {
-            const double dx = xj - xi, dy = yj - yi;
-            const float fx = (float)dx, fy = (float)dy;
+        auto test = [&](int rj, float fx, float fy) {
             const float d2f = fx * fx + fy * fy;
             if (d2f > thr_hi) return;
             if (d2f >= thr_lo) {
+                const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
                 const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (!(rad < twoh)) return;
             }
@@ -94,16 +118,19 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             ++cnt;
         };
         if (ok) {
+            const float xri = D.xr[r], yri = D.yr[r];
             for (int q = 0; q < 4; ++q) {
+                float ox, oy;
+                cell_offset(P, D.cell[r], cc[q], ox, oy);
                 const int r1 = D.cell_end[cc[q]];
                 int rj = D.cell_start[cc[q]];
                 for (; rj + 1 < r1; rj += 2) {   // two independent candidate loads in flight
-                    const double x0 = __ldg(D.x + rj), y0 = __ldg(D.y + rj);
-                    const double x1 = __ldg(D.x + rj + 1), y1 = __ldg(D.y + rj + 1);
-                    if (rj != r) test(rj, x0, y0);   // (tid, matid) self-exclusion
-                    if (rj + 1 != r) test(rj + 1, x1, y1);
+                    const float x0 = __ldg(D.xr + rj) + ox, y0 = __ldg(D.yr + rj) + oy;
+                    const float x1 = __ldg(D.xr + rj + 1) + ox, y1 = __ldg(D.yr + rj + 1) + oy;
+                    if (rj != r) test(rj, x0 - xri, y0 - yri);   // (tid, matid) self-exclusion
+                    if (rj + 1 != r) test(rj + 1, x1 - xri, y1 - yri);
                 }
-                if (rj < r1 && rj != r) test(rj, __ldg(D.x + rj), __ldg(D.y + rj));
+                if (rj < r1 && rj != r) test(rj, (__ldg(D.xr + rj) + ox) - xri, (__ldg(D.yr + rj) + oy) - yri);
             }
         }
         if (cnt > kmax) set_err(D, R.s, BS_ERR_NBR_OVERFLOW);
@@ -181,9 +208,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 else if (own_q == 1) { ord[0] = cc[1]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[3]; }
                 else { ord[0] = cc[3]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[1]; }
                 const double wsolid = 1.0 - P.por * 1.0;
+                const float t2f = (float)(P.twoh * P.twoh) * (1.0f + 1e-5f);
+                const float xri = D.xr[r], yri = D.yr[r];
                 for (int q = 0; q < 4; ++q) {
+                    float ox, oy;
+                    cell_offset(P, D.cell[r], ord[q], ox, oy);
                     const int g1 = D.gcell_end[ord[q]];
                     for (int g = D.gcell_start[ord[q]]; g < g1; ++g) {
+                        // FP32 prefilter (as in the neighbour scan): a grain
+                        // rejected here is outside 2h in FP64 as well
+                        const float fx = (__ldg(D.gxr + g) + ox) - xri, fy = (__ldg(D.gyr + g) + oy) - yri;
+                        if (fx * fx + fy * fy > t2f) continue;
                         const double dx = xi - D.gx[g], dy = yi - D.gy[g];
                         if (sizeof(T) == 4) {   // mixed: Newton sqrt (W(2h) = 0: the cut needs no exact test)
                             const double s2 = dx * dx + dy * dy;
@@ -703,6 +738,7 @@ namespace bs {
     } while (0)
 
 void search(const Dev& D, const Launch& L, int precision, int do_search, int do_effpor) {
+    BS_PLAIN(K_RELPOS, k_relpos, D);
     BS_DISPATCH(K_SEARCH, precision, k_search, D, do_search, do_effpor);
 }
 void freesurf(const Dev& D, const Launch& L) { BS_PLAIN(K_FREESURF, k_freesurf, D); }
