@@ -46,6 +46,7 @@ class Params(C.Structure):
         ("xlcutoff", _d), ("ytcutoff", _d),
         ("ppe_tol", _d), ("ppe_maxit", _i), ("ppe_stop", _i), ("precision", _i),
         ("kmax", _i), ("mixed_inner_tol", _d), ("mixed_max_outer", _i), ("ppe_precond", _i),
+        ("wc_c0", _d), ("wc_gamma", _d), ("wc_delta", _d), ("wc_ysurf", _d), ("wc_form", _i), ("wc_pad", _i),
     ]
 
     def as_dict(self):
@@ -87,6 +88,10 @@ def default_params():
     p.mixed_inner_tol = 1e-3
     p.mixed_max_outer = 0   # 0: the mixed mode solves the PPE with the FP64 BiCGStab
     p.ppe_precond = 1       # multigrid V-cycle preconditioner
+    p.wc_c0 = 0.0           # set per scene (10 sqrt(g depth))
+    p.wc_gamma = 7.0        # t_gam, initialize.f90:46
+    p.wc_delta = 0.1        # delt, initialize.f90:40
+    p.wc_ysurf = 0.0        # set per scene (still-water level)
     return p
 
 

@@ -60,6 +60,12 @@ def _load():
         "bs_density_update": (C.c_int, [vp]),
         "bs_timestep": (C.c_int, [vp]),
         "bs_step": (C.c_int, [vp, i32]),
+        "bs_wcsph_continuity": (C.c_int, [vp]),
+        "bs_wcsph_update_density": (C.c_int, [vp]),
+        "bs_wcsph_eos": (C.c_int, [vp]),
+        "bs_wcsph_pressure_to_density": (C.c_int, [vp]),
+        "bs_wcsph_wall_pressure": (C.c_int, [vp]),
+        "bs_wcsph_step": (C.c_int, [vp, i32]),
         "bs_bicgstab_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, vp, vp]),
         "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
         "bs_event_record": (C.c_int, [vp, i32]),
@@ -193,6 +199,10 @@ class Context:
 
     def step(self, n=1):
         self._check(lib.bs_step(self.h, n), "step")
+
+    def wcsph_step(self, n=1):
+        """WCSPH step (continuity + Tait EOS instead of the PPE), n times."""
+        self._check(lib.bs_wcsph_step(self.h, n), "wcsph_step")
 
     def sync(self):
         self._check(lib.bs_sync(self.h), "sync")

@@ -180,6 +180,7 @@ void bs_params_default(bs_params* p) {
     p->xlcutoff = -1e300; p->ytcutoff = 1e300;
     p->ppe_tol = 1e-8; p->ppe_maxit = 5000; p->ppe_stop = BS_STOP_RELRES; p->precision = BS_PREC_FP64;
     p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 0;
+    p->wc_gamma = 7.0; p->wc_delta = 0.1;
 }
 
 int bs_set_device(int32_t device) {
@@ -221,6 +222,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
         P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;
         P.xlcutoff = p.xlcutoff; P.ytcutoff = p.ytcutoff; P.ppe_tol = p.ppe_tol; P.inner_tol = p.mixed_inner_tol;
+        P.wc_c0 = p.wc_c0; P.wc_gamma = p.wc_gamma; P.wc_delta = p.wc_delta; P.wc_ysurf = p.wc_ysurf;
+        P.wc_form = p.wc_form;
         P.cellx = p.cellx; P.celly = p.celly; P.ncell = p.cellx * p.celly; P.cell0 = cell;
         P.row0 = row; P.cap = cap; P.kmax = ctx->kmax; P.maxit = p.ppe_maxit;
         P.adaptive_dt = p.adaptive_dt; P.scalar_on = p.scalar_on; P.precision = p.precision; P.stop_rule = p.ppe_stop;
@@ -251,7 +254,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(tid2, R); A(flags2, R); A(pid2, R); A(cell2, R);
     A(por, R); A(resx, R); A(resy, R); A(nut, R); A(tke, R); A(varts, R); A(gradvx, R); A(vel, R); A(cdiff, R);
     A(c0, R); A(c1, R); A(c2, R); A(c3, R); A(Dp0, R); A(Dp1, R); A(Dp2, R); A(Dp3, R); A(Dt, R);
-    A(rho_new, R); A(vol_new, R); A(con_new, R);
+    A(rho_new, R); A(vol_new, R); A(con_new, R); A(tden, R); A(whyd, R);
     A(ncount, R); A(nidx, E);
     A(adiag, R); A(rhs, R);
     A(sr, R); A(srhat, R); A(sp, R); A(sp2, R); A(sv, R); A(sv2, R); A(ss, R); A(st, R); A(sxd, R);
@@ -857,6 +860,76 @@ int bs_timestep(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     bs::cell_max_timestep(ctx->D, launch_of(ctx), 0, 1);
     return check_launch(ctx);
+}
+
+// ---- WCSPH (wcsph.f90)
+int bs_wcsph_continuity(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::wc_continuity(ctx->D, launch_of(ctx), ctx->precision);
+    return check_launch(ctx);
+}
+int bs_wcsph_update_density(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::wc_rows(ctx->D, launch_of(ctx), 1);
+    return check_launch(ctx);
+}
+int bs_wcsph_eos(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::wc_rows(ctx->D, launch_of(ctx), 2);
+    return check_launch(ctx);
+}
+int bs_wcsph_pressure_to_density(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::wc_rows(ctx->D, launch_of(ctx), 4);
+    return check_launch(ctx);
+}
+int bs_wcsph_wall_pressure(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::wc_wall_pressure(ctx->D, launch_of(ctx), ctx->precision);
+    return check_launch(ctx);
+}
+
+// WCSPH step: bs_step's sequence with the PPE replaced by continuity,
+// updateden, dentopress and the wall pressure; the porosity pass keeps the
+// continuity density and densityupdate is left out.
+int bs_wcsph_step(bs_ctx* ctx, int32_t nsteps) {
+    if (!ctx || nsteps < 0) return BS_E_ARG;
+    Dev& D = ctx->D;
+    for (int it = 0; it < nsteps; ++it) {
+        bs::Launch L = launch_of(ctx);
+        bs::advance_time(D, L);
+        bool any_scalar = false;
+        for (auto& p : ctx->prm) any_scalar |= p.scalar_on != 0;
+        if (any_scalar) {
+            if (!ctx->disp_ready) {
+                bs::disp(D, L);
+                ctx->disp_ready = true;
+            }
+            for (int j1 = 0; j1 < ctx->max_solsteps; ++j1) st_scalar(ctx, j1);
+        }
+        st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
+        st_search(ctx, 1, 2);                // neighbour + effpor keeping the density
+        bs::eddy(D, L, ctx->precision, 1, 1, 0);
+        bs::int_vel(D, L, ctx->precision);
+        bs::wc_continuity(D, L, ctx->precision);   // calmasscons
+        bs::wc_rows(D, L, 1 | 2);            // updateden, dentopress
+        bs::wc_wall_pressure(D, L, ctx->precision);
+        bs::comp_vel(D, L, ctx->precision, 1, 1);   // comp_vel + comp_pos
+        bs::cell_max_timestep(D, L, 1, 0);
+        st_rebin(ctx, 0, 1);                 // cellshiftalt
+        st_search(ctx, 1, 2);
+        bs::freesurf(D, L);
+        bs::shift(D, L, ctx->precision);
+        bs::apply_density(D, L, 1, 0);       // shift apply only
+        bs::cell_max_timestep(D, L, 0, 1);   // timestep
+        bs::eddy(D, L, ctx->precision, 1, 0, 1);
+        ctx->disp_ready = true;
+        int rc = check_launch(ctx);
+        if (rc) return rc;
+        rc = read_solsteps(ctx);
+        if (rc) return rc;
+    }
+    return 0;
 }
 
 // Full production step, main.f90:199-272 (open-boundary buffers excluded).

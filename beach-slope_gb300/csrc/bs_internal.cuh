@@ -43,6 +43,8 @@ struct ScenePar {                 // per-scene constants
     double csh, maxshift, sig1;
     double xlcutoff, ytcutoff;
     double ppe_tol, inner_tol;
+    double wc_c0, wc_gamma, wc_delta, wc_ysurf;   // WCSPH (wcsph.f90)
+    int wc_form, wc_pad;
     int cellx, celly, ncell, cell0;   // grid dims and first global cell
     int row0, cap, kmax, maxit;
     int adaptive_dt, scalar_on, precision, stop_rule;
@@ -124,6 +126,7 @@ struct Dev {
     double *c0, *c1, *c2, *c3;      // coff (L^-1), search.f90:276-278
     double *Dp0, *Dp1, *Dp2, *Dp3, *Dt;   // scalar dispersion per particle
     double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
+    double *tden, *whyd;            // WCSPH: continuity density, hydrostatic Tait density per row
     double *con_new;
     // neighbour lists (ELL)
     int* ncount;
@@ -302,7 +305,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -386,6 +389,11 @@ void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_tim
 void shift(const Dev& D, const Launch& L, int precision);
 void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density);
 void scalar(const Dev& D, const Launch& L, int precision, int substep);
+// WCSPH (wcsph.f90): continuity, row updates (bit0 updateden, bit1
+// dentopress, bit2 presstoden), wall pressure of the WCSPH step
+void wc_continuity(const Dev& D, const Launch& L, int precision);
+void wc_rows(const Dev& D, const Launch& L, int mode);
+void wc_wall_pressure(const Dev& D, const Launch& L, int precision);
 void advance_time(const Dev& D, const Launch& L);
 void derive_fields(const Dev& D, const Launch& L);
 // solver

@@ -238,8 +238,13 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             phi = 1.0 - sf;
             const double od = D.oden[r];
             const double rn = phi * od;
-            D.rho_new[r] = rn;
-            D.vol_new[r] = D.mass[r] / rn;
+            if (do_effpor == 2) {   // WCSPH: the density is the continuity equation's
+                D.rho_new[r] = D.rho[r];
+                D.vol_new[r] = D.vol[r];
+            } else {
+                D.rho_new[r] = rn;
+                D.vol_new[r] = D.mass[r] / rn;
+            }
             const double phi3 = phi * phi * phi;
             const double Fch = 1.750 / sqrt(150.0 * phi3);
             const double vx = D.vx[r], vy = D.vy[r];
@@ -723,6 +728,117 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep) {
 
 namespace bs {
 
+// ------------------------------------------------------------------ WCSPH
+// wcsph.f90, a module the reference ships but never calls.
+
+// hydrostatic Tait density at height y (the term2 expression, wcsph.f90:78-82)
+__device__ __forceinline__ double wc_hyd(const ScenePar& P, double y) {
+    const double rho = P.rho, co = P.wc_c0, gam = P.wc_gamma;
+    return rho * pow(((((P.wc_ysurf - y) * rho) * fabs(P.g)) * gam) / (rho * (co * co)) + 1.0, 1.0 / gam);
+}
+
+// per-row hydrostatic density (one pow per particle, not per pair)
+__global__ void k_wc_hyd(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    D.whyd[R.r] = wc_hyd(D.par[R.s], D.y[R.r]);
+}
+
+// calmasscons, wcsph.f90:65-129, for fluid rows: tden = rho + dt * (term1 +
+// term2), the L-corrected velocity divergence plus delta-SPH diffusion with
+// the hydrostatic correction.  As written (wc_form 0) term2 is also the
+// pair's hydrostatic difference and is overwritten by it at every
+// neighbour, so only the last neighbour's y contribution survives, and the
+// delta-SPH term runs along (r_i - r_j), which makes it anti-diffusive;
+// wc_form 1 sums the y terms over all neighbours and takes (r_j - r_i).
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_wc_continuity(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    if (!(D.tid[r] > 2)) return;
+    const ScenePar& P = D.par[R.s];
+    const double co = P.wc_c0, delt = P.wc_delta, h1 = P.h, lam = P.lam;
+    const double dt = D.dyn[R.s].dt;
+    const double xi = D.x[r], yi = D.y[r], vxi = D.vx[r], vyi = D.vy[r], rhoi = D.rho[r];
+    const double c0 = D.c0[r], c1 = D.c1[r], c2 = D.c2[r], c3 = D.c3[r];
+    const double hydi = D.whyd[r];
+    const double dfac = ((delt * 2) * h1) * co;
+    double term1 = 0.0, term2 = 0.0;
+    const int n = D.ncount[r];
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, D.kmax);
+        const int j = D.nidx[e];
+        const double rad = (double)ld<T>(D.ndist, e);
+        const double wx = (double)ld<T>(D.nkx, e), wy = (double)ld<T>(D.nky, e);
+        const double hd = D.whyd[j] - hydi;
+        // as written: term2 doubles as the hydrostatic difference and the
+        // delta term runs along (r_i - r_j) (anti-diffusive); corrected:
+        // own y sum, delta term along (r_j - r_i)
+        const double sg = (P.wc_form == 0) ? 1.0 : -1.0;
+        if (P.wc_form == 0) term2 = hd;
+        const double gx = c0 * wx + c1 * wy;
+        const double gy = c2 * wx + c3 * wy;
+        const double mj = D.mass[j], rhoj = D.rho[j];
+        const double vr = mj / rhoj, den = rad * rad + lam;
+        term1 = term1 - ((mj * (D.vx[j] - vxi)) * gx) * (rhoi / rhoj) +
+                (((dfac * (rhoj - rhoi - hd)) * (sg * (xi - D.x[j]))) * gx) * vr / den;
+        term2 = term2 - ((mj * (D.vy[j] - vyi)) * gy) * (rhoi / rhoj) +
+                (((dfac * (rhoj - rhoi - hd)) * (sg * (yi - D.y[j]))) * gy) * vr / den;
+    }
+    D.tden[r] = rhoi + (term1 + term2) * dt;
+}
+
+// per-row WCSPH updates: bit0 updateden (wcsph.f90:131-154), bit1
+// dentopress (Tait, wcsph.f90:35-63), bit2 presstoden (wcsph.f90:13-33);
+// the derived volume m/rho follows the density
+__global__ void k_wc_rows(Dev D, int mode) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    const ScenePar& P = D.par[R.s];
+    const double rho = P.rho, co = P.wc_c0, gam = P.wc_gamma;
+    double d = D.rho[r];
+    const bool fluid = D.tid[r] > 2;
+    if ((mode & 1) && fluid) d = D.tden[r];
+    if ((mode & 2) && fluid) {
+        double p = (rho * (co * co)) * (pow(d / rho, gam) - 1) / gam;
+        if (p < 0.0) {
+            p = 0.0;
+            d = rho;
+        }
+        D.p[r] = p;
+    }
+    if (mode & 4) d = rho * pow((D.p[r] * gam / (rho * (co * co))) + 1, 1 / gam);
+    if (d != D.rho[r]) {
+        D.rho[r] = d;
+        D.vol[r] = D.mass[r] / d;
+    }
+}
+
+// wall and ghost pressure of the WCSPH step (this library's boundary rule):
+// Shepard average over fluid neighbours of p_f + rho_f |g| (y_f - y_w)
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_wc_wallp(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    if (D.tid[r] == BS_TID_FLUID) return;
+    const ScenePar& P = D.par[R.s];
+    const double ag = fabs(P.g), yw = D.y[r];
+    double num = 0.0, den = 0.0;
+    const int n = D.ncount[r];
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, D.kmax);
+        const int j = D.nidx[e];
+        if (D.tid[j] != BS_TID_FLUID) continue;
+        const double w = bs_W((double)ld<T>(D.ndist, e), P);
+        num += (D.p[j] + D.rho[j] * ag * (D.y[j] - yw)) * w;
+        den += w;
+    }
+    D.p[r] = den > 0.0 ? num / den : 0.0;
+}
+
 #define BS_DISPATCH(id, prec, kern, ...)                                                          \
     do {                                                                                          \
         const int q_ = tbegin(L, id);                                                             \
@@ -758,6 +874,14 @@ void disp(const Dev& D, const Launch& L) { BS_PLAIN(K_DISP, k_disp, D); }
 void velmag(const Dev& D, const Launch& L) { BS_PLAIN(K_VELMAG, k_velmag, D); }
 void scalar(const Dev& D, const Launch& L, int precision, int substep) {
     BS_DISPATCH(K_SCALAR, precision, k_scalar, D, substep);
+}
+void wc_continuity(const Dev& D, const Launch& L, int precision) {
+    BS_PLAIN(K_WC_CONT, k_wc_hyd, D);
+    BS_DISPATCH(K_WC_CONT, precision, k_wc_continuity, D);
+}
+void wc_rows(const Dev& D, const Launch& L, int mode) { BS_PLAIN(K_WC_ROWS, k_wc_rows, D, mode); }
+void wc_wall_pressure(const Dev& D, const Launch& L, int precision) {
+    BS_DISPATCH(K_WC_WALLP, precision, k_wc_wallp, D);
 }
 
 }  // namespace bs

@@ -78,7 +78,7 @@ def porosity_field(x, y, grains, h, por):
 
 def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.05,
                 por=0.40, d50=0.005, A=0.06, x0=None, layers=3, saline_beach=True,
-                hfac=1.3, dt=1e-4, ppe_tol=1e-8, precision=abi.PREC_FP64):
+                hfac=1.3, dt=1e-4, ppe_tol=1e-8, precision=abi.PREC_FP64, wcsph=False):
     """Solitary wave on a porous beach slope in a 2-D tank.
 
     Tank [0,L]x[0,H] (inner), still depth `depth`, impermeable slope of
@@ -87,6 +87,10 @@ def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.0
     eta = A sech^2(k(x-x0)), k = sqrt(3A/(4 d^3)), u = sqrt(g/d) eta.
     The crest sits at x0 (default toe/2: a 4 m tank cannot hold the crest
     3/k upstream of a toe at 2 m).
+    With wcsph=True the state is set up for the WCSPH step: every fluid
+    particle carries the full lattice mass rho0*dx^2 (the grains still set
+    porosity and drag) and the hydrostatic Tait density of its depth; the
+    speed of sound is 10 sqrt(g d) and the still-water level d.
     Returns (params, state dict, grains dict).
     """
     p = abi.default_params()
@@ -166,6 +170,15 @@ def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.0
     parts.append(_mk(fx, fy, np.full(len(fx), abi.TID_FLUID), oden * ovol, phi * oden, oden,
                      ovol, con, vx=u, vy=w, p=pf))
     st = _cat(parts)
+    p.wc_c0 = 10.0 * math.sqrt(-g * d)
+    p.wc_ysurf = Y0 + d
+    if wcsph:
+        p.wc_form = 1   # the corrected continuity (the form as written is unstable)
+        fl = st["tid"] == abi.TID_FLUID
+        st["ovol"] = np.where(fl, dx * dx, st["ovol"])
+        st["mass"] = np.where(fl, st["oden"] * dx * dx, st["mass"])
+        c2 = p.wc_c0 ** 2
+        st["rho"] = np.where(fl, rho * (st["p"] * p.wc_gamma / (rho * c2) + 1.0) ** (1.0 / p.wc_gamma), st["rho"])
     _grid_for(p, X0 + L + (layers + 1) * dx, Y0 + H + 0.3)
     return p, st, grains
 
@@ -196,6 +209,8 @@ def lattice_scene(n=1000, dx=1e-3, jitter=0.25, seed=20261203, layers=3, hfac=1.
     parts = [_mk(wx, wy, wt, fmass, p.rho, 0.0, 0.0, 0.0),
              _mk(fx, fy, np.full(n * n, abi.TID_FLUID), fmass, p.rho, p.rho, dx * dx, -0.5)]
     st = _cat(parts)
+    p.wc_c0 = 10.0 * math.sqrt(-p.g * n * dx)
+    p.wc_ysurf = Y0 + n * dx
     _grid_for(p, X0 + (n + layers + 1) * dx, Y0 + (n + 4) * dx)
     grains = {"x": np.zeros(0), "y": np.zeros(0), "mass": np.zeros(0), "rho": np.zeros(0)}
     return p, st, grains

@@ -117,6 +117,23 @@ typedef struct bs_params {
     /* PPE preconditioner: 0 none (the reference's plain BiCGStab), 1 cell-grid
      * aggregation multigrid V-cycle (FP64 in BS_PREC_FP64, FP32 in BS_PREC_MIXED) */
     int32_t ppe_precond;
+    /* WCSPH (wcsph.f90): speed of sound co (never set by the reference,
+     * setup.f90:134; 10*sqrt(g*depth) for the beach scenes), Tait exponent
+     * t_gam (7, initialize.f90:46), delta-SPH coefficient delt (0.1,
+     * initialize.f90:40), and the still-water level that the reference
+     * writes as brrealy*distfac*(2*bl-1)+wc (wcsph.f90:78-82) */
+    double wc_c0;
+    double wc_gamma;
+    double wc_delta;
+    double wc_ysurf;
+    /* calmasscons form: 0 as the reference writes it (term2 doubles as the
+     * pair's hydrostatic difference, so only the last neighbour's y term
+     * survives, and the delta-SPH term runs along r_i - r_j, which is
+     * anti-diffusive, wcsph.f90:78-117); 1 this library's correction (y term
+     * summed over all neighbours, delta term along r_j - r_i; no reference
+     * counterpart) */
+    int32_t wc_form;
+    int32_t wc_pad;
 } bs_params;
 
 /*
@@ -221,6 +238,22 @@ int bs_timestep(struct bs_ctx* ctx);        /* timestep, integrator.f90:885     
 
 /* Full production step (main.f90:199-272) with fused kernels, nsteps times. */
 int bs_step(struct bs_ctx* ctx, int32_t nsteps);
+
+/* ---- WCSPH (wcsph.f90, a module the reference ships but does not call) --- */
+int bs_wcsph_continuity(struct bs_ctx* ctx);   /* calmasscons, wcsph.f90:65-129: tden of fluid rows */
+int bs_wcsph_update_density(struct bs_ctx* ctx); /* updateden, wcsph.f90:131-154: density = tden   */
+int bs_wcsph_eos(struct bs_ctx* ctx);          /* dentopress, wcsph.f90:35-63: Tait pressure      */
+int bs_wcsph_pressure_to_density(struct bs_ctx* ctx); /* presstoden, wcsph.f90:13-33              */
+/* Wall and ghost pressure for the WCSPH step: Shepard average over fluid
+ * neighbours of p_f + rho_f |g| (y_f - y_w).  No counterpart in the
+ * reference, which has no WCSPH boundary treatment. */
+int bs_wcsph_wall_pressure(struct bs_ctx* ctx);
+/* WCSPH step, nsteps times: the production step of bs_step with the PPE
+ * assembly and solve replaced by continuity + updateden + dentopress + wall
+ * pressure, the density kept from the continuity equation (the porosity pass
+ * and densityupdate leave it alone).  The reference has no WCSPH time loop;
+ * this composition of its routines is this library's. */
+int bs_wcsph_step(struct bs_ctx* ctx, int32_t nsteps);
 
 /* Standalone BiCGStab on a CSR system (solver.f90:129-254 with the CSR
  * operator spmv, solver.f90:53-82) -- the solvertest.f90 driver's path.

@@ -35,7 +35,7 @@ const double SP_1EM9 = (double)1e-9f;            // scalar.f90:246, integrator.f
 
 struct Particle {   // particles, particle.f90:31-47
     double mass = 0, density = 0, pressure = 0, vx = 0, vy = 0, vxs = 0, vys = 0, x = 0, y = 0,
-           xs = 0, ys = 0, con = 0, ovol = 0, oden = 0;
+           xs = 0, ys = 0, con = 0, ovol = 0, oden = 0, tden = 0;
     int tid = 0, pid = 0, matid = 0;
     bool free = false, vicinity = false, buffer = false;
 };
@@ -395,7 +395,7 @@ void neighbour(or_scene* s) {
 
 // ------------------------------------------------------------------ porosity
 // effpor + porsearch, porous.f90:32-224
-void effpor(or_scene* s) {
+void effpor(or_scene* s, bool keep_density = false) {
     const double por = s->P.por, lamk = s->P.lamk, d50 = s->P.d50, h1 = s->h;
     for_interior(s, [&](int i, int j) {
         Cell& c = s->C(i, j);
@@ -434,7 +434,7 @@ void effpor(or_scene* s) {
             }
             if (solidfrac > (1.0 - por)) solidfrac = 1.0 - por;
             pp.porosity = 1.0 - solidfrac;
-            p.density = pp.porosity * p.oden;
+            if (!keep_density) p.density = pp.porosity * p.oden;   // WCSPH keeps its own density
             const double phi = pp.porosity;
             const double Fch = 1.750 / (std::sqrt(150 * (phi * phi * phi)));
             const double vmag = std::sqrt(p.vx * p.vx + p.vy * p.vy);
@@ -1113,6 +1113,118 @@ void scalar_substep(or_scene* s) {
 
 // Initial state: what the reference's warm-up leaves for the production loop
 // (ids, neighbour lists, porosity, eddy viscosity, per-cell maxima, timestep).
+// --------------------------------------------------------------- WCSPH
+// wcsph.f90 (compiled into no reference executable).  co, t_gam, delt and
+// the still-water level come from the parameters (co is never set by the
+// reference, setup.f90:134).
+
+// hydrostatic Tait density at height y (the term2 expression, wcsph.f90:78-82)
+double hyd_density(const or_scene* s, double y) {
+    const double rho = s->P.rho, co = s->P.wc_c0, gam = s->P.wc_gamma;
+    return rho * std::pow(((((s->P.wc_ysurf - y) * rho) * std::fabs(s->P.g)) * gam) / (rho * (co * co)) + 1.0,
+                          1.0 / gam);
+}
+
+// calmasscons, wcsph.f90:65-129.  term2 is both the hydrostatic density
+// difference of the current pair and the y accumulator: the reference
+// overwrites it with the pair's hydrostatic difference at every neighbour,
+// so only the last neighbour's y contribution survives; kept as written.
+void calmasscons(or_scene* s) {
+    const double rho = s->P.rho, co = s->P.wc_c0, delt = s->P.wc_delta, h1 = s->h, lam = s->lam;
+    const double dt = s->dt;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            if (!(p.tid > 2)) continue;
+            const Props& pp = c.pplist[k];
+            const Verlet& L = c.list[k];
+            double term1 = 0.0, term2 = 0.0;
+            for (int m = 0; m < L.count; ++m) {
+                const Particle& x = s->cells[L.nh[m].cell].plist[L.nh[m].slot];
+                const double r = L.dist[m];
+                const double wx = Wabx(x, p, r, h1), wy = Waby(x, p, r, h1);
+                const double gx = pp.coff[0] * wx + pp.coff[1] * wy;
+                const double gy = pp.coff[2] * wx + pp.coff[3] * wy;
+                const double hd = hyd_density(s, x.y) - hyd_density(s, p.y);
+                // as written: term2 doubles as hd, delta term along (r_i - r_j)
+                // (anti-diffusive); corrected: own y sum, along (r_j - r_i)
+                const double sg = (s->P.wc_form == 0) ? 1.0 : -1.0;
+                if (s->P.wc_form == 0) term2 = hd;
+                term1 = term1 - ((x.mass * (x.vx - p.vx)) * gx) * (p.density / x.density) +
+                        ((((((delt * 2) * h1) * co) * (x.density - p.density - hd)) * (sg * (p.x - x.x))) * gx) *
+                            (x.mass / x.density) / (r * r + lam);
+                term2 = term2 - ((x.mass * (x.vy - p.vy)) * gy) * (p.density / x.density) +
+                        ((((((delt * 2) * h1) * co) * (x.density - p.density - hd)) * (sg * (p.y - x.y))) * gy) *
+                            (x.mass / x.density) / (r * r + lam);
+            }
+            p.tden = p.density + (term1 + term2) * dt;
+        }
+    });
+}
+
+// updateden, wcsph.f90:131-154
+void updateden(or_scene* s) {
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k)
+            if (c.plist[k].tid > 2) c.plist[k].density = c.plist[k].tden;
+    });
+}
+
+// dentopress, wcsph.f90:35-63 (Tait equation of state, no tension)
+void dentopress(or_scene* s) {
+    const double rho = s->P.rho, co = s->P.wc_c0, gam = s->P.wc_gamma;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            if (!(p.tid > 2)) continue;
+            p.pressure = (rho * (co * co)) * (std::pow(p.density / rho, gam) - 1) / gam;
+            if (p.pressure < 0.0) {
+                p.pressure = 0.0;
+                p.density = rho;
+            }
+        }
+    });
+}
+
+// presstoden, wcsph.f90:13-33
+void presstoden(or_scene* s) {
+    const double rho = s->P.rho, co = s->P.wc_c0, gam = s->P.wc_gamma;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            p.density = rho * std::pow((p.pressure * gam / (rho * (co * co))) + 1, 1 / gam);
+        }
+    });
+}
+
+// Wall and ghost pressure of the WCSPH step (this library's boundary rule;
+// the reference has none): Shepard average over fluid neighbours of
+// p_f + rho_f |g| (y_f - y_w), 0 without fluid neighbours.
+void wall_pressure(or_scene* s) {
+    const double ag = std::fabs(s->P.g), h1 = s->h;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            if (p.tid == 3) continue;
+            const Verlet& L = c.list[k];
+            double num = 0.0, den = 0.0;
+            for (int m = 0; m < L.count; ++m) {
+                const Particle& x = s->cells[L.nh[m].cell].plist[L.nh[m].slot];
+                if (x.tid != 3) continue;
+                const double w = Wab(L.dist[m], h1);
+                num += (x.pressure + x.density * ag * (x.y - p.y)) * w;
+                den += w;
+            }
+            p.pressure = den > 0.0 ? num / den : 0.0;
+        }
+    });
+}
+
 void prime(or_scene* s) {
     resetid(s);
     neighbour(s);
@@ -1158,6 +1270,34 @@ void step(or_scene* s) {
     effpor(s);
     opt2_shift(s);
     densityupdate(s);
+    timestep(s);
+    eddyvis(s);
+}
+
+// WCSPH step: the production step with continuity + Tait EOS + wall
+// pressure in place of the PPE, density kept from the continuity equation
+void wcsph_step(or_scene* s) {
+    s->t = s->t + s->dt;
+    if (s->P.scalar_on)
+        for (int j1 = 1; j1 <= s->solsteps; ++j1) scalar_substep(s);
+    projection(s);
+    cellshift(s, false);
+    resetid(s);
+    neighbour(s);
+    effpor(s, true);
+    eddyvis(s);
+    int_vel(s);
+    calmasscons(s);
+    updateden(s);
+    dentopress(s);
+    wall_pressure(s);
+    comp_vel(s);
+    comp_pos(s);
+    cellshift(s, true);
+    neighbour(s);
+    freesurf(s);
+    effpor(s, true);
+    opt2_shift(s);
     timestep(s);
     eddyvis(s);
 }
@@ -1343,6 +1483,12 @@ int or_stage(or_scene* s, int32_t stage) {
         case OR_TIMESTEP: timestep(s); break;
         case OR_SCALAR_SUBSTEP: scalar_substep(s); break;
         case OR_PRIME: prime(s); break;
+        case OR_CALMASSCONS: calmasscons(s); break;
+        case OR_UPDATEDEN: updateden(s); break;
+        case OR_DENTOPRESS: dentopress(s); break;
+        case OR_PRESSTODEN: presstoden(s); break;
+        case OR_WALL_PRESSURE: wall_pressure(s); break;
+        case OR_EFFPOR_KEEP: effpor(s, true); break;
         default: return BS_E_ARG;
     }
     return 0;
@@ -1360,6 +1506,11 @@ int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule, int32_t* 
 
 int or_step(or_scene* s, int32_t nsteps) {
     for (int k = 0; k < nsteps; ++k) step(s);
+    return 0;
+}
+
+int or_wcsph_step(or_scene* s, int32_t nsteps) {
+    for (int k = 0; k < nsteps; ++k) wcsph_step(s);
     return 0;
 }
 

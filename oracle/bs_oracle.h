@@ -27,7 +27,11 @@ enum {
     OR_PROJECTION = 1, OR_CELLSHIFT, OR_CELLSHIFTALT, OR_RESETID, OR_NEIGHBOUR,
     OR_EFFPOR, OR_EDDYVIS, OR_INT_VEL, OR_PPE_ASSEMBLE, OR_PPE_SOLVE, OR_COMP_VEL,
     OR_COMP_POS, OR_FREESURF, OR_OPT2_SHIFT, OR_DENSITYUPDATE, OR_TIMESTEP,
-    OR_SCALAR_SUBSTEP, OR_PRIME
+    OR_SCALAR_SUBSTEP, OR_PRIME,
+    /* wcsph.f90 */
+    OR_CALMASSCONS, OR_UPDATEDEN, OR_DENTOPRESS, OR_PRESSTODEN,
+    OR_WALL_PRESSURE,   /* the WCSPH step's wall rule (no reference counterpart) */
+    OR_EFFPOR_KEEP      /* effpor without its density write (WCSPH step)        */
 };
 
 or_scene* or_create(const bs_params* p, const bs_state* st, const bs_grains* gr);
@@ -44,6 +48,7 @@ int or_stage(or_scene* s, int32_t stage);
 int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule,
                  int32_t* iters, double* relres);
 int or_step(or_scene* s, int32_t nsteps);
+int or_wcsph_step(or_scene* s, int32_t nsteps);
 /* overwrite pressures (used to pin a common PPE guess in tests) */
 int or_set_pressure(or_scene* s, const double* p);
 int or_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,

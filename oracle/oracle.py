@@ -22,7 +22,8 @@ DEPS = SRC + [os.path.join(HERE, "bs_oracle.h"),
 STAGES = dict(projection=1, cellshift=2, cellshiftalt=3, resetid=4, neighbour=5, effpor=6,
               eddyvis=7, int_vel=8, ppe_assemble=9, ppe_solve=10, comp_vel=11, comp_pos=12,
               freesurf=13, opt2_shift=14, densityupdate=15, timestep=16, scalar_substep=17,
-              prime=18)
+              prime=18, calmasscons=19, updateden=20, dentopress=21, presstoden=22,
+              wall_pressure=23, effpor_keep=24)
 
 
 def build(force=False):
@@ -58,6 +59,7 @@ def lib():
         L.or_stage.argtypes = [vp, C.c_int32]
         L.or_ppe_solve.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, vp, vp]
         L.or_step.argtypes = [vp, C.c_int32]
+        L.or_wcsph_step.argtypes = [vp, C.c_int32]
         L.or_set_pressure.argtypes = [vp, vp]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_bicgstab_csr.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_int32,
@@ -151,6 +153,9 @@ class Oracle:
 
     def step(self, n=1):
         lib().or_step(self.h, n)
+
+    def wcsph_step(self, n=1):
+        lib().or_wcsph_step(self.h, n)
 
     def set_pressure(self, p):
         p = np.ascontiguousarray(p, dtype=np.float64)
