@@ -142,6 +142,14 @@ def state_in(arrs):
     return st
 
 
+def empty_state():
+    """A scene with no particles (a free slot of a request loop)."""
+    st = {f: np.zeros(0) for f in STATE_FIELDS_F64}
+    st.update({f: np.zeros(0, np.int32) for f in STATE_FIELDS_I32})
+    st["flags"] = np.zeros(0, np.uint8)
+    return st
+
+
 def state_out(n, full=True):
     """Allocate numpy arrays for a download and a bs_state pointing at them."""
     out = {}

@@ -33,6 +33,8 @@ def _load():
         "bs_create": (C.c_int, [i32, vp, vp, vp, C.POINTER(vp)]),
         "bs_destroy": (C.c_int, [vp]),
         "bs_upload": (C.c_int, [vp, i32, vp, vp]),
+        "bs_set_scene": (C.c_int, [vp, i32, vp, vp, vp]),
+        "bs_prime_scene": (C.c_int, [vp, i32]),
         "bs_download": (C.c_int, [vp, i32, vp]),
         "bs_scene_info_get": (C.c_int, [vp, i32, vp]),
         "bs_clear_errors": (C.c_int, [vp]),
@@ -92,7 +94,7 @@ STAGE_FUNCS = ["prime", "scalar_substep", "projection", "search", "porosity", "e
 class Context:
     """A batch of scenes resident on the GPU."""
 
-    def __init__(self, params, states, grains=None, capacity=None, tuning=None):
+    def __init__(self, params, states, grains=None, capacity=None, tuning=None, grain_capacity=None):
         if not isinstance(params, (list, tuple)):
             params, states, grains = [params], [states], [grains]
         n = len(params)
@@ -101,7 +103,7 @@ class Context:
         self.nscenes = n
         self.params = (abi.Params * n)(*params)
         caps = capacity or [len(s["x"]) for s in states]
-        gcaps = [len(g["x"]) if g is not None else 0 for g in grains]
+        gcaps = grain_capacity or [len(g["x"]) if g is not None else 0 for g in grains]
         self._caps = (C.c_int32 * n)(*caps)
         self._gcaps = (C.c_int32 * n)(*gcaps)
         h = C.c_void_p()
@@ -137,6 +139,19 @@ class Context:
         st = abi.state_in(state)
         gr = abi.grains_in(grains) if grains is not None and len(grains["x"]) else None
         self._check(lib.bs_upload(self.h, s, C.byref(st), C.byref(gr) if gr is not None else None), "upload")
+
+    def set_scene(self, s, params, state, grains=None):
+        """Put another scene into slot s (its cell grid no larger than the
+        slot's creation grid); the other slots keep running untouched."""
+        st = abi.state_in(state)
+        gr = abi.grains_in(grains) if grains is not None and len(grains["x"]) else None
+        self.params[s] = abi.Params.from_buffer_copy(params)
+        self._check(lib.bs_set_scene(self.h, s, C.byref(self.params[s]), C.byref(st),
+                                     C.byref(gr) if gr is not None else None), "set_scene")
+
+    def prime_scene(self, s):
+        """Prime slot s alone (the other slots are left exactly as they are)."""
+        self._check(lib.bs_prime_scene(self.h, s), "prime_scene")
 
     def info(self, s=0):
         si = abi.SceneInfo()

@@ -214,7 +214,7 @@ __global__ void k_projection(Dev D) {
 // One thread per cell; per-scene finisher = last block of the scene.
 __global__ void k_cellmax(Dev D, int do_cellmax) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= D.ncell_total || !do_cellmax) return;
+    if (c >= D.ncell_total || !do_cellmax || D.dyn[D.cell_scene[c]].hold) return;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
     if (r1 > r0) {
         double mv = 0.0, me = 0.0;
@@ -230,6 +230,7 @@ __global__ void k_cellmax(Dev D, int do_cellmax) {
 // one block per scene
 __global__ void k_timestep(Dev D) {
     const int s = blockIdx.x;
+    if (D.dyn[s].hold) return;
     const ScenePar& P = D.par[s];
     __shared__ double sh[2 * 32];
     double v[2] = {0.0, 0.0};

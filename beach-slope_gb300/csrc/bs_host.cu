@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -39,6 +40,9 @@ struct bs_ctx {
     bs::KTimer timer;
     bs::IterGraph graph;
     std::vector<MgLevel> mglev;          // multigrid level tables (kernel arguments), index = level
+    std::vector<std::vector<std::pair<int, int>>> mgdims;   // per scene: current grid of each level
+    std::vector<std::vector<int>> mgrange;   // per scene: cells reserved on each level (fixed at create)
+    std::vector<int> cellx_cap, celly_cap;   // per scene: largest cell grid the slot takes
     std::vector<unsigned char> mgneed;   // per level: which launches some scene needs (Launch::mgneed)
 };
 
@@ -78,6 +82,74 @@ bs::Launch launch_of(bs_ctx* c) {
     L.mglev = c->mglev.empty() ? nullptr : c->mglev.data();
     L.mgneed = c->mgneed.empty() ? nullptr : c->mgneed.data();
     return L;
+}
+
+// multigrid grids of a scene: level 1 = half-cells, then 2x2 coarsening
+// until at most 256 cells (each scene on its own, so its cycle is the same
+// alone and inside any batch)
+std::vector<std::pair<int, int>> mg_dims_of(int cellx, int celly) {
+    std::vector<std::pair<int, int>> d;
+    int nx = 2 * cellx, ny = 2 * celly;
+    d.push_back({nx, ny});
+    while (nx * ny > 256 && (int)d.size() < BS_MG_MAXL) {
+        nx = (nx + 1) / 2;
+        ny = (ny + 1) / 2;
+        d.push_back({nx, ny});
+    }
+    return d;
+}
+
+// Level tables (kernel arguments), the launches each level needs, and the
+// device copies of the current grids, from the scenes' current grids and the
+// fixed per-level ranges.
+void mg_tables(bs_ctx* c) {
+    MgDev& M = c->D.mg;
+    const int L = M.nlev, ns = c->nscene;
+    c->mglev.assign(L + 2, MgLevel{});
+    c->mgneed.assign(L + 2, 0);
+    for (int l = 1; l <= L; ++l) {
+        MgLevel& G = c->mglev[l];
+        G.l = l;
+        G.n = M.n[l];
+        G.ns = ns;
+        int o = 0;
+        std::vector<int> nxv(ns, 0), nyv(ns, 0);
+        for (int s = 0; s < ns; ++s) {
+            G.off[s] = o;
+            const int Lc = (int)c->mgdims[s].size();
+            const bool has = Lc >= l;
+            G.nx[s] = nxv[s] = has ? c->mgdims[s][l - 1].first : 0;
+            G.ny[s] = nyv[s] = has ? c->mgdims[s][l - 1].second : 0;
+            G.lev[s] = Lc;
+            o += (int)c->mgrange[s].size() >= l ? c->mgrange[s][l - 1] : 0;
+            if (l <= Lc) c->mgneed[l] |= 1;
+            if (l < Lc) c->mgneed[l] |= 2;
+            if (l == Lc) c->mgneed[l] |= 4;
+        }
+        G.off[ns] = o;
+        cudaMemcpy((void*)M.nx[l], nxv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)M.ny[l], nyv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
+    }
+    for (int s = 0; s < ns; ++s) c->hpar[s].mg_lev = (int)c->mgdims[s].size();
+}
+
+// per-scene constants that do not depend on the layout
+void fill_par(ScenePar& P, const bs_params& p, int kmax) {
+    P.h = p.h; P.twoh = 2.0 * p.h; P.lam = 0.0010 * (p.h * p.h); P.dl = p.dl; P.cw = 4.0 * p.h;
+    P.inv_h = 1.0 / p.h; P.inv_h2 = 1.0 / (p.h * p.h); P.inv_h3 = 1.0 / (p.h * p.h * p.h);
+    P.cn1 = 0.1 * (10.0 / (BS_C28 * (p.h * p.h)));
+    P.cn2 = (1.0 - 0.1) * (1.0 / (BS_C3 * (p.h * p.h)));
+    P.wo = 0.1 * 4.0 * (10.0 / (BS_C28 * (p.h * p.h))) + (1.0 - 0.1) * 6.0 * (1.0 / (BS_C3 * (p.h * p.h)));
+    P.rho = p.rho; P.rhomin = p.rhomin; P.rhomax = p.rhomax; P.rel_den = p.rel_den; P.g = p.g;
+    P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
+    P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;
+    P.xlcutoff = p.xlcutoff; P.ytcutoff = p.ytcutoff; P.ppe_tol = p.ppe_tol; P.inner_tol = p.mixed_inner_tol;
+    P.wc_c0 = p.wc_c0; P.wc_gamma = p.wc_gamma; P.wc_delta = p.wc_delta; P.wc_ysurf = p.wc_ysurf;
+    P.wc_form = p.wc_form;
+    P.cellx = p.cellx; P.celly = p.celly; P.ncell = p.cellx * p.celly;
+    P.kmax = kmax; P.maxit = p.ppe_maxit;
+    P.adaptive_dt = p.adaptive_dt; P.scalar_on = p.scalar_on; P.precision = p.precision; P.stop_rule = p.ppe_stop;
+    P.max_outer = p.mixed_max_outer;
 }
 
 // cell bounds as setup.f90:120-123
@@ -213,21 +285,12 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         ScenePar& P = ctx->hpar[s];
         std::memset(&P, 0, sizeof(P));
         const int cap = ((std::max(capacity[s], 1) + BS_ALIGN - 1) / BS_ALIGN) * BS_ALIGN;
-        P.h = p.h; P.twoh = 2.0 * p.h; P.lam = 0.0010 * (p.h * p.h); P.dl = p.dl; P.cw = 4.0 * p.h;
-        P.inv_h = 1.0 / p.h; P.inv_h2 = 1.0 / (p.h * p.h); P.inv_h3 = 1.0 / (p.h * p.h * p.h);
-        P.cn1 = 0.1 * (10.0 / (BS_C28 * (p.h * p.h)));
-        P.cn2 = (1.0 - 0.1) * (1.0 / (BS_C3 * (p.h * p.h)));
-        P.wo = 0.1 * 4.0 * (10.0 / (BS_C28 * (p.h * p.h))) + (1.0 - 0.1) * 6.0 * (1.0 / (BS_C3 * (p.h * p.h)));
-        P.rho = p.rho; P.rhomin = p.rhomin; P.rhomax = p.rhomax; P.rel_den = p.rel_den; P.g = p.g;
-        P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
-        P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;
-        P.xlcutoff = p.xlcutoff; P.ytcutoff = p.ytcutoff; P.ppe_tol = p.ppe_tol; P.inner_tol = p.mixed_inner_tol;
-        P.wc_c0 = p.wc_c0; P.wc_gamma = p.wc_gamma; P.wc_delta = p.wc_delta; P.wc_ysurf = p.wc_ysurf;
-        P.wc_form = p.wc_form;
-        P.cellx = p.cellx; P.celly = p.celly; P.ncell = p.cellx * p.celly; P.cell0 = cell;
-        P.row0 = row; P.cap = cap; P.kmax = ctx->kmax; P.maxit = p.ppe_maxit;
-        P.adaptive_dt = p.adaptive_dt; P.scalar_on = p.scalar_on; P.precision = p.precision; P.stop_rule = p.ppe_stop;
-        P.nblk = cap / BS_THREADS; P.blk0 = blk; P.max_outer = p.mixed_max_outer;
+        fill_par(P, p, ctx->kmax);
+        P.cell0 = cell;
+        P.row0 = row; P.cap = cap;
+        P.nblk = cap / BS_THREADS; P.blk0 = blk;
+        ctx->cellx_cap.push_back(p.cellx);
+        ctx->celly_cap.push_back(p.celly);
         for (int b = 0; b < P.nblk; ++b) blk_scene.push_back(s);
         for (int q = 0; q < P.ncell; ++q) cell_scene.push_back(s);
         row += cap;
@@ -295,24 +358,20 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.pre0 = 1;
         M.prec = 1;
         M.wlev = 2;
-        // each scene coarsens on its own until it has at most 256 cells, so
-        // its V-cycle is the same alone and inside any batch
+        // each scene reserves the levels of its creation grid (the largest
+        // grid the slot takes, bs_set_scene)
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
+        ctx->mgrange.assign(nscenes, {});
         int L = 1;
         for (int s = 0; s < nscenes; ++s) {
-            int nx = 2 * params[s].cellx, ny = 2 * params[s].celly;
-            dims[s].push_back({nx, ny});
-            while (nx * ny > 256 && (int)dims[s].size() < BS_MG_MAXL) {
-                nx = (nx + 1) / 2;
-                ny = (ny + 1) / 2;
-                dims[s].push_back({nx, ny});
-            }
-            ctx->hpar[s].mg_lev = (int)dims[s].size();
+            dims[s] = mg_dims_of(params[s].cellx, params[s].celly);
+            for (auto& d : dims[s]) ctx->mgrange[s].push_back(d.first * d.second);
             L = std::max(L, (int)dims[s].size());
         }
+        ctx->mgdims = dims;
         const size_t tw = (ctx->precision == BS_PREC_MIXED) ? sizeof(float) : sizeof(double);
         M.nlev = L;
-        M.coarse_max = 1;
+        M.coarse_max = 256;   // a coarsest level holds at most 256 cells (unless BS_MG_MAXL ends it)
         for (int s = 0; s < nscenes; ++s)
             M.coarse_max = std::max(M.coarse_max, dims[s].back().first * dims[s].back().second);
         for (int l = 1; l <= L && !rc; ++l) {
@@ -348,30 +407,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         char *d0, *ad, *xi, *uu, *zz;
         if (!rc) rc = dalloc(ctx, &M.sub, R);
         if (!rc) rc = dalloc(ctx, &M.agg1, R);
-        // level tables for the level kernels' arguments, and the levels
-        // that need launches at all
-        ctx->mglev.assign(L + 2, MgLevel{});
-        ctx->mgneed.assign(L + 2, 0);
-        for (int l = 1; l <= L; ++l) {
-            MgLevel& G = ctx->mglev[l];
-            G.l = l;
-            G.n = M.n[l];
-            G.ns = nscenes;
-            int o = 0;
-            for (int s = 0; s < nscenes; ++s) {
-                G.off[s] = o;
-                const int Lc = (int)dims[s].size();
-                const bool has = Lc >= l;
-                G.nx[s] = has ? dims[s][l - 1].first : 0;
-                G.ny[s] = has ? dims[s][l - 1].second : 0;
-                G.lev[s] = Lc;
-                o += G.nx[s] * G.ny[s];
-                if (l <= Lc) ctx->mgneed[l] |= 1;
-                if (l < Lc) ctx->mgneed[l] |= 2;
-                if (l == Lc) ctx->mgneed[l] |= 4;
-            }
-            G.off[nscenes] = o;
-        }
+        if (!rc) mg_tables(ctx);
         if (!rc) rc = dalloc(ctx, &d0, R * tw);
         if (!rc) rc = dalloc(ctx, &ad, R * tw);
         if (!rc) rc = dalloc(ctx, &xi, R * tw);
@@ -760,6 +796,35 @@ int bs_set_rhs(bs_ctx* ctx, int32_t s, const double* b) {
     return 0;
 }
 
+// Re-use scene slot s for another scene: new parameters (its cell grid no
+// larger than the one the slot was created with), particles and grains.
+int bs_set_scene(bs_ctx* ctx, int32_t s, const bs_params* p, const bs_state* st, const bs_grains* gr) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !p || !st) return BS_E_ARG;
+    if (p->precision != ctx->precision || p->kmax > ctx->kmax || p->h <= 0 || p->cellx < 4 || p->celly < 4)
+        return fail(ctx, BS_E_ARG, "scene parameters do not fit this context");
+    if (p->cellx > ctx->cellx_cap[s] || p->celly > ctx->celly_cap[s])
+        return fail(ctx, BS_E_CAPACITY, "cell grid larger than the slot's");
+    if (st->n > ctx->hpar[s].cap) return fail(ctx, BS_E_CAPACITY, "scene larger than its capacity");
+    if (gr && gr->n > ctx->gcap[s]) return fail(ctx, BS_E_CAPACITY, "more grains than the grain capacity");
+    CK(cudaStreamSynchronize(ctx->stream));
+    Dev& D = ctx->D;
+    ScenePar& P = ctx->hpar[s];
+    // empty every reserved cell of the slot (cells beyond the new grid stay empty)
+    const size_t nc = (size_t)ctx->cellx_cap[s] * ctx->celly_cap[s];
+    int* zc[] = {D.cell_start, D.cell_end, D.cell_start2, D.cell_end2, D.gcell_start, D.gcell_end, D.cell_total};
+    for (int* a : zc) CK(cudaMemset(a + P.cell0, 0, sizeof(int) * nc));
+    CK(cudaMemset(D.cell_maxvel + P.cell0, 0, sizeof(double) * nc));
+    CK(cudaMemset(D.cell_maxeddy + P.cell0, 0, sizeof(double) * nc));
+    ctx->prm[s] = *p;
+    fill_par(P, *p, ctx->kmax);
+    ctx->mgdims[s] = mg_dims_of(p->cellx, p->celly);
+    mg_tables(ctx);
+    CK(cudaMemcpy((void*)(D.par + s), &P, sizeof(ScenePar), cudaMemcpyHostToDevice));
+    ctx->graph.valid = false;   // the level tables are baked into the captured chunk
+    ctx->assembled = false;
+    return bs_upload(ctx, s, st, gr);
+}
+
 // ------------------------------------------------------------------ stages
 int bs_prime(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
@@ -773,6 +838,24 @@ int bs_prime(bs_ctx* ctx) {
     int rc = check_launch(ctx);
     if (rc) return rc;
     return read_solsteps(ctx);
+}
+
+// Prime one scene only: the others are held (their rows, cells and
+// timestep untouched), so scenes already stepping carry on exactly as if no
+// other scene had joined.
+int bs_prime_scene(bs_ctx* ctx, int32_t s) {
+    if (!ctx || s < 0 || s >= ctx->nscene) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    const size_t off = offsetof(SceneDyn, hold);
+    for (int k = 0; k < ctx->nscene; ++k) {
+        const int h = (k != s);
+        CK(cudaMemcpy((char*)(ctx->D.dyn + k) + off, &h, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    const int rc = bs_prime(ctx);
+    const int zero = 0;
+    for (int k = 0; k < ctx->nscene; ++k)
+        CK(cudaMemcpy((char*)(ctx->D.dyn + k) + off, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    return rc;
 }
 
 int bs_scalar_substep(bs_ctx* ctx) {

@@ -59,7 +59,7 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     double bnorm2, rnorm2, relres, rtrue2;
     int iters, converged, breakdown, outer;
     unsigned err;
-    int pad1;
+    int hold;                      // 1: row sweeps and timestep leave the scene alone (bs_prime_scene)
     double part_tmp;
 };
 

@@ -66,6 +66,7 @@ __global__ void k_mg_gal0(Dev D) {
     if (c >= D.ncell_total) return;
     const int s = D.cell_scene[c];
     const ScenePar& P = D.par[s];
+    if (c - P.cell0 >= P.ncell) return;   // reserved cells beyond the scene's current grid
     const int celly = P.celly;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
     const double* A = (const double*)D.aval;
@@ -135,6 +136,7 @@ __global__ void k_mg_galc(Dev D, int l) {
     const int s = M.scene_of[l + 1][Q];
     const int q = Q - M.off[l + 1][s];
     const int nyc = M.ny[l + 1][s];
+    if (q >= nyc * M.nx[l + 1][s]) return;   // reserved beyond the scene's current grid
     const int I = q % nyc, J = q / nyc;
     const int nyf = M.ny[l][s], nxf = M.nx[l][s], fo = M.off[l][s];
     const T* Af = (const T*)M.A[l];
@@ -178,7 +180,7 @@ __global__ void k_mg_l0_down(Dev D) {
     const int lane = threadIdx.x & 31;
     if (c >= D.ncell_total) return;
     const int s = D.cell_scene[c];
-    if (mg_skip(D, s)) return;
+    if (mg_skip(D, s) || c - D.par[s].cell0 >= D.par[s].ncell) return;
     const T* __restrict__ xin = (const T*)D.mg.xin;
     const T* __restrict__ u = (const T*)D.mg.u;
     const T* __restrict__ ad = (const T*)D.mg.adiagT;
@@ -259,6 +261,7 @@ __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_const
     const int k = scene_at(C, Q);
     const int q = Q - C.off[k];
     const int nyc = C.ny[k];
+    if (q >= nyc * C.nx[k]) return;   // reserved beyond the scene's current grid
     const int I = q % nyc, J = q / nyc;
     const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
     const T* __restrict__ A = (const T*)M.A[F.l];
@@ -300,6 +303,7 @@ __global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
     const int k = scene_at(F, c);
     const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
     const int q = c - fo;
+    if (q >= fnx * fny) return;
     const int i = q % fny, j = q / fny;
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* z = (const T*)M.z[F.l];
@@ -326,6 +330,7 @@ __global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constan
     if (F.l >= F.lev[k]) return;   // the coarse solve wrote this level
     const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
     const int q = c - fo;
+    if (q >= fnx * fny) return;
     const int i = q % fny, j = q / fny;
     const int nyc = C.ny[k], oc = C.off[k];
     const T* __restrict__ A = (const T*)M.A[F.l];

@@ -11,14 +11,17 @@ namespace {
 
 struct RowCtx {
     int r, s;
-    bool active;
+    bool active;   // a particle row of a scene that is not held
+    bool held;     // a particle row of a held scene
 };
 
 __device__ __forceinline__ RowCtx row_ctx(const Dev& D) {
     RowCtx c;
     c.r = blockIdx.x * blockDim.x + threadIdx.x;
     c.s = D.blk_scene[blockIdx.x];
-    c.active = c.r < D.par[c.s].row0 + D.dyn[c.s].n;
+    const bool row = c.r < D.par[c.s].row0 + D.dyn[c.s].n;
+    c.held = row && D.dyn[c.s].hold;
+    c.active = row && !c.held;
     return c;
 }
 
@@ -85,7 +88,13 @@ __device__ __forceinline__ void st(void* p, long e, T v) { ((T*)p)[e] = v; }
 template <typename T>
 __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int do_effpor) {
     const RowCtx R = row_ctx(D);
-    if (!R.active) return;
+    if (!R.active) {
+        if (R.held && do_effpor) {   // keep a held scene's density across the buffer swap
+            D.rho_new[R.r] = D.rho[R.r];
+            D.vol_new[R.r] = D.vol[R.r];
+        }
+        return;
+    }
     const ScenePar& P = D.par[R.s];
     const int r = R.r;
     const int tid = D.tid[r];

@@ -216,15 +216,28 @@ def lattice_scene(n=1000, dx=1e-3, jitter=0.25, seed=20261203, layers=3, hfac=1.
     return p, st, grains
 
 
-def batch_scenes(count=64, seed=20261203, precision=abi.PREC_MIXED, dx_range=(0.005, 0.02)):
+def batch_scenes(count=64, seed=20261203, precision=abi.PREC_MIXED, dx_range=(0.005, 0.02), wcsph=False,
+                 dx=None):
     """Seeded beach scenes: slope 1:5..1:20, amplitude 0.02..0.10 m,
-    porosity 0.3..0.5, dx in dx_range (uneven sizes)."""
+    porosity 0.3..0.5, dx log-uniform in dx_range (uneven sizes) or the
+    given list of dx."""
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(count):
+    for k in range(count):
         slope = 1.0 / rng.uniform(5.0, 20.0)
         A = rng.uniform(0.02, 0.10)
         por = rng.uniform(0.3, 0.5)
-        dx = float(np.exp(rng.uniform(np.log(dx_range[0]), np.log(dx_range[1]))))
-        out.append(beach_scene(dx=dx, slope=slope, A=A, por=por, precision=precision))
+        d = float(np.exp(rng.uniform(np.log(dx_range[0]), np.log(dx_range[1]))))
+        if dx is not None:
+            d = float(dx[k])
+        out.append(beach_scene(dx=d, slope=slope, A=A, por=por, precision=precision, wcsph=wcsph))
     return out
+
+
+# particles of a beach scene per unit 1/dx^2 (fluid + walls, A = 0.06, 1:10)
+BEACH_N_DX2 = 712460 * 0.00125 ** 2
+
+
+def dx_for_particles(n):
+    """Lattice spacing that gives a beach scene of about n particles."""
+    return float(np.sqrt(BEACH_N_DX2 / n))

@@ -203,6 +203,18 @@ int bs_get_neighbours(struct bs_ctx* ctx, int32_t scene, int32_t* counts, int32_
  * aligned with the neighbour list, rhs[n]. */
 int bs_get_matrix(struct bs_ctx* ctx, int32_t scene, double* diag, double* off, double* rhs);
 
+/* Re-use scene slot `scene` for another scene (new parameters, particles and
+ * grains; a request loop refills slots this way).  The slot keeps the
+ * capacities it was created with: rows, grains, and the cell grid given by
+ * the parameters passed to bs_create -- the new cellx/celly may not exceed
+ * those (BS_E_CAPACITY).  The other scenes are untouched.  No counterpart in
+ * the reference (one scene per run). */
+int bs_set_scene(struct bs_ctx* ctx, int32_t scene, const bs_params* params, const bs_state* st,
+                 const bs_grains* gr);
+/* bs_prime for one scene only; the other scenes are left exactly as they
+ * are, so a scene joining a running batch does not perturb the others. */
+int bs_prime_scene(struct bs_ctx* ctx, int32_t scene);
+
 /* Solver tunables, set by the project autotuner (beach-slope_gb300/autotune.py):
  * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
  * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),
