@@ -172,15 +172,26 @@ def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.0
     st = _cat(parts)
     p.wc_c0 = 10.0 * math.sqrt(-g * d)
     p.wc_ysurf = Y0 + d
-    if wcsph:
-        p.wc_form = 1   # the corrected continuity (the form as written is unstable)
-        fl = st["tid"] == abi.TID_FLUID
-        st["ovol"] = np.where(fl, dx * dx, st["ovol"])
-        st["mass"] = np.where(fl, st["oden"] * dx * dx, st["mass"])
-        c2 = p.wc_c0 ** 2
-        st["rho"] = np.where(fl, rho * (st["p"] * p.wc_gamma / (rho * c2) + 1.0) ** (1.0 / p.wc_gamma), st["rho"])
     _grid_for(p, X0 + L + (layers + 1) * dx, Y0 + H + 0.3)
+    if wcsph:
+        p, st = to_wcsph(p, st)
     return p, st, grains
+
+
+def to_wcsph(p, st):
+    """WCSPH set-up of a beach scene: every fluid particle carries the full
+    lattice mass rho0 dl^2 and the Tait density of its pressure; the
+    corrected continuity (the form as written is unstable)."""
+    p = abi.Params.from_buffer_copy(p)
+    st = dict(st)
+    p.wc_form = 1
+    dx, rho = p.dl, p.rho
+    fl = st["tid"] == abi.TID_FLUID
+    st["ovol"] = np.where(fl, dx * dx, st["ovol"])
+    st["mass"] = np.where(fl, st["oden"] * dx * dx, st["mass"])
+    c2 = p.wc_c0 ** 2
+    st["rho"] = np.where(fl, rho * (st["p"] * p.wc_gamma / (rho * c2) + 1.0) ** (1.0 / p.wc_gamma), st["rho"])
+    return p, st
 
 
 def lattice_scene(n=1000, dx=1e-3, jitter=0.25, seed=20261203, layers=3, hfac=1.3):

@@ -352,6 +352,91 @@ def cpu_baseline(args):
             "sample": f"1 production step of the full {args.workload} scene ({o.n} particles), {t:.1f} s"}
 
 
+def run_batched(args):
+    """64 seeded beach scenes of uneven size in one context (one launch per
+    stage for all of them): ISPH and WCSPH steps, mixed precision."""
+    from beachslope_gb300 import abi, api, scene
+    scenes = scene.batch_scenes(args.batch_scenes, precision=abi.PREC_MIXED)
+    P = [s[0] for s in scenes]
+    S = [s[1] for s in scenes]
+    G = [s[2] for s in scenes]
+    n = sum(len(s["x"]) for s in S)
+    out = {"scenes": len(P), "particles": n, "particles_min": min(len(s["x"]) for s in S),
+           "particles_max": max(len(s["x"]) for s in S), "steps": args.batch_steps,
+           "description": "slope 1:5-1:20, A 0.02-0.10 m, porosity 0.3-0.5, dx 5-20 mm log-uniform (seeded)"}
+    for mode in ("isph", "wcsph"):
+        if mode == "wcsph":
+            conv = [scene.to_wcsph(p, s) for p, s in zip(P, S)]
+            Pm, Sm = [c[0] for c in conv], [c[1] for c in conv]
+        else:
+            Pm, Sm = P, S
+        ctx = api.Context(Pm, Sm, G)
+        ctx.prime()
+        if mode == "wcsph":
+            ctx.stage("wcsph_pressure_to_density")
+        stepf = ctx.step if mode == "isph" else ctx.wcsph_step
+        stepf(2)
+        ctx.sync()
+        ctx.record(0)
+        stepf(args.batch_steps)
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        err = [ctx.info(k)["err_bits"] for k in range(len(Pm))]
+        out[mode] = {"value": n * args.batch_steps / (ms / 1e3), "unit": UNIT,
+                     "ms_per_step": ms / args.batch_steps, "scenes_with_errors": int(sum(e != 0 for e in err))}
+        ctx.close()
+    return out
+
+
+def run_serving(args):
+    """Request loop: Poisson arrivals, log-uniform sizes, slot admission into
+    one batched context (mixed precision); the same requests solved one at a
+    time with the FP64 drop-in as the serial baseline."""
+    from beachslope_gb300 import abi, api, scene, serve
+    reqs = serve.poisson_requests(args.serve_requests, args.serve_rate, precision=abi.PREC_MIXED)
+    steps = args.serve_steps
+    classes = [(500_000, 3), (64_000, 5)]   # (largest request, slots)
+    templates = []
+    for cap, k in classes:
+        tp, tst, tgr = scene.beach_scene(dx=scene.dx_for_particles(cap), precision=abi.PREC_MIXED)
+        templates += [(tp, int(1.3 * len(tst["x"])), int(1.3 * len(tgr["x"])) + 64)] * k
+    srv = serve.Server(templates)
+    t0 = time.perf_counter()
+    res = srv.run(reqs, steps)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([res[r.rid]["latency"] for r in reqs])
+    psteps = sum(len(r.state["x"]) for r in reqs) * steps
+    out = {"requests": len(reqs), "rate_per_s": args.serve_rate, "steps_per_request": steps,
+           "particles_min": min(len(r.state["x"]) for r in reqs),
+           "particles_max": max(len(r.state["x"]) for r in reqs),
+           "slots": {str(c): k for c, k in classes},
+           "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                         "mean": float(lat.mean())},
+           "value": psteps / wall, "unit": UNIT, "wall_s": wall,
+           "errors": int(sum(res[r.rid]["info"]["err_bits"] != 0 for r in reqs)),
+           "note": "each request %d production steps (the configuration's 0.5 s of physical time is %d steps)"
+                   % (steps, 5000)}
+    # serial FP64 baseline: the same requests one after another
+    t0 = time.perf_counter()
+    lat_s = []
+    for r in reqs:
+        p = abi.Params.from_buffer_copy(r.params)
+        p.precision = abi.PREC_FP64
+        c = api.Context([p], [r.state], [r.grains], tuning="auto")
+        c.prime()
+        c.step(steps)
+        c.sync()
+        c.close()
+        lat_s.append(time.perf_counter() - t0 - r.arrival)
+    wall_s = time.perf_counter() - t0
+    lat_s = np.array(lat_s)
+    out["serial_fp64"] = {"value": psteps / wall_s, "unit": UNIT, "wall_s": wall_s,
+                          "latency_s": {"p50": float(np.percentile(lat_s, 50)),
+                                        "p99": float(np.percentile(lat_s, 99))}}
+    return out
+
+
 def dtype_of(precision):
     return "f64" if precision == "fp64" else "f32+f64"
 
@@ -367,6 +452,13 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched workload")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop workload")
+    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-steps", type=int, default=40)
     args = ap.parse_args()
     D = Dist()
     config = {"workload": args.workload, "description": WORKLOADS[args.workload], "dt": 1e-4,
@@ -401,6 +493,10 @@ def main():
         line["config"]["solver_tuning"] = out["tuning"]
         if D.world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(args)
+        if not args.no_batch:
+            line["batched"] = run_batched(args)
+        if not args.no_serve:
+            line["serving"] = run_serving(args)
         print(json.dumps(line), flush=True)
     D.close()
 
