@@ -35,6 +35,7 @@ def _load():
         "bs_upload": (C.c_int, [vp, i32, vp, vp]),
         "bs_set_scene": (C.c_int, [vp, i32, vp, vp, vp]),
         "bs_prime_scene": (C.c_int, [vp, i32]),
+        "bs_write_combined": (C.c_int, [vp, i32, C.c_char_p, C.c_char_p]),
         "bs_download": (C.c_int, [vp, i32, vp]),
         "bs_scene_info_get": (C.c_int, [vp, i32, vp]),
         "bs_clear_errors": (C.c_int, [vp]),
@@ -148,6 +149,11 @@ class Context:
         self.params[s] = abi.Params.from_buffer_copy(params)
         self._check(lib.bs_set_scene(self.h, s, C.byref(self.params[s]), C.byref(st),
                                      C.byref(gr) if gr is not None else None), "set_scene")
+
+    def write_combined(self, fluid_path, buffer_path=None, s=0):
+        """The reference's combined text output (output.f90:188-222) for scene s."""
+        self._check(lib.bs_write_combined(self.h, s, fluid_path.encode(),
+                                          buffer_path.encode() if buffer_path else None), "write_combined")
 
     def prime_scene(self, s):
         """Prime slot s alone (the other slots are left exactly as they are)."""

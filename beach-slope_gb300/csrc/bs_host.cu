@@ -825,6 +825,64 @@ int bs_set_scene(bs_ctx* ctx, int32_t s, const bs_params* p, const bs_state* st,
     return bs_upload(ctx, s, st, gr);
 }
 
+// ------------------------------------------------------------------ output
+namespace {
+// Fortran Fw.d / ESw.d edit descriptors as gfortran prints them: right
+// justified in w columns, asterisks when the value does not fit
+void fortran_f(std::string& out, double v, int w, int d) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%*.*f", w, d, v);
+    out += (int)std::strlen(b) > w ? std::string(w, '*') : std::string(b);
+}
+void fortran_es(std::string& out, double v, int w, int d) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%*.*E", w, d, v);
+    out += (int)std::strlen(b) > w ? std::string(w, '*') : std::string(b);
+}
+}  // namespace
+
+int bs_write_combined(bs_ctx* ctx, int32_t s, const char* fluid_path, const char* buffer_path) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !fluid_path) return BS_E_ARG;
+    SceneDyn hd;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&hd, ctx->D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    const int n = hd.n, off = ctx->hpar[s].row0;
+    const Dev& D = ctx->D;
+    std::vector<double> x(n), y(n), p(n), vx(n), vy(n), con(n);
+    std::vector<int8_t> tid(n);
+    std::vector<uint8_t> fl(n);
+    double* dst[] = {x.data(), y.data(), p.data(), vx.data(), vy.data(), con.data()};
+    const double* src[] = {D.x, D.y, D.p, D.vx, D.vy, D.con};
+    for (int f = 0; f < 6; ++f)
+        if (n) CK(cudaMemcpy(dst[f], src[f] + off, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (n) CK(cudaMemcpy(tid.data(), D.tid + off, n, cudaMemcpyDeviceToHost));
+    if (n) CK(cudaMemcpy(fl.data(), D.flags + off, n, cudaMemcpyDeviceToHost));
+    FILE* ff = std::fopen(fluid_path, "w");
+    if (!ff) return fail(ctx, BS_E_ARG, std::string("cannot write ") + fluid_path);
+    FILE* fb = buffer_path ? std::fopen(buffer_path, "w") : nullptr;
+    std::string line;
+    // rows are in the reference's order: columns of cells, rows of cells,
+    // slots (output.f90:199-216)
+    for (int q = 0; q < n; ++q) {
+        if (tid[q] != BS_TID_FLUID) continue;
+        const bool buf = (fl[q] & BS_FLAG_BUFFER) != 0;
+        FILE* f = buf ? fb : ff;
+        if (!f) continue;
+        line.clear();
+        fortran_f(line, x[q], 10, 3); line += ' ';
+        fortran_f(line, y[q], 10, 3); line += ' ';
+        fortran_f(line, p[q], 10, 3); line += ' ';
+        fortran_es(line, vx[q], 10, 3); line += ' ';
+        fortran_es(line, vy[q], 10, 3); line += ' ';
+        fortran_f(line, con[q] + 0.50, 10, 5);
+        line += '\n';
+        std::fputs(line.c_str(), f);
+    }
+    std::fclose(ff);
+    if (fb) std::fclose(fb);
+    return 0;
+}
+
 // ------------------------------------------------------------------ stages
 int bs_prime(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;

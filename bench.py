@@ -138,6 +138,12 @@ def peaks():
 # Kernels bracketed by CUDA events during the timed region (the candidates for
 # the dominant kernel).
 TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down", "mg_l0_up")
+# DRAM bytes per launch measured by ncu over the algorithmic bytes of the same
+# launch (0.18 M-particle beach, mixed; profiles/*_beach_dx0.0025_mixed.md);
+# the traffic grows with the nonzeros and rows, so the ratio scales it to the
+# bench's workload.  k_it2_64 has k_it1_64's access pattern.
+TRAFFIC_RATIO = {"search_effpor": 0.46, "bicg_it1_spmv": 0.99, "bicg_it2_spmv": 0.99,
+                 "mg_l0_down": 0.98, "mg_l0_up": 0.93}
 
 
 def algorithmic_bytes(ctx, kernel, precision):
@@ -221,7 +227,9 @@ def run_ours(args, D):
         achieved = alg / avg_s / 1e9
         out["roofline"] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": pk,
                            "peak_source": src, "unit": "GB/s", "frac": round(achieved / pk, 4),
-                           "traffic": None, "algorithmic_bytes_per_launch": alg,
+                           "traffic": (round(TRAFFIC_RATIO[name] * alg) if args.precision == "mixed" else None),
+                           "traffic_source": "ncu dram__bytes_read+write on the 0.18 M-particle case, scaled",
+                           "algorithmic_bytes_per_launch": alg,
                            "avg_launch_us": round(avg_s * 1e6, 2), "launches": cnt,
                            "share_of_step": round(tms / ms_timed, 3),
                            "note": "durations from a second pass of the same steps with per-launch events",

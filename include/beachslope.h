@@ -215,6 +215,12 @@ int bs_set_scene(struct bs_ctx* ctx, int32_t scene, const bs_params* params, con
  * are, so a scene joining a running batch does not perturb the others. */
 int bs_prime_scene(struct bs_ctx* ctx, int32_t scene);
 
+/* combined, output.f90:188-222: the scene's fluid particles as text, one
+ * line each in the reference's order and format (F10.3 x, y, p; ES10.3 vx,
+ * vy; F10.5 con+0.5) -- non-buffer particles to fluid_path, buffer particles
+ * to buffer_path (may be NULL: not written). */
+int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path, const char* buffer_path);
+
 /* Solver tunables, set by the project autotuner (beach-slope_gb300/autotune.py):
  * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
  * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),

@@ -16,8 +16,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <limits>
+#include <string>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1506,6 +1508,41 @@ int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule, int32_t* 
 
 int or_step(or_scene* s, int32_t nsteps) {
     for (int k = 0; k < nsteps; ++k) step(s);
+    return 0;
+}
+
+// combined, output.f90:188-222 (gfortran's Fw.d / ESw.d: right justified,
+// asterisks when the value does not fit)
+static void ffmt(std::string& o, double v, int w, int d, bool es) {
+    char b[64];
+    std::snprintf(b, sizeof b, es ? "%*.*E" : "%*.*f", w, d, v);
+    o += (int)std::strlen(b) > w ? std::string(w, '*') : std::string(b);
+}
+int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_path) {
+    FILE* ff = std::fopen(fluid_path, "w");
+    if (!ff) return BS_E_ARG;
+    FILE* fb = buffer_path ? std::fopen(buffer_path, "w") : nullptr;
+    for (int j = 2; j <= s->cellx - 1; ++j)
+        for (int i = 2; i <= s->celly - 1; ++i) {
+            const Cell& c = s->C(i, j);
+            for (int k = 0; k < c.ptot; ++k) {
+                const Particle& p = c.plist[k];
+                if (p.tid != 3) continue;
+                FILE* f = p.buffer ? fb : ff;
+                if (!f) continue;
+                std::string o;
+                ffmt(o, p.x, 10, 3, false); o += ' ';
+                ffmt(o, p.y, 10, 3, false); o += ' ';
+                ffmt(o, p.pressure, 10, 3, false); o += ' ';
+                ffmt(o, p.vx, 10, 3, true); o += ' ';
+                ffmt(o, p.vy, 10, 3, true); o += ' ';
+                ffmt(o, p.con + 0.50, 10, 5, false);
+                o += '\n';
+                std::fputs(o.c_str(), f);
+            }
+        }
+    std::fclose(ff);
+    if (fb) std::fclose(fb);
     return 0;
 }
 

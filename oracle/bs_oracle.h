@@ -49,6 +49,8 @@ int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule,
                  int32_t* iters, double* relres);
 int or_step(or_scene* s, int32_t nsteps);
 int or_wcsph_step(or_scene* s, int32_t nsteps);
+/* combined, output.f90:188-222 (fluid / buffer text files) */
+int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_path);
 /* overwrite pressures (used to pin a common PPE guess in tests) */
 int or_set_pressure(or_scene* s, const double* p);
 int or_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,

@@ -60,6 +60,7 @@ def lib():
         L.or_ppe_solve.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, vp, vp]
         L.or_step.argtypes = [vp, C.c_int32]
         L.or_wcsph_step.argtypes = [vp, C.c_int32]
+        L.or_write_combined.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.or_set_pressure.argtypes = [vp, vp]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_bicgstab_csr.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_int32,
@@ -156,6 +157,10 @@ class Oracle:
 
     def wcsph_step(self, n=1):
         lib().or_wcsph_step(self.h, n)
+
+    def write_combined(self, fluid_path, buffer_path=None):
+        return lib().or_write_combined(self.h, fluid_path.encode(),
+                                       buffer_path.encode() if buffer_path else None)
 
     def set_pressure(self, p):
         p = np.ascontiguousarray(p, dtype=np.float64)
