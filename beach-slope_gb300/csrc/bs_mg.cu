@@ -231,12 +231,18 @@ __global__ void k_mg_l0_prolong(Dev D) {
     ((T*)D.mg.zz)[r] = pre + (T)D.mg.cscale * ((const T*)D.mg.z[1])[D.mg.agg1[r]];
 }
 
-// ---- level operations on the cell levels (l >= 1), one cell per thread.
-// The level's per-scene tables arrive as a kernel argument (MgLevel, in the
-// constant bank), so a cell's scene, offsets and grid size cost no memory
-// round trip; on these small levels the kernels are bound by the latency of
-// their dependent loads, not by bandwidth.  Converged scenes are not
-// skipped here (their cells are few and the result is unused).
+// ---- level operations on the cell levels (l >= 1), one cell per call.
+// A scene's view of a level: its grid, its first cell in the level's arrays
+// and the level's total size (the stride of the stencil arrays).  The
+// per-level kernels build views from the MgLevel tables (kernel arguments,
+// in the constant bank: no memory round trip for a cell's scene, offsets and
+// grid); the tail kernel from its scene's tables in shared memory.  On these
+// small levels the kernels are bound by the latency of their dependent
+// loads, not by bandwidth.  Converged scenes are not skipped here (their
+// cells are few and the result is unused).
+struct LevelS {
+    int l, n, off, nx, ny;
+};
 
 // largest scene index k with G.off[k] <= c (scenes absent from the level
 // have empty ranges)
@@ -249,21 +255,17 @@ __device__ __forceinline__ int scene_at(const MgLevel& G, int c) {
     }
     return lo;
 }
+__device__ __forceinline__ LevelS view_of(const MgLevel& G, int k) {
+    LevelS v;
+    v.l = G.l; v.n = G.n; v.off = G.off[k]; v.nx = G.nx[k]; v.ny = G.ny[k];
+    return v;
+}
 
-// Levels l -> l+1 for coarse cell Q: pre-smooth from zero, residual,
-// restriction (2x2 sum).
+// Levels l -> l+1 for coarse cell q of the scene: pre-smooth from zero,
+// residual, restriction (2x2 sum).
 template <typename T>
-__global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C) {
-    BS_PDL_ENTRY();
-    const int Q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (Q >= C.n) return;
-    const MgDev& M = D.mg;
-    const int k = scene_at(C, Q);
-    const int q = Q - C.off[k];
-    const int nyc = C.ny[k];
-    if (q >= nyc * C.nx[k]) return;   // reserved beyond the scene's current grid
-    const int I = q % nyc, J = q / nyc;
-    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
+__device__ __forceinline__ void op_down(const MgDev& M, const LevelS& F, const LevelS& C, int q) {
+    const int I = q % C.ny, J = q / C.ny;
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* __restrict__ dinv = (const T*)M.dinv[F.l];
     const T* __restrict__ r = (const T*)M.r[F.l];
@@ -272,8 +274,8 @@ __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_const
     for (int b = 0; b < 2; ++b)
         for (int a = 0; a < 2; ++a) {
             const int fi = 2 * I + a, fj = 2 * J + b;
-            if (fi >= fny || fj >= fnx) continue;
-            const int c = fo + fj * fny + fi;
+            if (fi >= F.ny || fj >= F.nx) continue;
+            const int c = F.off + fj * F.ny + fi;
             const T rc = r[c];
             if (!M.prec) {
                 sum += rc;
@@ -283,28 +285,21 @@ __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_const
 #pragma unroll
             for (int t = 0; t < 9; ++t) {
                 const int ni = fi + (t % 3) - 1, nj = fj + (t / 3) - 1;
-                if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
-                const int nb = fo + nj * fny + ni;
+                if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+                const int nb = F.off + nj * F.ny + ni;
                 ax += __ldg(A + (long)t * F.n + c) * (w * r[nb] * __ldg(dinv + nb));
             }
             sum += rc - ax;
         }
-    ((T*)M.r[C.l])[Q] = sum;
+    ((T*)M.r[C.l])[C.off + q] = sum;
 }
 
-// In-place residual on level l, cell c: r = r - A z (between the two visits
-// of a W-cycle level; reads its own r and the z of its stencil).
+// In-place residual on level l, cell q of the scene: r = r - A z (between
+// the two visits of a W-cycle level; reads its own r and the stencil's z).
 template <typename T>
-__global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
-    BS_PDL_ENTRY();
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= F.n) return;
-    const MgDev& M = D.mg;
-    const int k = scene_at(F, c);
-    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
-    const int q = c - fo;
-    if (q >= fnx * fny) return;
-    const int i = q % fny, j = q / fny;
+__device__ __forceinline__ void op_resid(const MgDev& M, const LevelS& F, int q) {
+    const int i = q % F.ny, j = q / F.ny;
+    const int c = F.off + q;
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* z = (const T*)M.z[F.l];
     T* r = (T*)M.r[F.l];
@@ -312,27 +307,18 @@ __global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
-        if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
-        ax += __ldg(A + (long)t * F.n + c) * z[fo + nj * fny + ni];
+        if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+        ax += __ldg(A + (long)t * F.n + c) * z[F.off + nj * F.ny + ni];
     }
     r[c] = r[c] - ax;
 }
 
-// Levels l+1 -> l for cell c: prolongation (constant per box, scaled) + one
-// post-sweep; with acc the result is added to z (second visit).
+// Levels l+1 -> l for cell q of the scene: prolongation (constant per box,
+// scaled) + one post-sweep; with acc the result is added to z.
 template <typename T>
-__global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C, int acc) {
-    BS_PDL_ENTRY();
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= F.n) return;
-    const MgDev& M = D.mg;
-    const int k = scene_at(F, c);
-    if (F.l >= F.lev[k]) return;   // the coarse solve wrote this level
-    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
-    const int q = c - fo;
-    if (q >= fnx * fny) return;
-    const int i = q % fny, j = q / fny;
-    const int nyc = C.ny[k], oc = C.off[k];
+__device__ __forceinline__ void op_up(const MgDev& M, const LevelS& F, const LevelS& C, int acc, int q) {
+    const int i = q % F.ny, j = q / F.ny;
+    const int c = F.off + q;
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* __restrict__ dinv = (const T*)M.dinv[F.l];
     const T* __restrict__ r = (const T*)M.r[F.l];
@@ -340,15 +326,15 @@ __global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constan
     const T w = (T)M.omega, cs = (T)M.cscale;
     const T wp = M.prec ? w : (T)0;
     auto zval = [&](int ii, int jj) -> T {
-        const int nb = fo + jj * fny + ii;
-        return wp * r[nb] * __ldg(dinv + nb) + cs * e[oc + (jj / 2) * nyc + (ii / 2)];
+        const int nb = F.off + jj * F.ny + ii;
+        return wp * r[nb] * __ldg(dinv + nb) + cs * e[C.off + (jj / 2) * C.ny + (ii / 2)];
     };
     const T zc = zval(i, j);
     T ax = 0;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
-        if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
+        if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
         ax += __ldg(A + (long)t * F.n + c) * (t == 4 ? zc : zval(ni, nj));
     }
     const T v = zc + w * __ldg(dinv + c) * (r[c] - ax);
@@ -356,20 +342,13 @@ __global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constan
     zo[c] = acc ? zo[c] + v : v;
 }
 
-// Coarsest level: damped Jacobi sweeps from zero in shared memory, one
-// block per scene whose coarsest level is F.l; with acc the result is added
-// to z (second visit).
+// Coarsest level of one scene: damped Jacobi sweeps from zero by the whole
+// block in shared memory (z, z2: coarse_max values each); with acc the
+// result is added to z.  Every thread of the block calls it.
 template <typename T>
-__global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
-    BS_PDL_ENTRY();
-    const int k = blockIdx.x;
-    if (F.lev[k] != F.l) return;
-    const MgDev& M = D.mg;
-    extern __shared__ unsigned char smem[];
-    T* z = (T*)smem;
+__device__ __forceinline__ void op_coarse(const MgDev& M, const LevelS& F, int acc, T* z) {
     T* z2 = z + M.coarse_max;
-    const int fo = F.off[k], fnx = F.nx[k], fny = F.ny[k];
-    const int m = fnx * fny;
+    const int m = F.nx * F.ny;
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* __restrict__ dinv = (const T*)M.dinv[F.l];
     const T* __restrict__ r = (const T*)M.r[F.l];
@@ -378,14 +357,14 @@ __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
     __syncthreads();
     for (int it = 0; it < M.coarse_sweeps; ++it) {
         for (int q = threadIdx.x; q < m; q += blockDim.x) {
-            const int i = q % fny, j = q / fny;
-            const int c = fo + q;
+            const int i = q % F.ny, j = q / F.ny;
+            const int c = F.off + q;
             T ax = 0;
 #pragma unroll
             for (int t = 0; t < 9; ++t) {
                 const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
-                if (ni < 0 || nj < 0 || ni >= fny || nj >= fnx) continue;
-                ax += __ldg(A + (long)t * F.n + c) * z[nj * fny + ni];
+                if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+                ax += __ldg(A + (long)t * F.n + c) * z[nj * F.ny + ni];
             }
             z2[q] = z[q] + w * __ldg(dinv + c) * (r[c] - ax);
         }
@@ -394,7 +373,113 @@ __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
         __syncthreads();
     }
     T* out = (T*)M.z[F.l];
-    for (int q = threadIdx.x; q < m; q += blockDim.x) out[fo + q] = acc ? out[fo + q] + z[q] : z[q];
+    for (int q = threadIdx.x; q < m; q += blockDim.x) out[F.off + q] = acc ? out[F.off + q] + z[q] : z[q];
+}
+
+// ---- one launch per level operation.  A scene whose tail kernel starts
+// at or above a level (F.l >= tl) is left to it.
+template <typename T>
+__global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C) {
+    BS_PDL_ENTRY();
+    const int Q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (Q >= C.n) return;
+    const int k = scene_at(C, Q);
+    const LevelS c = view_of(C, k);
+    const int q = Q - c.off;
+    if (q >= c.nx * c.ny || F.l >= F.tl[k]) return;   // reserved cells; tail kernel's levels
+    op_down<T>(D.mg, view_of(F, k), c, q);
+}
+
+template <typename T>
+__global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
+    BS_PDL_ENTRY();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F.n) return;
+    const int k = scene_at(F, c);
+    const LevelS f = view_of(F, k);
+    const int q = c - f.off;
+    if (q >= f.nx * f.ny || F.l > F.tl[k]) return;
+    op_resid<T>(D.mg, f, q);
+}
+
+template <typename T>
+__global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C, int acc) {
+    BS_PDL_ENTRY();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F.n) return;
+    const int k = scene_at(F, c);
+    if (F.l >= F.lev[k] || F.l >= F.tl[k]) return;   // written by the coarse solve / the tail kernel
+    const LevelS f = view_of(F, k);
+    const int q = c - f.off;
+    if (q >= f.nx * f.ny) return;
+    op_up<T>(D.mg, f, view_of(C, k), acc, q);
+}
+
+template <typename T>
+__global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
+    BS_PDL_ENTRY();
+    const int k = blockIdx.x;
+    if (F.lev[k] != F.l || F.tl[k] <= F.l) return;
+    extern __shared__ unsigned char smem[];
+    op_coarse<T>(D.mg, view_of(F, k), acc, (T*)smem);
+}
+
+// ---- tail kernel: one block per scene runs the scene's whole cycle from
+// its tail level tl (the first level with at most BS_MG_TAIL_CELLS cells)
+// down to its coarsest, the phases separated by block barriers instead of
+// kernel launches.  The same per-cell operations as the per-level kernels.
+template <typename T>
+__global__ void __launch_bounds__(BS_MG_TAIL_THREADS) k_mg_tail(Dev D, __grid_constant__ const MgLevel G, int acc) {
+    BS_PDL_ENTRY();
+    const int k = blockIdx.x;
+    const int tl = G.l;
+    if (G.tl[k] != tl) return;
+    const int Lc = G.lev[k];
+    const MgDev& M = D.mg;
+    __shared__ LevelS lv[BS_MG_MAXL + 2];
+    extern __shared__ unsigned char smem[];
+    if (threadIdx.x <= Lc - tl) {
+        const int l = tl + threadIdx.x;
+        LevelS v;
+        v.l = l; v.n = M.n[l]; v.off = M.off[l][k]; v.nx = M.nx[l][k]; v.ny = M.ny[l][k];
+        lv[l] = v;
+    }
+    __syncthreads();
+    // the recursion of cycle_t from tl, as an explicit stack (level, acc, stage)
+    int sl[BS_MG_MAXL + 2], sa[BS_MG_MAXL + 2], st[BS_MG_MAXL + 2];
+    int top = 1;
+    sl[0] = tl; sa[0] = acc; st[0] = 0;
+    while (top > 0) {
+        const int l = sl[top - 1], a = sa[top - 1];
+        if (st[top - 1] == 0) {
+            if (l == Lc) {
+                op_coarse<T>(M, lv[l], a, (T*)smem);
+                __syncthreads();
+                --top;
+                continue;
+            }
+            const LevelS F = lv[l], C = lv[l + 1];
+            for (int q = threadIdx.x; q < C.nx * C.ny; q += blockDim.x) op_down<T>(M, F, C, q);
+            __syncthreads();
+            st[top - 1] = 1;
+            sl[top] = l + 1; sa[top] = 0; st[top] = 0; ++top;
+            continue;
+        }
+        if (st[top - 1] == 1) {
+            st[top - 1] = 2;
+            if (l <= M.wlev) {
+                const LevelS C = lv[l + 1];
+                for (int q = threadIdx.x; q < C.nx * C.ny; q += blockDim.x) op_resid<T>(M, C, q);
+                __syncthreads();
+                sl[top] = l + 1; sa[top] = 1; st[top] = 0; ++top;
+                continue;
+            }
+        }
+        const LevelS F = lv[l], C = lv[l + 1];
+        for (int q = threadIdx.x; q < F.nx * F.ny; q += blockDim.x) op_up<T>(M, F, C, a, q);
+        __syncthreads();
+        --top;
+    }
 }
 
 // Level 0 post-sweep after the prolongation; writes the preconditioned
@@ -450,6 +535,11 @@ void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     const unsigned char need = L.mgneed[l];
     if (!(need & 1)) return;
     int q;
+    if (need & 8) {   // scenes whose cycle from level l runs in the tail kernel
+        q = tbegin(L, K_MG_TAIL);
+        launch_pdl(L, k_mg_tail<T>, D.nscene, BS_MG_TAIL_THREADS, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
+        tend(L, q);
+    }
     if (need & 4) {
         q = tbegin(L, K_MG_COARSE);
         launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);

@@ -64,8 +64,13 @@ def test_combined_gpu_matches_oracle(api, oracle, tmp_path):
     assert len(ra) == len(rb)
     A = np.array([_num(c) for c in zip(*ra)])
     B = np.array([_num(c) for c in zip(*rb)])
-    # same particles in the same order; values equal up to the last printed digit
-    assert np.all(np.abs(A[:3] - B[:3]) <= 1.001e-3)
+    # a field printed as asterisks (value does not fit F10.3) must be so in both
+    assert np.array_equal(np.isnan(A), np.isnan(B))
+    A, B = np.nan_to_num(A), np.nan_to_num(B)
+    # same particles in the same order; values equal up to the last printed
+    # digit (the pressure also within the step's 1e-8 relative parity)
+    assert np.all(np.abs(A[:2] - B[:2]) <= 1.001e-3)
+    assert np.all(np.abs(A[2] - B[2]) <= 1.001e-3 + 1e-7 * np.abs(B[2]))
     assert np.all(np.abs(A[3:5] - B[3:5]) <= 1.001e-3 * np.abs(B[3:5]) + 1e-12)
     assert np.all(np.abs(A[5] - B[5]) <= 1.001e-5)
     same = np.mean([ra[k] == rb[k] for k in range(len(ra))])
