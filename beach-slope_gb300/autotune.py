@@ -82,12 +82,12 @@ def tune(ctx, grains, steps=2, verbose=True):
             print(f"  {opts} -> {ms:.2f} ms/step, iters {iters:.0f}{'' if ok else ' (errors)'}", flush=True)
         return ms if ok else math.inf
 
-    base = {"mg_tail": 1, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
+    base = {"mg_tail": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
             "mg_coarse_sweeps": 10}
     best, best_ms = dict(base), run(base)
     stages = [
         [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
-        [{"mg_tail": t} for t in (0, 1)],
+        [{"mg_tail": t} for t in (0, 256, 1024, 4096)],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
         [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
         [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],

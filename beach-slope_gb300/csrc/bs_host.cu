@@ -123,9 +123,9 @@ void mg_tables(bs_ctx* c) {
             G.lev[s] = Lc;
             // tail level: the first level small enough for one block
             int tl = Lc + 1;
-            if (M.tail_on)
+            if (M.tail_on > 0)
                 for (int m = 1; m <= Lc; ++m)
-                    if (c->mgdims[s][m - 1].first * c->mgdims[s][m - 1].second <= BS_MG_TAIL_CELLS) {
+                    if (c->mgdims[s][m - 1].first * c->mgdims[s][m - 1].second <= M.tail_on) {
                         tl = m;
                         break;
                     }
@@ -369,7 +369,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.pre0 = 1;
         M.prec = 1;
         M.wlev = 2;
-        M.tail_on = 1;
+        M.tail_on = 0;
         // each scene reserves the levels of its creation grid (the largest
         // grid the slot takes, bs_set_scene)
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
@@ -776,8 +776,8 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_prec") M.prec = value != 0;
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
     else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
-    else if (k == "mg_tail") {
-        M.tail_on = value != 0;
+    else if (k == "mg_tail" && value >= 0 && value <= BS_MG_TAIL_CELLS) {
+        M.tail_on = (int)value;
         mg_tables(ctx);
         ctx->graph.valid = false;   // the level tables are baked into the captured chunk
     }

@@ -89,7 +89,8 @@ struct MgDev {
     int coarse_sweeps, coarse_max;
     int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
     int wlev;                         // levels 1..wlev recurse twice
-    int tail_on;                      // small levels of a scene in one block (k_mg_tail)
+    int tail_on;                      // >0: a scene's levels from the first with at most this many
+                                      // cells down run in one block (k_mg_tail); 0: per-level launches
     uint8_t* sub;                     // level 0: quadrant of the row in its cell (bit0 lower, bit1 right)
     int* agg1;                        // level 0: global level-1 index of the row's half-cell
 };
@@ -105,7 +106,7 @@ struct MgLevel {
     int lev[BS_MG_MAXS];       // the scene's coarsest level
     int tl[BS_MG_MAXS];        // the scene's tail level: from it down, one block runs the cycle
 };
-#define BS_MG_TAIL_CELLS 4096  // largest tail level (cells)
+#define BS_MG_TAIL_CELLS 4096  // largest tail level the option accepts (cells)
 #define BS_MG_TAIL_THREADS 1024
 
 // device pointers of one context (passed by value to kernels)

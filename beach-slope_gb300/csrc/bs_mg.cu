@@ -425,7 +425,7 @@ __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
 }
 
 // ---- tail kernel: one block per scene runs the scene's whole cycle from
-// its tail level tl (the first level with at most BS_MG_TAIL_CELLS cells)
+// its tail level tl (the first level with at most mg_tail cells)
 // down to its coarsest, the phases separated by block barriers instead of
 // kernel launches.  The same per-cell operations as the per-level kernels.
 template <typename T>

@@ -77,6 +77,14 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def aggregate(D, n_particles, steps, ms):
+    """Whole-job throughput of N replicas: every rank's particle-steps over
+    the slowest rank's time (value, max ms)."""
+    ms_max = D.allreduce(ms, "max")
+    parts = D.allreduce(n_particles, "sum")
+    return parts * steps / (ms_max / 1e3), ms_max
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
@@ -203,11 +211,10 @@ def run_ours(args, D):
     ms_timed = ctx.elapsed_ms(2, 3)
     kt = ctx.kernel_times()
     ctx.kernel_timing(0)
-    ms_max = D.allreduce(ms, "max")
-    parts = D.allreduce(n_particles, "sum")
+    value, ms_max = aggregate(D, n_particles, args.steps, ms)
     info = [ctx.info(s) for s in range(ctx.nscenes)]
     out = {
-        "value": parts * args.steps / (ms_max / 1e3),
+        "value": value,
         "ms_per_step": ms_max / args.steps,
         "particles": n_particles,
         "gpu_launches": int(l1 - l0),

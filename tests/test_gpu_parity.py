@@ -301,7 +301,7 @@ def test_tail_kernel_same_solution(api, precision):
         q.ppe_tol = 1e-12
         P.append(q)
     out = []
-    for tail in (1, 0):
+    for tail in (4096, 0):
         c = api.Context(P, [sc[1] for sc in scenes], [sc[2] for sc in scenes])
         c.set_option("mg_tail", tail)
         c.set_option("mg_wlev", 3)
