@@ -1,8 +1,7 @@
 """Autotuner for the PPE solver's multigrid V-cycle.
 
 Measures ms/step of the real workload (CUDA events on the context's stream)
-for a small staged grid of multigrid cycle shapes -- W-cycle depth, small
-levels in one block per scene or one launch per level,
+for a small staged grid of multigrid cycle shapes -- W-cycle depth,
 pre-smoothing on the particle and cell levels, Jacobi damping,
 coarse-correction scale, coarsest sweeps --
 and keeps the fastest configuration whose solves converged without error
@@ -17,7 +16,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
-OPTIONS = ("mg_tail", "mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
+OPTIONS = ("mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
 
 
 def bucket(n_particles):
@@ -82,12 +81,11 @@ def tune(ctx, grains, steps=2, verbose=True):
             print(f"  {opts} -> {ms:.2f} ms/step, iters {iters:.0f}{'' if ok else ' (errors)'}", flush=True)
         return ms if ok else math.inf
 
-    base = {"mg_tail": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
+    base = {"mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
             "mg_coarse_sweeps": 10}
     best, best_ms = dict(base), run(base)
     stages = [
         [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
-        [{"mg_tail": t} for t in (0, 256, 1024, 4096)],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
         [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
         [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],

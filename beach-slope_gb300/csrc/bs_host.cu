@@ -121,21 +121,10 @@ void mg_tables(bs_ctx* c) {
             G.nx[s] = nxv[s] = has ? c->mgdims[s][l - 1].first : 0;
             G.ny[s] = nyv[s] = has ? c->mgdims[s][l - 1].second : 0;
             G.lev[s] = Lc;
-            // tail level: the first level small enough for one block
-            int tl = Lc + 1;
-            if (M.tail_on > 0)
-                for (int m = 1; m <= Lc; ++m)
-                    if (c->mgdims[s][m - 1].first * c->mgdims[s][m - 1].second <= M.tail_on) {
-                        tl = m;
-                        break;
-                    }
-            G.tl[s] = tl;
             o += (int)c->mgrange[s].size() >= l ? c->mgrange[s][l - 1] : 0;
-            const int stop = std::min(tl, Lc);   // last level visited by per-level launches
-            if (l <= stop) c->mgneed[l] |= 1;
-            if (l < stop) c->mgneed[l] |= 2;
-            if (l == Lc && tl > Lc) c->mgneed[l] |= 4;
-            if (l == tl && tl <= Lc) c->mgneed[l] |= 8;
+            if (l <= Lc) c->mgneed[l] |= 1;
+            if (l < Lc) c->mgneed[l] |= 2;
+            if (l == Lc) c->mgneed[l] |= 4;
         }
         G.off[ns] = o;
         cudaMemcpy((void*)M.nx[l], nxv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
@@ -369,7 +358,6 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.pre0 = 1;
         M.prec = 1;
         M.wlev = 2;
-        M.tail_on = 0;
         // each scene reserves the levels of its creation grid (the largest
         // grid the slot takes, bs_set_scene)
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
@@ -776,11 +764,6 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_prec") M.prec = value != 0;
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
     else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
-    else if (k == "mg_tail" && value >= 0 && value <= BS_MG_TAIL_CELLS) {
-        M.tail_on = (int)value;
-        mg_tables(ctx);
-        ctx->graph.valid = false;   // the level tables are baked into the captured chunk
-    }
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
     ctx->graph.valid = false;   // the captured iteration holds the old values
@@ -797,7 +780,6 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "mg_prec") *value = M.prec;
     else if (k == "mg_coarse_sweeps") *value = M.coarse_sweeps;
     else if (k == "mg_wlev") *value = M.wlev;
-    else if (k == "mg_tail") *value = M.tail_on;
     else if (k == "mg_levels") *value = M.nlev;
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
     else return BS_E_ARG;

@@ -89,8 +89,6 @@ struct MgDev {
     int coarse_sweeps, coarse_max;
     int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
     int wlev;                         // levels 1..wlev recurse twice
-    int tail_on;                      // >0: a scene's levels from the first with at most this many
-                                      // cells down run in one block (k_mg_tail); 0: per-level launches
     uint8_t* sub;                     // level 0: quadrant of the row in its cell (bit0 lower, bit1 right)
     int* agg1;                        // level 0: global level-1 index of the row's half-cell
 };
@@ -104,10 +102,7 @@ struct MgLevel {
     int off[BS_MG_MAXS + 1];
     int nx[BS_MG_MAXS], ny[BS_MG_MAXS];
     int lev[BS_MG_MAXS];       // the scene's coarsest level
-    int tl[BS_MG_MAXS];        // the scene's tail level: from it down, one block runs the cycle
 };
-#define BS_MG_TAIL_CELLS 4096  // largest tail level the option accepts (cells)
-#define BS_MG_TAIL_THREADS 1024
 
 // device pointers of one context (passed by value to kernels)
 struct Dev {
@@ -310,7 +305,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_MG_TAIL, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -340,8 +335,7 @@ struct Launch {
     IterGraph* graph;   // nullptr: launch kernels one by one
     const MgLevel* mglev;          // host tables of the multigrid levels, indexed by level
     const unsigned char* mgneed;   // per level: bit0 some scene visits it, bit1 restriction and
-                                   // prolongation to the next level, bit2 coarsest-level solve,
-                                   // bit3 tail kernel entered here
+                                   // prolongation to the next level, bit2 coarsest-level solve
 };
 // Programmatic dependent launch: a kernel launched by launch_pdl may be
 // scheduled while its predecessor in the stream still runs.  Its first

@@ -236,7 +236,7 @@ __global__ void k_mg_l0_prolong(Dev D) {
 // and the level's total size (the stride of the stencil arrays).  The
 // per-level kernels build views from the MgLevel tables (kernel arguments,
 // in the constant bank: no memory round trip for a cell's scene, offsets and
-// grid); the tail kernel from its scene's tables in shared memory.  On these
+// grid).  On these
 // small levels the kernels are bound by the latency of their dependent
 // loads, not by bandwidth.  Converged scenes are not skipped here (their
 // cells are few and the result is unused).
@@ -376,8 +376,7 @@ __device__ __forceinline__ void op_coarse(const MgDev& M, const LevelS& F, int a
     for (int q = threadIdx.x; q < m; q += blockDim.x) out[F.off + q] = acc ? out[F.off + q] + z[q] : z[q];
 }
 
-// ---- one launch per level operation.  A scene whose tail kernel starts
-// at or above a level (F.l >= tl) is left to it.
+// ---- one launch per level operation
 template <typename T>
 __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C) {
     BS_PDL_ENTRY();
@@ -386,7 +385,7 @@ __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_const
     const int k = scene_at(C, Q);
     const LevelS c = view_of(C, k);
     const int q = Q - c.off;
-    if (q >= c.nx * c.ny || F.l >= F.tl[k]) return;   // reserved cells; tail kernel's levels
+    if (q >= c.nx * c.ny) return;   // reserved beyond the scene's current grid
     op_down<T>(D.mg, view_of(F, k), c, q);
 }
 
@@ -398,7 +397,7 @@ __global__ void k_mg_resid(Dev D, __grid_constant__ const MgLevel F) {
     const int k = scene_at(F, c);
     const LevelS f = view_of(F, k);
     const int q = c - f.off;
-    if (q >= f.nx * f.ny || F.l > F.tl[k]) return;
+    if (q >= f.nx * f.ny) return;
     op_resid<T>(D.mg, f, q);
 }
 
@@ -408,7 +407,7 @@ __global__ void k_mg_up(Dev D, __grid_constant__ const MgLevel F, __grid_constan
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= F.n) return;
     const int k = scene_at(F, c);
-    if (F.l >= F.lev[k] || F.l >= F.tl[k]) return;   // written by the coarse solve / the tail kernel
+    if (F.l >= F.lev[k]) return;   // the coarse solve wrote this level
     const LevelS f = view_of(F, k);
     const int q = c - f.off;
     if (q >= f.nx * f.ny) return;
@@ -419,67 +418,9 @@ template <typename T>
 __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
     BS_PDL_ENTRY();
     const int k = blockIdx.x;
-    if (F.lev[k] != F.l || F.tl[k] <= F.l) return;
+    if (F.lev[k] != F.l) return;
     extern __shared__ unsigned char smem[];
     op_coarse<T>(D.mg, view_of(F, k), acc, (T*)smem);
-}
-
-// ---- tail kernel: one block per scene runs the scene's whole cycle from
-// its tail level tl (the first level with at most mg_tail cells)
-// down to its coarsest, the phases separated by block barriers instead of
-// kernel launches.  The same per-cell operations as the per-level kernels.
-template <typename T>
-__global__ void __launch_bounds__(BS_MG_TAIL_THREADS) k_mg_tail(Dev D, __grid_constant__ const MgLevel G, int acc) {
-    BS_PDL_ENTRY();
-    const int k = blockIdx.x;
-    const int tl = G.l;
-    if (G.tl[k] != tl) return;
-    const int Lc = G.lev[k];
-    const MgDev& M = D.mg;
-    __shared__ LevelS lv[BS_MG_MAXL + 2];
-    extern __shared__ unsigned char smem[];
-    if (threadIdx.x <= Lc - tl) {
-        const int l = tl + threadIdx.x;
-        LevelS v;
-        v.l = l; v.n = M.n[l]; v.off = M.off[l][k]; v.nx = M.nx[l][k]; v.ny = M.ny[l][k];
-        lv[l] = v;
-    }
-    __syncthreads();
-    // the recursion of cycle_t from tl, as an explicit stack (level, acc, stage)
-    int sl[BS_MG_MAXL + 2], sa[BS_MG_MAXL + 2], st[BS_MG_MAXL + 2];
-    int top = 1;
-    sl[0] = tl; sa[0] = acc; st[0] = 0;
-    while (top > 0) {
-        const int l = sl[top - 1], a = sa[top - 1];
-        if (st[top - 1] == 0) {
-            if (l == Lc) {
-                op_coarse<T>(M, lv[l], a, (T*)smem);
-                __syncthreads();
-                --top;
-                continue;
-            }
-            const LevelS F = lv[l], C = lv[l + 1];
-            for (int q = threadIdx.x; q < C.nx * C.ny; q += blockDim.x) op_down<T>(M, F, C, q);
-            __syncthreads();
-            st[top - 1] = 1;
-            sl[top] = l + 1; sa[top] = 0; st[top] = 0; ++top;
-            continue;
-        }
-        if (st[top - 1] == 1) {
-            st[top - 1] = 2;
-            if (l <= M.wlev) {
-                const LevelS C = lv[l + 1];
-                for (int q = threadIdx.x; q < C.nx * C.ny; q += blockDim.x) op_resid<T>(M, C, q);
-                __syncthreads();
-                sl[top] = l + 1; sa[top] = 1; st[top] = 0; ++top;
-                continue;
-            }
-        }
-        const LevelS F = lv[l], C = lv[l + 1];
-        for (int q = threadIdx.x; q < F.nx * F.ny; q += blockDim.x) op_up<T>(M, F, C, a, q);
-        __syncthreads();
-        --top;
-    }
 }
 
 // Level 0 post-sweep after the prolongation; writes the preconditioned
@@ -535,11 +476,6 @@ void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     const unsigned char need = L.mgneed[l];
     if (!(need & 1)) return;
     int q;
-    if (need & 8) {   // scenes whose cycle from level l runs in the tail kernel
-        q = tbegin(L, K_MG_TAIL);
-        launch_pdl(L, k_mg_tail<T>, D.nscene, BS_MG_TAIL_THREADS, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
-        tend(L, q);
-    }
     if (need & 4) {
         q = tbegin(L, K_MG_COARSE);
         launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);

@@ -225,9 +225,7 @@ int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path,
  * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
  * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),
  * "mg_coarse_sweeps", "mg_wlev" (coarse levels 1..mg_wlev visit the next
- * level twice: W-cycle on top, V-cycle below), "mg_tail" (n > 0: a scene's
- * levels from the first one of at most n <= 4096 cells down run in one block
- * per scene; 0: one launch per level operation), "ppe_precond";
+ * level twice: W-cycle on top, V-cycle below), "ppe_precond";
  * bs_get_option also reads "mg_levels". */
 int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
 int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);

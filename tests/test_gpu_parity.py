@@ -287,34 +287,6 @@ def test_batched_scenes_equal_alone(api):
         assert alone.info()["ppe_iters"] == batch.info(k)["ppe_iters"]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_tail_kernel_same_solution(api, precision):
-    """A scene's small multigrid levels run in one block (tail kernel) or as
-    one launch per level operation: the same preconditioner arithmetic, so
-    the same iterations and, solved to 1e-12, the same pressure."""
-    from beachslope_gb300 import abi, scene
-    scenes = [scene.beach_scene(dx=d, A=a) for d, a in ((0.008, 0.05), (0.02, 0.08))]
-    P = []
-    for sc in scenes:
-        q = abi.Params.from_buffer_copy(sc[0])
-        q.precision = abi.PREC_MIXED if precision == "mixed" else abi.PREC_FP64
-        q.ppe_tol = 1e-12
-        P.append(q)
-    out = []
-    for tail in (4096, 0):
-        c = api.Context(P, [sc[1] for sc in scenes], [sc[2] for sc in scenes])
-        c.set_option("mg_tail", tail)
-        c.set_option("mg_wlev", 3)
-        c.prime()
-        c.step(2)
-        out.append(([c.download(k) for k in range(2)], [c.info(k) for k in range(2)]))
-        c.close()
-    for k in range(2):
-        assert relL2(out[0][0][k]["p"], out[1][0][k]["p"]) < 1e-9
-        assert abs(out[0][1][k]["ppe_iters"] - out[1][1][k]["ppe_iters"]) <= 1
-        assert out[0][1][k]["err_bits"] == 0
-
-
 def test_mixed_precision_against_fp64(api):
     """The mixed form (FP32 pair storage and sweeps, FP32 V-cycle, FP64
     Krylov) from the same state as the FP64 drop-in: identical neighbour sets
