@@ -26,7 +26,8 @@ ERR_BITS = {
 TID_WALL, TID_GHOST, TID_FLUID = 1, 2, 3
 FLAG_FREE, FLAG_VICINITY, FLAG_BUFFER = 0x01, 0x02, 0x04
 PREC_FP64, PREC_MIXED = 0, 1
-STOP_RELRES, STOP_REFERENCE = 0, 1
+STOP_RELRES, STOP_REFERENCE, STOP_R0 = 0, 1, 2
+SOLVER_BICGSTAB, SOLVER_FGMRES = 0, 1
 
 _d = C.c_double
 _i = C.c_int32
@@ -47,6 +48,7 @@ class Params(C.Structure):
         ("ppe_tol", _d), ("ppe_maxit", _i), ("ppe_stop", _i), ("precision", _i),
         ("kmax", _i), ("mixed_inner_tol", _d), ("mixed_max_outer", _i), ("ppe_precond", _i),
         ("wc_c0", _d), ("wc_gamma", _d), ("wc_delta", _d), ("wc_ysurf", _d), ("wc_form", _i), ("wc_pad", _i),
+        ("ppe_solver", _i), ("ppe_restart", _i),
     ]
 
     def as_dict(self):
@@ -92,6 +94,8 @@ def default_params():
     p.wc_gamma = 7.0        # t_gam, initialize.f90:46
     p.wc_delta = 0.1        # delt, initialize.f90:40
     p.wc_ysurf = 0.0        # set per scene (still-water level)
+    p.ppe_solver = 0        # BiCGStab
+    p.ppe_restart = 150     # FGMRES restart length (MKL's default in the reference's call)
     return p
 
 

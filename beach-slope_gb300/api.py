@@ -71,6 +71,7 @@ def _load():
         "bs_wcsph_step": (C.c_int, [vp, i32]),
         "bs_bicgstab_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, vp, vp]),
         "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
+        "bs_fgmres_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, i32, vp, vp]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
         "bs_kernel_timing": (C.c_int, [vp, C.c_uint64]),
@@ -295,6 +296,21 @@ def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=abi.STOP_
     rr = C.c_double()
     rc = lib.bs_bicgstab_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data, b.ctypes.data,
                              x.ctypes.data, tol, maxit, rule, C.byref(it), C.byref(rr))
+    return rc, x, it.value, rr.value
+
+
+def fgmres_csr(row_ptr, col, val, b, x0, tol=1e-3, maxit=150, restart=150, rule=abi.STOP_R0):
+    """fgmres (solver.f90:306-350): restarted GMRES on a host CSR system,
+    solved on the GPU; defaults are the reference's MKL settings."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    it = C.c_int32()
+    rr = C.c_double()
+    rc = lib.bs_fgmres_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data, b.ctypes.data,
+                           x.ctypes.data, tol, maxit, restart, rule, C.byref(it), C.byref(rr))
     return rc, x, it.value, rr.value
 
 

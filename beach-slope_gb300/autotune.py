@@ -1,9 +1,10 @@
-"""Autotuner for the PPE solver's multigrid V-cycle.
+"""Autotuner for the PPE solver: Krylov method and multigrid cycle shape.
 
 Measures ms/step of the real workload (CUDA events on the context's stream)
-for a small staged grid of multigrid cycle shapes -- W-cycle depth,
+for a small staged grid -- the Krylov method (BiCGStab, or FGMRES with a
+restart length), then the multigrid cycle shape (W-cycle depth,
 pre-smoothing on the particle and cell levels, Jacobi damping,
-coarse-correction scale, coarsest sweeps --
+coarse-correction scale, coarsest sweeps), then the restart length again --
 and keeps the fastest configuration whose solves converged without error
 bits.  The result is written to tuning.json next to this file, keyed by
 precision and a particle-count bucket; Context(..., tuning="auto") applies it.
@@ -16,7 +17,8 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
-OPTIONS = ("mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale", "mg_coarse_sweeps")
+OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale",
+           "mg_coarse_sweeps")
 
 
 def bucket(n_particles):
@@ -81,15 +83,18 @@ def tune(ctx, grains, steps=2, verbose=True):
             print(f"  {opts} -> {ms:.2f} ms/step, iters {iters:.0f}{'' if ok else ' (errors)'}", flush=True)
         return ms if ok else math.inf
 
-    base = {"mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9, "mg_cscale": 1.5,
-            "mg_coarse_sweeps": 10}
+    base = {"ppe_restart": 30, "ppe_solver": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9,
+            "mg_cscale": 1.5, "mg_coarse_sweeps": 10}
     best, best_ms = dict(base), run(base)
+    solver_stage = [{"ppe_solver": 0}] + [{"ppe_solver": 1, "ppe_restart": r} for r in (20, 30, 50, 80, 120)]
     stages = [
+        solver_stage,
         [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
         [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
         [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],
         [{"mg_coarse_sweeps": c} for c in (5, 10, 20)],
+        solver_stage,
     ]
     for stage in stages:
         stage_best, stage_ms = best, best_ms
@@ -118,8 +123,9 @@ def save(precision, n_particles, best, best_ms, workload):
 def apply(ctx, precision, n_particles):
     t = lookup(precision, n_particles)
     if t:
-        for k, v in t["options"].items():
-            ctx.set_option(k, v)
+        # the restart length before the method, so FGMRES storage is sized once
+        for k in sorted(t["options"], key=lambda k: OPTIONS.index(k) if k in OPTIONS else len(OPTIONS)):
+            ctx.set_option(k, t["options"][k])
     return t
 
 

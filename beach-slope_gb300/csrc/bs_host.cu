@@ -22,7 +22,7 @@ struct bs_ctx {
     int nscene = 0;
     std::vector<bs_params> prm;
     std::vector<ScenePar> hpar;
-    int nrow_total = 0, nblk_total = 0, ncell_total = 0, kmax = 0, ngrain_total = 0;
+    int nrow_total = 0, nblk_total = 0, ncell_total = 0, kmax = 0, ngrain_total = 0, ngrp_total = 0;
     int precision = 0;
     std::vector<int> grain0, gcap;
     Dev D{};
@@ -68,6 +68,57 @@ int dalloc(bs_ctx* ctx, T** p, size_t n) {
     cudaMemset(q, 0, n * sizeof(T));
     ctx->allocs.push_back(q);
     *p = (T*)q;
+    return 0;
+}
+
+template <class T>
+void dfree(bs_ctx* ctx, T*& p) {
+    if (!p) return;
+    for (size_t i = 0; i < ctx->allocs.size(); ++i)
+        if (ctx->allocs[i] == (void*)p) {
+            ctx->allocs.erase(ctx->allocs.begin() + i);
+            break;
+        }
+    cudaFree(p);
+    p = nullptr;
+}
+
+// FGMRES storage for the context's restart length and preconditioner: basis
+// V [(m+1) x rows], preconditioned basis Z [m x rows] (only with the
+// multigrid cycle), block partials and the per-scene small matrices
+int fg_ensure(bs_ctx* ctx) {
+    Dev& D = ctx->D;
+    const int m = ctx->prm[0].ppe_restart;
+    const bool precond = ctx->prm[0].ppe_precond != 0;
+    if (m < 1 || m > BS_FG_MAXM) return fail(ctx, BS_E_ARG, "ppe_restart outside 1..150");
+    if (D.fg_V && D.fg_m == m && (!precond || D.fg_Z)) return 0;
+    cudaStreamSynchronize(ctx->stream);
+    auto release = [&]() {
+        dfree(ctx, D.fg_V);
+        dfree(ctx, D.fg_Z);
+        dfree(ctx, D.fg_part);
+        dfree(ctx, D.fg_gpart);
+        dfree(ctx, D.fg_small);
+        dfree(ctx, D.fg_gdone);
+    };
+    release();
+    const size_t R = ctx->nrow_total;
+    const size_t ld = bs::fg_part_ld(m);
+    int rc = dalloc(ctx, &D.fg_V, (size_t)(m + 1) * R);
+    if (!rc && precond) rc = dalloc(ctx, &D.fg_Z, (size_t)m * R);
+    if (!rc) rc = dalloc(ctx, &D.fg_part, (size_t)ctx->nblk_total * ld);
+    if (!rc) rc = dalloc(ctx, &D.fg_gpart, (size_t)ctx->ngrp_total * ld);
+    if (!rc) rc = dalloc(ctx, &D.fg_gdone, (size_t)ctx->ngrp_total);
+    if (!rc) rc = dalloc(ctx, &D.fg_small, (size_t)ctx->nscene * bs::fg_small_size(m));
+    if (rc) {
+        release();
+        D.fg_m = 0;
+        return rc;
+    }
+    D.fg_m = m;
+    D.fg_ld = (int)R;
+    D.fg_small_n = bs::fg_small_size(m);
+    ctx->graph.valid = false;
     return 0;
 }
 
@@ -230,7 +281,11 @@ int st_solve(bs_ctx* c) {
     bs::Launch L = launch_of(c);
     int maxit = 0;
     for (auto& p : c->prm) maxit = std::max(maxit, (int)p.ppe_maxit);
-    if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
+    if (c->prm[0].ppe_solver == BS_SOLVER_FGMRES) {
+        if (int rc = fg_ensure(c)) return rc;
+        bs::solve_fgmres(c->D, L, maxit, c->prm[0].ppe_precond ? 2 : 8, c->prm[0].ppe_precond, c->precision,
+                         c->d_nconv, c->h_pinned, c->evsync);
+    } else if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
         bs::solve_mixed(c->D, L, maxit, 8, c->d_nconv, c->h_pinned, c->evsync);
     else
         bs::solve_fp64(c->D, L, maxit, c->prm[0].ppe_precond ? 4 : 8, c->prm[0].ppe_precond, c->precision,
@@ -253,6 +308,7 @@ void bs_params_default(bs_params* p) {
     p->ppe_tol = 1e-8; p->ppe_maxit = 5000; p->ppe_stop = BS_STOP_RELRES; p->precision = BS_PREC_FP64;
     p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 0;
     p->wc_gamma = 7.0; p->wc_delta = 0.1;
+    p->ppe_solver = BS_SOLVER_BICGSTAB; p->ppe_restart = 150;
 }
 
 int bs_set_device(int32_t device) {
@@ -277,7 +333,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     }
     if (ctx->kmax <= 0 || ctx->kmax > 64) { delete ctx; return BS_E_ARG; }
     // layout
-    int row = 0, blk = 0, cell = 0, gr = 0;
+    int row = 0, blk = 0, cell = 0, gr = 0, grp = 0;
     std::vector<int> blk_scene, cell_scene;
     ctx->hpar.resize(nscenes);
     for (int s = 0; s < nscenes; ++s) {
@@ -289,6 +345,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         P.cell0 = cell;
         P.row0 = row; P.cap = cap;
         P.nblk = cap / BS_THREADS; P.blk0 = blk;
+        P.grp0 = grp;
+        grp += (P.nblk + 31) / 32;
         ctx->cellx_cap.push_back(p.cellx);
         ctx->celly_cap.push_back(p.celly);
         for (int b = 0; b < P.nblk; ++b) blk_scene.push_back(s);
@@ -303,6 +361,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     }
     ctx->nrow_total = row;
     ctx->nblk_total = blk;
+    ctx->ngrp_total = grp;
     ctx->ncell_total = cell;
     ctx->ngrain_total = gr;
     Dev& D = ctx->D;
@@ -460,10 +519,19 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     D.nblk_total = blk;
     D.nscene = nscenes;
     D.kmax = ctx->kmax;
+    D.fg_V = D.fg_Z = D.fg_part = D.fg_gpart = D.fg_small = nullptr;
+    D.fg_gdone = nullptr;
+    D.fg_m = D.fg_small_n = D.fg_ld = 0;
     cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (auto& e : ctx->ev) cudaEventCreate(&e);
     cudaEventCreateWithFlags(&ctx->evsync, cudaEventDisableTiming);
     cudaMallocHost(&ctx->h_pinned, sizeof(int) * (nscenes + 4));
+    if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES) {
+        if (int r2 = fg_ensure(ctx)) {
+            bs_destroy(ctx);
+            return r2;
+        }
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         bs_destroy(ctx);
@@ -765,7 +833,13 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
     else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
+    else if (k == "ppe_solver" && (value == BS_SOLVER_BICGSTAB || value == BS_SOLVER_FGMRES))
+        for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
+    else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
+        for (auto& p : ctx->prm) p.ppe_restart = (int32_t)value;
     else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
+    if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
+        if (int rc = fg_ensure(ctx)) return rc;
     ctx->graph.valid = false;   // the captured iteration holds the old values
     return 0;
 }
@@ -782,6 +856,8 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "mg_wlev") *value = M.wlev;
     else if (k == "mg_levels") *value = M.nlev;
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
+    else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;
+    else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
     else return BS_E_ARG;
     return 0;
 }
@@ -962,8 +1038,9 @@ int bs_ppe_assemble(bs_ctx* ctx) {
 int bs_ppe_solve(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     if (!ctx->assembled) return fail(ctx, BS_E_STATE, "solve before assemble");
-    st_solve(ctx);
-    int rc = bs_sync(ctx);
+    int rc = st_solve(ctx);
+    if (rc) return rc;
+    rc = bs_sync(ctx);
     if (rc) return rc;
     unsigned e = 0;
     CK(cudaMemcpy(&e, ctx->D.err_word, sizeof(unsigned), cudaMemcpyDeviceToHost));
@@ -1096,7 +1173,7 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
         bs::int_vel(D, L, ctx->precision);
         bs::assemble(D, L, ctx->precision);
         ctx->assembled = true;
-        st_solve(ctx);                       // bicgstab + pressure scatter
+        if (int rc = st_solve(ctx)) return rc;   // bicgstab / fgmres + pressure scatter
         bs::comp_vel(D, L, ctx->precision, 1, 1);   // comp_vel + comp_pos
         bs::cell_max_timestep(D, L, 1, 0);
         st_rebin(ctx, 0, 1);                 // cellshiftalt
@@ -1117,8 +1194,9 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
 
 // Stand-alone BiCGStab on a host CSR system: the system becomes a one-scene
 // context (diagonal entries summed into adiag, the rest in the sliced ELL).
-int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val, const double* b,
-                    double* x, double tol, int32_t maxit, int32_t stop_rule, int32_t* iters, double* relres) {
+static int krylov_csr(int solver, int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                      const double* b, double* x, double tol, int32_t maxit, int32_t restart, int32_t stop_rule,
+                      int32_t* iters, double* relres) {
     if (n <= 0 || !row_ptr || !col || !val || !b || !x) return BS_E_ARG;
     int kmax = 1;
     for (int r = 0; r < n; ++r) {
@@ -1135,6 +1213,8 @@ int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const
     p.ppe_tol = tol;
     p.ppe_maxit = maxit;
     p.ppe_stop = stop_rule;
+    p.ppe_solver = solver;
+    p.ppe_restart = restart;
     bs_ctx* ctx = nullptr;
     int rc = bs_create(1, &p, &n, nullptr, &ctx);
     if (rc) return rc;
@@ -1162,7 +1242,10 @@ int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const
     CK(cudaMemcpy(D.nidx, idx.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(D.aval, aval.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
     ctx->assembled = true;
-    bs::solve_fp64(D, launch_of(ctx), maxit, 1, 0, BS_PREC_FP64, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
+    if (solver == BS_SOLVER_FGMRES)
+        bs::solve_fgmres(D, launch_of(ctx), maxit, 1, 0, BS_PREC_FP64, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
+    else
+        bs::solve_fp64(D, launch_of(ctx), maxit, 1, 0, BS_PREC_FP64, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
     rc = bs_sync(ctx);
     if (!rc) {
         CK(cudaMemcpy(x, D.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
@@ -1173,6 +1256,18 @@ int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const
     }
     bs_destroy(ctx);
     return rc;
+}
+
+int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val, const double* b,
+                    double* x, double tol, int32_t maxit, int32_t stop_rule, int32_t* iters, double* relres) {
+    return krylov_csr(BS_SOLVER_BICGSTAB, n, row_ptr, col, val, b, x, tol, maxit, 150, stop_rule, iters, relres);
+}
+
+int bs_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val, const double* b,
+                  double* x, double tol, int32_t maxit, int32_t restart, int32_t stop_rule, int32_t* iters,
+                  double* relres) {
+    if (restart < 1 || restart > BS_FG_MAXM) return BS_E_ARG;
+    return krylov_csr(BS_SOLVER_FGMRES, n, row_ptr, col, val, b, x, tol, maxit, restart, stop_rule, iters, relres);
 }
 
 int bs_event_record(bs_ctx* ctx, int32_t slot) {

@@ -24,6 +24,7 @@
 #define BS_THREADS 256
 #define BS_NCAT 10      // bucket categories per cell in the re-bin (see k_rank)
 #define BS_MAXDOT 8     // partial sums per block in the solver
+#define BS_FG_MAXM 150  // longest FGMRES restart cycle (the reference's MKL default)
 
 // constants with the reference's literal precision (default REAL = single)
 #define BS_C28 ((double)(28.0f * 3.14f))   // kernel.f90:61
@@ -49,6 +50,7 @@ struct ScenePar {                 // per-scene constants
     int row0, cap, kmax, maxit;
     int adaptive_dt, scalar_on, precision, stop_rule;
     int nblk, blk0, max_outer, mg_lev;   // mg_lev: this scene's coarsest multigrid level
+    int grp0, pad_grp;                    // first group of 32 row blocks (two-level reductions)
 };
 
 struct SceneDyn {                 // per-scene dynamic state (device)
@@ -61,6 +63,9 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     unsigned err;
     int hold;                      // 1: row sweeps and timestep leave the scene alone (bs_prime_scene)
     double part_tmp;
+    // FGMRES: Arnoldi column of the current cycle, cycle state (0 running,
+    // 1 restart, 2 converged, 3 iteration cap) and the columns the update applies
+    int fg_j, fg_state, fg_k, fg_pad;
 };
 
 // Aggregation multigrid over the cell grid.  Level 1 = half-cells (2h x 2h,
@@ -145,6 +150,13 @@ struct Dev {
     const int* cell_scene;          // global cell -> scene
     int* blk_done;                  // per-scene block counters for finisher reductions
     double* part;                   // per-block partial sums [nblk_total][BS_MAXDOT]
+    // FGMRES (ppe_solver = BS_SOLVER_FGMRES): Krylov basis V [(m+1) x rows],
+    // preconditioned basis Z [m x rows], partials per block and per group of
+    // 32 blocks [.. x (2m+4)], per-scene Hessenberg and Gram matrices,
+    // rotations and right-hand side [nscene x fg_small]
+    double *fg_V, *fg_Z, *fg_part, *fg_gpart, *fg_small;
+    int* fg_gdone;                  // per-group block counters
+    int fg_m, fg_small_n, fg_ld;    // restart length, doubles per scene, rows per basis vector
     // cells
     int *cell_start, *cell_end, *cell_start2, *cell_end2;
     int* bucket;                    // [ncell_total*BS_NCAT] counts then starts
@@ -305,7 +317,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -322,7 +334,7 @@ struct KTimer {
 struct IterGraph {
     cudaGraphExec_t exec = nullptr;
     Dev key;
-    int precond = -1, prec = -1, chunk = 0;
+    int precond = -1, prec = -1, chunk = 0, solver = -1;
     int64_t nkernels = 0;
     bool valid = false;
 };
@@ -410,4 +422,9 @@ __device__ __forceinline__ void mg_put_input(const Dev& D, int r, double x) {
 }
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_all_conv,
                  int* h_all_conv_pinned, cudaEvent_t ev);
+void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
+                  int* d_nconv, int* h_nconv, cudaEvent_t ev);
+// per-scene small FGMRES storage for restart length m (doubles)
+inline int fg_small_size(int m) { return (m + 1) * m + (m + 1) * (m + 1) + 2 * m + (m + 1) + m + (m + 1) + 8; }
+__host__ __device__ inline int fg_part_ld(int m) { return 2 * m + 4; }
 }  // namespace bs

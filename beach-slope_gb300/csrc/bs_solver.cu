@@ -511,6 +511,425 @@ __global__ void k_true_res64(Dev D) {
     }
 }
 
+// ---------------------------------------------------------------- FGMRES
+// Restarted flexible GMRES (Saad, SIAM J. Sci. Comput. 14, 1993), the Krylov
+// method of the reference's live solver (fgmres, solver.f90:306-350: MKL's
+// RCI dfgmres with spmv2 as the operator, the previous pressure as the first
+// guess, memory.f90:144, isph.f90:477).  Per scene: r0 = b - A x0, v0 =
+// r0/||r0||; column j: z_j = M^-1 v_j (the multigrid cycle; z_j = v_j
+// unpreconditioned), w = A z_j, classical Gram-Schmidt against v_0..v_j
+// applied twice in two passes over the basis (the second projection from
+// the basis' Gram matrix), h_{j+1,j} = ||w||, v_{j+1} = w / h_{j+1,j}; Givens rotations keep
+// the least-squares residual |g_{j+1}| current.  The cycle ends when |g_{j+1}|
+// <= ref, h_{j+1,j} <= 1e-12 (lucky breakdown), j+1 = m (restart) or at the
+// iteration cap; then y = R^-1 g and x += Z y.  Scenes run their cycles in lock
+// step; a scene whose cycle ended returns at the top of every column kernel,
+// and the column index lives in the scene's state, so one captured chunk of
+// columns serves every cycle.
+
+// Per-scene small storage: H [(m+1) x m] column-major (R of the rotated
+// Hessenberg matrix), Gm [(m+1) x (m+1)] (the Gram matrix V^T V of the
+// basis), cs[m], sn[m], g[m+1], y[m], hc[m+1] (the column's coefficients)
+struct FgSmall {
+    double *H, *Gm, *cs, *sn, *g, *y, *hc;
+};
+__device__ __forceinline__ FgSmall fg_small(const Dev& D, int s) {
+    const int m = D.fg_m;
+    double* b = D.fg_small + (long)s * D.fg_small_n;
+    FgSmall f;
+    f.H = b;
+    b += (long)(m + 1) * m;
+    f.Gm = b;
+    b += (long)(m + 1) * (m + 1);
+    f.cs = b;
+    b += m;
+    f.sn = b;
+    b += m;
+    f.g = b;
+    b += m + 1;
+    f.y = b;
+    b += m;
+    f.hc = b;
+    return f;
+}
+
+__device__ __forceinline__ bool fg_running(const Dev& D, int s) {
+    return D.dyn[s].converged == 0 && D.dyn[s].fg_state == 0;
+}
+
+__device__ __forceinline__ double warp_sum(double a) {
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+}
+
+// Sum `cnt` rows of nv partials (row stride ld) in a fixed order: thread t
+// takes value t % nv over rows q, q+Q, ... (q = t / nv, Q = 256 / nv), the
+// Q sub-sums are added in q order.  Rows of zeros at the end change nothing,
+// so a scene's sums do not depend on its slot's capacity.
+__device__ __forceinline__ void fg_sum_rows(const double* __restrict__ src, int cnt, int ld, int nv, double* out,
+                                            double* scratch /*[BS_THREADS]*/) {
+    const int t = threadIdx.x;
+    if (nv <= BS_THREADS) {
+        const int Q = BS_THREADS / nv;
+        const int i = t % nv, q = t / nv;
+        if (q < Q) {
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int b = q;
+            for (; b + 3 * Q < cnt; b += 4 * Q) {   // four loads in flight per thread
+                a0 += __ldcg(src + (long)b * ld + i);
+                a1 += __ldcg(src + (long)(b + Q) * ld + i);
+                a2 += __ldcg(src + (long)(b + 2 * Q) * ld + i);
+                a3 += __ldcg(src + (long)(b + 3 * Q) * ld + i);
+            }
+            for (; b < cnt; b += Q) a0 += __ldcg(src + (long)b * ld + i);
+            scratch[q * nv + i] = (a0 + a1) + (a2 + a3);
+        }
+        __syncthreads();
+        if (t < nv) {
+            double a = 0.0;
+            for (int k = 0; k < Q; ++k) a += scratch[k * nv + t];
+            out[t] = a;
+        }
+    } else {
+        for (int i = t; i < nv; i += BS_THREADS) {
+            double a0 = 0.0, a1 = 0.0;
+            int b = 0;
+            for (; b + 1 < cnt; b += 2) {
+                a0 += __ldcg(src + (long)b * ld + i);
+                a1 += __ldcg(src + (long)(b + 1) * ld + i);
+            }
+            if (b < cnt) a0 += __ldcg(src + (long)b * ld + i);
+            out[i] = a0 + a1;
+        }
+    }
+    __syncthreads();
+}
+
+// Two-level scene sum of nv per-block values in vals[] (shared): the last
+// block of each group of 32 row blocks sums the group, the last group of the
+// scene sums the groups into tot[] (shared); true in that block.
+__device__ __forceinline__ bool fg_scene_sum(const Dev& D, int s, int nv, const double* vals, double* tot) {
+    __shared__ double scratch[BS_THREADS];
+    __shared__ int last;
+    const ScenePar& P = D.par[s];
+    const int ld = bs::fg_part_ld(D.fg_m);
+    const int lb = blockIdx.x - P.blk0, grp = lb >> 5;
+    const int gsize = min(32, P.nblk - (grp << 5));
+    double* part = D.fg_part + (long)blockIdx.x * ld;
+    for (int i = threadIdx.x; i < nv; i += BS_THREADS) part[i] = vals[i];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(&D.fg_gdone[P.grp0 + grp], 1) == gsize - 1);
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    fg_sum_rows(D.fg_part + (long)(P.blk0 + (grp << 5)) * ld, gsize, ld, nv, tot, scratch);
+    double* gp = D.fg_gpart + (long)(P.grp0 + grp) * ld;
+    for (int i = threadIdx.x; i < nv; i += BS_THREADS) gp[i] = tot[i];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        D.fg_gdone[P.grp0 + grp] = 0;
+        last = (atomicAdd(&D.blk_done[s], 1) == ((P.nblk + 31) >> 5) - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    fg_sum_rows(D.fg_gpart + (long)P.grp0 * ld, (P.nblk + 31) >> 5, ld, nv, tot, scratch);
+    if (threadIdx.x == 0) D.blk_done[s] = 0;
+    return true;
+}
+
+// Cycle start: r = b - A x (into ss), ||r||, g = ||r|| e1.  first: every
+// scene, sets the stopping threshold (tol ||r0|| or tol ||b||).
+__global__ void k_fg_start(Dev D, int first, int* nconv) {
+    BS_PDL_ENTRY();
+    const int s = D.blk_scene[blockIdx.x];
+    if (!first && D.dyn[s].converged) return;
+    const ScenePar& P = D.par[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    double q[2] = {0.0, 0.0};
+    if (r < P.row0 + D.dyn[s].n) {
+        const double b = D.rhs[r];
+        const double rr = b - spmv_row64(D, D.p, r);
+        D.ss[r] = rr;
+        q[0] = rr * rr;
+        q[1] = b * b;
+    }
+    double tot[2];
+    if (scene_sum<2>(D, s, q, tot) && threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        const double beta = sqrt(tot[0]);
+        if (first) {
+            Y.bnorm2 = tot[1];
+            Y.iters = 0;
+            Y.outer = 0;
+            Y.converged = 0;
+            Y.breakdown = 0;
+            Y.part_tmp = P.ppe_tol * (P.stop_rule == BS_STOP_RELRES ? sqrt(tot[1]) : beta);
+        }
+        Y.rnorm2 = tot[0];
+        Y.rho_old = beta;   // norm of the vector the next column normalises
+        Y.fg_j = 0;
+        Y.fg_k = 0;
+        fg_small(D, s).g[0] = beta;
+        bool conv = tot[1] == 0.0 || beta <= Y.part_tmp;
+        if (!isfinite(tot[0])) {
+            conv = true;
+            set_err(D, s, BS_ERR_NONFINITE);
+        }
+        if (conv) {
+            Y.fg_state = 2;
+            Y.converged = 1;
+            atomicAdd(nconv, 1);
+            atomicAdd(nconv + 1, 1);
+        } else {
+            Y.fg_state = 0;
+            Y.outer += 1;   // cycles
+        }
+    }
+}
+
+// v_j = pending / its norm (into V), plus the V-cycle input (mgmode 1: FP64, 2: FP32)
+__global__ void k_fg_put(Dev D, int mgmode) {
+    BS_PDL_ENTRY();
+    const int s = D.blk_scene[blockIdx.x];
+    if (!fg_running(D, s)) return;
+    const SceneDyn& Y = D.dyn[s];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + Y.n) return;
+    const double v = D.ss[r] / Y.rho_old;
+    D.fg_V[(long)Y.fg_j * D.fg_ld + r] = v;
+    if (mgmode == 1) bs::mg_put_input<double>(D, r, v);
+    else if (mgmode == 2) bs::mg_put_input<float>(D, r, v);
+}
+
+// Column j, pass 1: w = A z_j (z_j = the V-cycle output in sp2, kept as Z_j;
+// or v_j) into sv; one read of v_0..v_j gives h = V^T w and the Gram column
+// c = V^T v_j.  Finisher: Gm(:,j) = c, then the column's coefficients
+// hc = (2I - Gm) h -- classical Gram-Schmidt applied twice,
+// (I - V V^T)^2 = I - V (2I - V^T V) V^T, with the second projection
+// taken from the Gram matrix instead of a second pass over V.
+__global__ void k_fg_arn1(Dev D, int precond) {
+    BS_PDL_ENTRY();
+    const int s = D.blk_scene[blockIdx.x];
+    if (!fg_running(D, s)) return;
+    __shared__ double ws[BS_THREADS], vs[BS_THREADS];
+    __shared__ double dsh[2 * (BS_FG_MAXM + 1)];
+    __shared__ double tsh[2 * (BS_FG_MAXM + 1)];
+    const int j = D.dyn[s].fg_j, nv = j + 1;
+    const int rend = D.par[s].row0 + D.dyn[s].n;
+    const long r0 = (long)blockIdx.x * BS_THREADS;
+    const int r = (int)r0 + threadIdx.x;
+    const long col = (long)j * D.fg_ld;
+    const double* u = precond ? D.sp2 : D.fg_V + col;
+    double w = 0.0, vj = 0.0;
+    if (r < rend) {
+        w = spmv_row64(D, u, r);
+        D.sv[r] = w;
+        vj = D.fg_V[col + r];
+        if (precond) D.fg_Z[col + r] = D.sp2[r];
+    }
+    ws[threadIdx.x] = w;
+    vs[threadIdx.x] = vj;
+    __syncthreads();
+    // Warp w takes basis vectors w + 8 (4g + u), u = 0..3: lanes across the
+    // block's rows (coalesced), 8 values per lane (4 vectors x 2 dots), summed
+    // over the lanes by a transposing butterfly -- 9 FP64 adds per lane for
+    // the 8 values rather than 5 per value (the FP64 pipe bounds this pass)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    for (int base = warp; base < nv; base += 4 * (BS_THREADS / 32)) {
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = base + (BS_THREADS / 32) * u;
+            double a = 0.0, c = 0.0;
+            if (i < nv) {
+                const double* v = D.fg_V + (long)i * D.fg_ld + r0;
+#pragma unroll
+                for (int k = 0; k < BS_THREADS / 32; ++k) {
+                    const int t = lane + 32 * k;
+                    const double vi = (r0 + t < rend) ? v[t] : 0.0;
+                    a += vi * ws[t];
+                    c += vi * vs[t];
+                }
+            }
+            x[2 * u] = a;
+            x[2 * u + 1] = c;
+        }
+        double y[4], z[2];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            y[k] = (b4 ? x[k + 4] : x[k]) + __shfl_xor_sync(0xffffffffu, b4 ? x[k] : x[k + 4], 16);
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+            z[k] = (b3 ? y[k + 2] : y[k]) + __shfl_xor_sync(0xffffffffu, b3 ? y[k] : y[k + 2], 8);
+        double tv = (b2 ? z[1] : z[0]) + __shfl_xor_sync(0xffffffffu, b2 ? z[0] : z[1], 4);
+        tv += __shfl_xor_sync(0xffffffffu, tv, 2);
+        tv += __shfl_xor_sync(0xffffffffu, tv, 1);
+        if ((lane & 3) == 0) {   // lane holds value q = lane / 4 = 2u + dot
+            const int q = lane >> 2;
+            const int i = base + (BS_THREADS / 32) * (q >> 1);
+            if (i < nv) dsh[(q & 1) ? nv + i : i] = tv;
+        }
+    }
+    __syncthreads();
+    if (!fg_scene_sum(D, s, 2 * nv, dsh, tsh)) return;
+    const FgSmall f = fg_small(D, s);
+    const int ldg = D.fg_m + 1;
+    for (int i = threadIdx.x; i < nv; i += BS_THREADS) {
+        f.Gm[i + (long)j * ldg] = tsh[nv + i];
+        f.Gm[j + (long)i * ldg] = tsh[nv + i];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += BS_THREADS) {
+        double acc = 2.0 * tsh[i];
+        for (int k = 0; k < nv; ++k) acc -= __ldcg(f.Gm + i + (long)k * ldg) * tsh[k];
+        f.hc[i] = acc;
+        f.H[i + (long)j * ldg] = acc;
+    }
+}
+
+// Column j, pass 2: w -= V hc (the pending vector, into ss), h_{j+1,j} = ||w||;
+// finisher: rotations, residual estimate, cycle end
+__global__ void k_fg_arn2(Dev D, int* nconv) {
+    BS_PDL_ENTRY();
+    const int s = D.blk_scene[blockIdx.x];
+    if (!fg_running(D, s)) return;
+    __shared__ double hs[BS_FG_MAXM + 1];
+    const ScenePar& P = D.par[s];
+    const int j = D.dyn[s].fg_j;
+    const int rend = P.row0 + D.dyn[s].n;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const FgSmall f = fg_small(D, s);
+    for (int i = threadIdx.x; i <= j; i += BS_THREADS) hs[i] = f.hc[i];
+    __syncthreads();
+    double q[1] = {0.0};
+    if (r < rend) {
+        double w = D.sv[r];
+        const double* v = D.fg_V + r;
+        int i = 0;
+        for (; i + 4 <= j + 1; i += 4) {   // four loads in flight
+            const double v0 = v[(long)i * D.fg_ld], v1 = v[(long)(i + 1) * D.fg_ld];
+            const double v2 = v[(long)(i + 2) * D.fg_ld], v3 = v[(long)(i + 3) * D.fg_ld];
+            w -= hs[i] * v0;
+            w -= hs[i + 1] * v1;
+            w -= hs[i + 2] * v2;
+            w -= hs[i + 3] * v3;
+        }
+        for (; i <= j; ++i) w -= hs[i] * v[(long)i * D.fg_ld];
+        D.ss[r] = w;
+        q[0] = w * w;
+    }
+    double tot[1];
+    if (!scene_sum<1>(D, s, q, tot)) return;
+    // finisher: the column and the rotations staged in shared memory, the
+    // rotation sweep (a dependent chain) run there by one thread
+    __shared__ double hcol[BS_FG_MAXM + 2], csh[BS_FG_MAXM], snh[BS_FG_MAXM];
+    const int m = D.fg_m;
+    double* h = f.H + (long)j * (m + 1);
+    for (int i = threadIdx.x; i <= j; i += BS_THREADS) hcol[i] = h[i];
+    for (int i = threadIdx.x; i < j; i += BS_THREADS) {
+        csh[i] = f.cs[i];
+        snh[i] = f.sn[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        const double hn = sqrt(tot[0]);
+        double hi = hcol[0];
+        for (int i = 0; i < j; ++i) {   // earlier rotations on the new column
+            const double b = hcol[i + 1];
+            hcol[i] = csh[i] * hi + snh[i] * b;
+            hi = -snh[i] * hi + csh[i] * b;
+        }
+        const double a = hi;
+        const double den = sqrt(a * a + hn * hn);
+        const double c = den > 0.0 ? a / den : 1.0, sn = den > 0.0 ? hn / den : 0.0;
+        f.cs[j] = c;
+        f.sn[j] = sn;
+        hcol[j] = den;
+        hcol[j + 1] = 0.0;
+        const double gj = f.g[j];
+        f.g[j] = c * gj;
+        f.g[j + 1] = -sn * gj;
+        const double res = fabs(f.g[j + 1]);
+        Y.rnorm2 = res * res;
+        Y.rho_old = hn;
+        Y.iters += 1;
+        Y.fg_j = j + 1;
+        int st = 0;
+        if (!isfinite(res) || !isfinite(hn)) {
+            st = 3;
+            set_err(D, s, BS_ERR_NONFINITE);
+        } else if (res <= Y.part_tmp || hn <= 1e-12) {
+            st = 2;
+        } else if (Y.iters >= P.maxit) {
+            st = 3;
+        } else if (j + 1 == m) {
+            st = 1;
+        }
+        Y.fg_state = st;
+        if (st) atomicAdd(nconv, 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j + 1; i += BS_THREADS) h[i] = hcol[i];
+}
+
+// One warp per scene: y = R^-1 g over the cycle's k columns; scenes that
+// converged (or met the cap) in this cycle are marked done
+__global__ void k_fg_solve(Dev D, int* nconv) {
+    BS_PDL_ENTRY();
+    const int s = blockIdx.x, lane = threadIdx.x;
+    SceneDyn& Y = D.dyn[s];
+    if (Y.converged) {
+        if (lane == 0) Y.fg_k = 0;
+        return;
+    }
+    __shared__ double ys[BS_FG_MAXM];
+    const int k = Y.fg_j;
+    const int ld = D.fg_m + 1;
+    const FgSmall f = fg_small(D, s);
+    for (int i = k - 1; i >= 0; --i) {
+        double acc = 0.0;
+        for (int l = i + 1 + lane; l < k; l += 32) acc += f.H[i + (long)l * ld] * ys[l];
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            const double d = f.H[i + (long)i * ld];
+            ys[i] = d != 0.0 ? (f.g[i] - acc) / d : 0.0;
+        }
+        __syncwarp();
+    }
+    for (int i = lane; i < k; i += 32) f.y[i] = ys[i];
+    if (lane == 0) {
+        Y.fg_k = k;
+        if (Y.fg_state >= 2) {
+            if (Y.fg_state == 3) set_err(D, s, BS_ERR_NOT_CONVERGED);
+            Y.converged = 1;
+            atomicAdd(nconv + 1, 1);
+        }
+    }
+}
+
+// x += Z y over the cycle's columns
+__global__ void k_fg_update(Dev D, int precond) {
+    BS_PDL_ENTRY();
+    const int s = D.blk_scene[blockIdx.x];
+    const int k = D.dyn[s].fg_k;
+    if (k == 0) return;
+    __shared__ double ys[BS_FG_MAXM];
+    const FgSmall f = fg_small(D, s);
+    for (int i = threadIdx.x; i < k; i += BS_THREADS) ys[i] = f.y[i];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const double* z = (precond ? D.fg_Z : D.fg_V) + r;
+    double dx = 0.0;
+    for (int i = 0; i < k; ++i) dx += ys[i] * z[(long)i * D.fg_ld];
+    D.p[r] += dx;
+}
+
 }  // namespace
 
 namespace bs {
@@ -560,8 +979,8 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
     // while per-kernel events are on
     IterGraph* G = L.graph;
     bool use_graph = G && !(L.timer && L.timer->mask);
-    if (use_graph && !(G->valid && G->precond == precond && G->prec == mg_prec && G->chunk == check_every &&
-                       std::memcmp(&G->key, &D, sizeof(Dev)) == 0)) {
+    if (use_graph && !(G->valid && G->solver == BS_SOLVER_BICGSTAB && G->precond == precond && G->prec == mg_prec &&
+                       G->chunk == check_every && std::memcmp(&G->key, &D, sizeof(Dev)) == 0)) {
         if (G->exec) cudaGraphExecDestroy(G->exec);
         G->exec = nullptr;
         G->valid = false;
@@ -573,6 +992,7 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
                 cudaGraphInstantiate(&G->exec, gr, 0) == cudaSuccess) {
                 G->valid = true;
                 G->key = D;
+                G->solver = BS_SOLVER_BICGSTAB;
                 G->precond = precond;
                 G->prec = mg_prec;
                 G->chunk = check_every;
@@ -598,6 +1018,99 @@ void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int p
         cudaEventSynchronize(ev);
         timer_collect(L.timer, false);
         if (*h_nconv >= D.nscene) break;
+    }
+    q = tbegin(L, K_TRUERES);
+    launch_pdl(L, k_true_res64, L.nblk_rows, BS_THREADS, 0, D);
+    tend(L, q);
+}
+
+// Host driver of FGMRES: per restart cycle one start kernel and a host read
+// of the converged count, then chunks of `check_every` columns (captured as
+// one CUDA graph) until every scene's cycle has ended, then the small
+// triangular solves and the update.  d_nconv[0] counts scenes whose cycle
+// ended, d_nconv[1] converged scenes.
+void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
+                  int* d_nconv, int* h_nconv, cudaEvent_t ev) {
+    int q;
+    if (precond) {
+        if (mg_prec == BS_PREC_MIXED) {
+            q = tbegin(L, K_MX_CONV);
+            launch_pdl(L, k_mx_convert, L.nblk_rows, BS_THREADS, 0, D);
+            tend(L, q);
+        }
+        mg_setup(D, L, mg_prec);
+    }
+    const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
+    auto column = [&]() {
+        int q2 = tbegin(L, K_FG_PUT);
+        launch_pdl(L, k_fg_put, L.nblk_rows, BS_THREADS, 0, D, mgmode);
+        tend(L, q2);
+        if (precond) mg_apply(D, L, mg_prec, D.fg_V, D.sp2);
+        q2 = tbegin(L, K_FG_ARN);
+        launch_pdl(L, k_fg_arn1, L.nblk_rows, BS_THREADS, 0, D, precond);
+        tend(L, q2);
+        q2 = tbegin(L, K_FG_ORTH);
+        launch_pdl(L, k_fg_arn2, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
+        tend(L, q2);
+    };
+    IterGraph* G = L.graph;
+    bool use_graph = G && !(L.timer && L.timer->mask);
+    if (use_graph && !(G->valid && G->solver == BS_SOLVER_FGMRES && G->precond == precond && G->prec == mg_prec &&
+                       G->chunk == check_every && std::memcmp(&G->key, &D, sizeof(Dev)) == 0)) {
+        if (G->exec) cudaGraphExecDestroy(G->exec);
+        G->exec = nullptr;
+        G->valid = false;
+        const int64_t before = *L.launches;
+        cudaGraph_t gr = nullptr;
+        if (cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            for (int c = 0; c < check_every; ++c) column();
+            if (cudaStreamEndCapture(L.stream, &gr) == cudaSuccess && gr &&
+                cudaGraphInstantiate(&G->exec, gr, 0) == cudaSuccess) {
+                G->valid = true;
+                G->key = D;
+                G->solver = BS_SOLVER_FGMRES;
+                G->precond = precond;
+                G->prec = mg_prec;
+                G->chunk = check_every;
+                G->nkernels = *L.launches - before;
+            }
+            if (gr) cudaGraphDestroy(gr);
+        }
+        *L.launches = before;
+        cudaGetLastError();
+        use_graph = G->valid;
+    }
+    cudaMemsetAsync(d_nconv, 0, 2 * sizeof(int), L.stream);
+    // every cycle does at least one column of each scene it starts, and the
+    // column kernels stop a scene at maxit columns
+    for (int cycle = 0; cycle <= maxit; ++cycle) {
+        cudaMemcpyAsync(d_nconv, d_nconv + 1, sizeof(int), cudaMemcpyDeviceToDevice, L.stream);
+        q = tbegin(L, K_FG_START);
+        launch_pdl(L, k_fg_start, L.nblk_rows, BS_THREADS, 0, D, cycle == 0 ? 1 : 0, d_nconv);
+        tend(L, q);
+        cudaMemcpyAsync(h_nconv, d_nconv, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+        cudaStreamSynchronize(L.stream);
+        timer_collect(L.timer, false);
+        if (h_nconv[1] >= D.nscene) break;
+        int it = 0;
+        while (it < D.fg_m) {
+            cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+            cudaEventRecord(ev, L.stream);
+            if (use_graph) {
+                cudaGraphLaunch(G->exec, L.stream);
+                *L.launches += G->nkernels;
+                it += check_every;
+            } else {
+                for (int c = 0; c < check_every && it < D.fg_m; ++c, ++it) column();
+            }
+            cudaEventSynchronize(ev);
+            timer_collect(L.timer, false);
+            if (*h_nconv >= D.nscene) break;
+        }
+        q = tbegin(L, K_FG_UPD);
+        launch_pdl(L, k_fg_solve, D.nscene, 32, 0, D, d_nconv);
+        launch_pdl(L, k_fg_update, L.nblk_rows, BS_THREADS, 0, D, precond);
+        tend(L, q);
     }
     q = tbegin(L, K_TRUERES);
     launch_pdl(L, k_true_res64, L.nblk_rows, BS_THREADS, 0, D);

@@ -67,6 +67,11 @@ extern "C" {
 /* PPE stopping rules */
 #define BS_STOP_RELRES     0  /* ||b - A x||_2 / ||b||_2 <= ppe_tol                    */
 #define BS_STOP_REFERENCE  1  /* every |dx_i/(x_i+1e-5)| <= 1e-2 (solver.f90:233-242)  */
+#define BS_STOP_R0         2  /* ||b - A x||_2 / ||b - A x0||_2 <= ppe_tol: the relative-to-initial-
+                                 residual test of the reference's FGMRES (dpar(1), solver.f90:324) */
+
+#define BS_SOLVER_BICGSTAB 0  /* bicgstab, solver.f90:129-254                          */
+#define BS_SOLVER_FGMRES   1  /* fgmres, solver.f90:306-350: restarted flexible GMRES   */
 
 /*
  * Scene parameters.  Defaults and formulas follow initialize.f90:21-81 and
@@ -134,6 +139,14 @@ typedef struct bs_params {
      * counterpart) */
     int32_t wc_form;
     int32_t wc_pad;
+    /* PPE Krylov method (BS_SOLVER_*) and the FGMRES restart length (1..150;
+     * the reference's MKL call keeps MKL's default, 150).  Context-wide, taken
+     * from scene 0 like ppe_precond.  FGMRES stops on ppe_stop =
+     * BS_STOP_RELRES (||r||/||b||) or BS_STOP_R0 (||r||/||r0||, the
+     * reference's rule; BS_STOP_REFERENCE is read as BS_STOP_R0 there), with
+     * ppe_maxit counting Arnoldi columns over all restart cycles */
+    int32_t ppe_solver;
+    int32_t ppe_restart;
 } bs_params;
 
 /*
@@ -279,6 +292,15 @@ int bs_wcsph_step(struct bs_ctx* ctx, int32_t nsteps);
 int bs_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
                     const double* b, double* x, double tol, int32_t maxit, int32_t stop_rule,
                     int32_t* iters, double* relres);
+
+/* Standalone restarted FGMRES on a CSR system: the Krylov method of the
+ * reference's live PPE solve (fgmres, solver.f90:306-350, which calls MKL's
+ * dfgmres with the spmv2 operator), unpreconditioned as there.  restart in
+ * 1..150, maxit counts Arnoldi columns, stop_rule BS_STOP_RELRES or
+ * BS_STOP_R0.  Host arrays, 0-based row_ptr/col. */
+int bs_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                  const double* b, double* x, double tol, int32_t maxit, int32_t restart,
+                  int32_t stop_rule, int32_t* iters, double* relres);
 
 /* No counterpart in the reference.  The same BiCGStab as bs_bicgstab_csr, but
  * on a CSR system already in device memory (0-based d_row_ptr[n+1], d_col,

@@ -795,6 +795,83 @@ int bicgstab(int n, Op spmv, const std::vector<double>& b, std::vector<double>& 
     return status;
 }
 
+// fgmres, solver.f90:306-350: the reference hands the system to MKL's RCI
+// dfgmres (Intel oneMKL, closed and absent; no preconditioner, ipar(11) = 0)
+// with the relative tolerance dpar(1) on the residual over the initial
+// residual (ipar(9) = 1), the zero-norm check of the new Krylov vector
+// (ipar(12) = 1, threshold dpar(8) = 1e-12) and the default restart / maximum
+// of 150 columns.  Restated from the published algorithm: restarted GMRES
+// (Saad & Schultz 1986; flexible form Saad 1993, identical without a
+// preconditioner), Arnoldi by modified Gram-Schmidt, Givens rotations on
+// the Hessenberg matrix.  rule 0: ||r|| <= tol ||b||; otherwise ||r|| <= tol
+// ||r0||.  Returns 1 when maxit columns ran out first.
+template <class Op>
+int fgmres(int n, Op spmv, const std::vector<double>& b, std::vector<double>& x, double tol, int maxit, int m,
+           int rule, int* iters, double* relres) {
+    std::vector<double> r(n), w(n);
+    std::vector<std::vector<double>> V(m + 1, std::vector<double>(n));
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    auto h = [&](int i, int j) -> double& { return H[(size_t)j * (m + 1) + i]; };
+    auto residual = [&]() {
+        spmv(x, w);
+        for (int k = 0; k < n; ++k) r[k] = b[k] - w[k];
+        return std::sqrt(vecvec(r, r));
+    };
+    const double bnorm = std::sqrt(vecvec(b, b));
+    double beta = residual();
+    const double ref = tol * (rule == 0 ? bnorm : beta);
+    int it = 0, status = 0;
+    bool conv = bnorm == 0.0 || beta <= ref;
+    while (!conv && status == 0) {
+        for (int k = 0; k < n; ++k) V[0][k] = r[k] / beta;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int kcol = 0;
+        for (int j = 0; j < m; ++j) {
+            spmv(V[j], w);
+            for (int i = 0; i <= j; ++i) {
+                h(i, j) = vecvec(w, V[i]);
+                for (int k = 0; k < n; ++k) w[k] -= h(i, j) * V[i][k];
+            }
+            const double hn = std::sqrt(vecvec(w, w));
+            for (int i = 0; i < j; ++i) {
+                const double a = h(i, j), c = h(i + 1, j);
+                h(i, j) = cs[i] * a + sn[i] * c;
+                h(i + 1, j) = -sn[i] * a + cs[i] * c;
+            }
+            const double a = h(j, j), den = std::sqrt(a * a + hn * hn);
+            cs[j] = den > 0.0 ? a / den : 1.0;
+            sn[j] = den > 0.0 ? hn / den : 0.0;
+            h(j, j) = den;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++it;
+            kcol = j + 1;
+            const double res = std::fabs(g[j + 1]);
+            if (!std::isfinite(res)) { status = 1; break; }
+            if (res <= ref || hn <= 1e-12) { conv = true; break; }
+            if (it >= maxit) { status = 1; break; }
+            if (j + 1 < m)
+                for (int k = 0; k < n; ++k) V[j + 1][k] = w[k] / hn;
+        }
+        for (int i = kcol - 1; i >= 0; --i) {
+            double acc = 0.0;
+            for (int l = i + 1; l < kcol; ++l) acc += h(i, l) * y[l];
+            y[i] = h(i, i) != 0.0 ? (g[i] - acc) / h(i, i) : 0.0;
+        }
+        for (int i = 0; i < kcol; ++i)
+            for (int k = 0; k < n; ++k) x[k] += y[i] * V[i][k];
+        if (conv || status) break;
+        beta = residual();
+        conv = beta <= ref;
+        if (!std::isfinite(beta)) status = 1;
+    }
+    const double rt = residual();
+    *iters = it;
+    *relres = bnorm > 0 ? rt / bnorm : rt;
+    return status;
+}
+
 int ppe_solve(or_scene* s, double tol, int maxit, int rule, int* iters, double* relres) {
     const int n = s->nrows;
     // warm start: each particle's current pressure at its row
@@ -1494,6 +1571,52 @@ int or_stage(or_scene* s, int32_t stage) {
         default: return BS_E_ARG;
     }
     return 0;
+}
+
+int or_ppe_fgmres(or_scene* s, double tol, int32_t maxit, int32_t restart, int32_t rule, int32_t* iters,
+                  double* relres) {
+    if (!s->assembled) return BS_E_STATE;
+    if (restart < 1) return BS_E_ARG;
+    const int n = s->nrows;
+    s->fsol.assign(n, 0.0);   // warm start, as ppe_solve
+    for (auto& c : s->cells)
+        for (int k = 0; k < c.ptot; ++k) s->fsol[c.plist[k].matid - 1] = c.plist[k].pressure;
+    int it = 0;
+    double rr = 0;
+    const int st = fgmres(
+        n, [&](const std::vector<double>& b, std::vector<double>& r) { spmv2(s, b, r); }, s->fvec, s->fsol, tol,
+        maxit, restart, rule, &it, &rr);
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) c.plist[k].pressure = s->fsol[c.plist[k].matid - 1];
+    });
+    s->last_iters = it;
+    s->last_relres = rr;
+    if (st) s->err |= BS_ERR_NOT_CONVERGED;
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st ? BS_E_NOTCONV : 0;
+}
+
+int or_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val, const double* b,
+                  double* x, double tol, int32_t maxit, int32_t restart, int32_t rule, int32_t* iters,
+                  double* relres) {
+    if (n <= 0 || restart < 1) return BS_E_ARG;
+    auto spmv = [&](const std::vector<double>& v, std::vector<double>& r) {
+        for (int is = 0; is < n; ++is) {
+            double comp = 0.0;
+            for (int js = row_ptr[is]; js < row_ptr[is + 1]; ++js) comp = comp + val[js] * v[col[js]];
+            r[is] = comp;
+        }
+    };
+    std::vector<double> bb(b, b + n), sl(x, x + n);
+    int it = 0;
+    double rr = 0;
+    const int st = fgmres(n, spmv, bb, sl, tol, maxit, restart, rule, &it, &rr);
+    for (int k = 0; k < n; ++k) x[k] = sl[k];
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st ? BS_E_NOTCONV : 0;
 }
 
 int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule, int32_t* iters, double* relres) {

@@ -47,6 +47,12 @@ int or_matrix(or_scene* s, int32_t kmax, double* diag, double* off, double* rhs)
 int or_stage(or_scene* s, int32_t stage);
 int or_ppe_solve(or_scene* s, double tol, int32_t maxit, int32_t rule,
                  int32_t* iters, double* relres);
+/* fgmres, solver.f90:306-350: restarted GMRES (rule 0: ||r||/||b||, else ||r||/||r0||) */
+int or_ppe_fgmres(or_scene* s, double tol, int32_t maxit, int32_t restart, int32_t rule,
+                  int32_t* iters, double* relres);
+int or_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                  const double* b, double* x, double tol, int32_t maxit, int32_t restart,
+                  int32_t rule, int32_t* iters, double* relres);
 int or_step(or_scene* s, int32_t nsteps);
 int or_wcsph_step(or_scene* s, int32_t nsteps);
 /* combined, output.f90:188-222 (fluid / buffer text files) */

@@ -63,6 +63,9 @@ def lib():
         L.or_write_combined.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.or_set_pressure.argtypes = [vp, vp]
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_ppe_fgmres.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32, vp, vp]
+        L.or_fgmres_csr.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_int32, C.c_int32,
+                                    C.c_int32, vp, vp]
         L.or_bicgstab_csr.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_int32,
                                       C.c_int32, vp, vp]
         L.or_Wab.restype = C.c_double
@@ -152,6 +155,12 @@ class Oracle:
         rc = lib().or_ppe_solve(self.h, tol, maxit, rule, C.byref(it), C.byref(rr))
         return rc, it.value, rr.value
 
+    def ppe_fgmres(self, tol, maxit=150, restart=150, rule=2):
+        it = C.c_int32(0)
+        rr = C.c_double(0)
+        rc = lib().or_ppe_fgmres(self.h, tol, maxit, restart, rule, C.byref(it), C.byref(rr))
+        return rc, it.value, rr.value
+
     def step(self, n=1):
         lib().or_step(self.h, n)
 
@@ -181,6 +190,19 @@ def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=0):
     rr = C.c_double(0)
     rc = lib().or_bicgstab_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data,
                                b.ctypes.data, x.ctypes.data, tol, maxit, rule, C.byref(it), C.byref(rr))
+    return rc, x, it.value, rr.value
+
+
+def fgmres_csr(row_ptr, col, val, b, x0, tol=1e-3, maxit=150, restart=150, rule=2):
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    it = C.c_int32(0)
+    rr = C.c_double(0)
+    rc = lib().or_fgmres_csr(len(b), row_ptr.ctypes.data, col.ctypes.data, val.ctypes.data, b.ctypes.data,
+                             x.ctypes.data, tol, maxit, restart, rule, C.byref(it), C.byref(rr))
     return rc, x, it.value, rr.value
 
 

@@ -208,3 +208,98 @@ def test_ghost_row_leftover_entry_oracle(oracle):
     for r in q:
         j0 = idx[r, 0]
         assert s["tid"][r] == 2 and s["tid"][j0] == 3 and j0 < r
+
+
+# ---------------------------------------------------------------- FGMRES
+# fgmres (solver.f90:306-350) hands the system to MKL's dfgmres, which is
+# closed and absent; the oracle restates restarted GMRES.  Pins: the 5x5
+# known answer, and the defining property of the method -- after k columns
+# of a cycle the iterate minimises ||b - A x|| over x0 + K_k(A, r0) -- checked
+# against a dense least-squares solve, cycle by cycle across a restart.
+
+def _nonsym(n, seed):
+    rng = np.random.default_rng(seed)
+    A = np.eye(n) * 4.0 + rng.standard_normal((n, n)) * (0.6 / np.sqrt(n))
+    return A, rng.standard_normal(n)
+
+
+def _csr(A):
+    rows, cols = np.nonzero(A)
+    ptr = np.zeros(A.shape[0] + 1, np.int64)
+    np.add.at(ptr, rows + 1, 1)
+    return np.cumsum(ptr), cols, A[rows, cols]
+
+
+def _krylov_min(A, b, x0, k):
+    r0 = b - A @ x0
+    K = np.empty((len(b), k))
+    v = r0 / np.linalg.norm(r0)
+    for j in range(k):
+        K[:, j] = v
+        v = A @ v
+        v = v / np.linalg.norm(v)
+    Q, _ = np.linalg.qr(K)
+    y, *_ = np.linalg.lstsq(A @ Q, r0, rcond=None)
+    return x0 + Q @ y
+
+
+def test_fgmres_known_answer(oracle):
+    rc, x, it, rr = oracle.fgmres_csr(KAT_ROW, KAT_COL, KAT_VAL, KAT_B, np.ones(5), tol=1e-13, maxit=20,
+                                      restart=5, rule=0)
+    assert rc == 0 and it <= 5
+    np.testing.assert_allclose(x, KAT_X, rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("k", [1, 3, 6])
+def test_fgmres_iterate_minimises_over_krylov_space(oracle, k):
+    A, b = _nonsym(40, 3)
+    ptr, col, val = _csr(A)
+    x0 = np.full(40, 0.25)
+    rc, x, it, rr = oracle.fgmres_csr(ptr, col, val, b, x0, tol=1e-300, maxit=k, restart=20, rule=0)
+    assert it == k and rc != 0   # stopped by the column cap
+    np.testing.assert_allclose(x, _krylov_min(A, b, x0, k), rtol=1e-10, atol=1e-12)
+
+
+def test_fgmres_restart_cycles(oracle):
+    A, b = _nonsym(40, 4)
+    ptr, col, val = _csr(A)
+    x0 = np.zeros(40)
+    rc, x, it, rr = oracle.fgmres_csr(ptr, col, val, b, x0, tol=1e-300, maxit=7, restart=4, rule=0)
+    assert it == 7
+    x1 = _krylov_min(A, b, x0, 4)          # first cycle: 4 columns
+    np.testing.assert_allclose(x, _krylov_min(A, b, x1, 3), rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("rule,tol", [(0, 1e-9), (2, 1e-3)])
+def test_fgmres_stopping_rules(oracle, rule, tol):
+    A, b = _nonsym(60, 5)
+    ptr, col, val = _csr(A)
+    x0 = np.ones(60)
+    r0 = np.linalg.norm(b - A @ x0)
+    rc, x, it, rr = oracle.fgmres_csr(ptr, col, val, b, x0, tol=tol, maxit=200, restart=150, rule=rule)
+    assert rc == 0
+    ref = tol * (np.linalg.norm(b) if rule == 0 else r0)
+    res = np.linalg.norm(b - A @ x)
+    assert res <= ref * (1 + 1e-6)
+    # one column fewer does not meet the rule (the stop is the first column that does)
+    rc2, x2, it2, _ = oracle.fgmres_csr(ptr, col, val, b, x0, tol=tol, maxit=it - 1, restart=150, rule=rule)
+    assert rc2 != 0 and np.linalg.norm(b - A @ x2) > ref
+
+
+def test_fgmres_scene_solve(oracle):
+    """The reference's live PPE settings on a small beach scene (R0 rule,
+    1e-3, restart and cap 150), from the warm start; the result agrees with
+    a tight BiCGStab solve to the accuracy the rule implies."""
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.04)
+    a = oracle.Oracle(p, st, gr)
+    b = oracle.Oracle(p, st, gr)
+    for o in (a, b):
+        for name in ("neighbour", "effpor", "int_vel", "ppe_assemble"):
+            o.stage(name)
+    rc, it, rr = a.ppe_fgmres(1e-3, maxit=150, restart=150, rule=2)
+    assert rc == 0 and 0 < it <= 150
+    rc2, it2, rr2 = b.ppe_solve(1e-12, maxit=20000)
+    assert rc2 == 0
+    pa, pb = a.get()["p"], b.get()["p"]
+    assert np.linalg.norm(pa - pb) / np.linalg.norm(pb) < 0.05
