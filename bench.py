@@ -145,25 +145,44 @@ def peaks():
 # ------------------------------------------------------------- our arm
 # Kernels bracketed by CUDA events during the timed region (the candidates for
 # the dominant kernel).
-TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down", "mg_l0_up")
+TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down", "mg_l0_up",
+                 "fg_arnoldi_spmv", "fg_project")
 # DRAM bytes per launch measured by ncu over the algorithmic bytes of the same
 # launch (0.18 M-particle beach, mixed; profiles/*_beach_dx0.0025_mixed.md);
 # the traffic grows with the nonzeros and rows, so the ratio scales it to the
 # bench's workload.  k_it2_64 has k_it1_64's access pattern.
 TRAFFIC_RATIO = {"search_effpor": 0.46, "bicg_it1_spmv": 0.99, "bicg_it2_spmv": 0.99,
-                 "mg_l0_down": 0.98, "mg_l0_up": 0.93}
+                 "mg_l0_down": 0.98, "mg_l0_up": 0.93, "fg_arnoldi_spmv": 0.99, "fg_project": 0.97}
 
 
-def algorithmic_bytes(ctx, kernel, precision):
+def fg_columns(iters, restart):
+    """Sum over the Arnoldi columns of one FGMRES solve of (j+1), the basis
+    vectors column j reads (cycles of `restart` columns)."""
+    tot, left = 0, int(iters)
+    while left > 0:
+        k = min(left, restart)
+        tot += k * (k + 1) // 2
+        left -= k
+    return tot
+
+
+def algorithmic_bytes(ctx, kernel, precision, basis_reads=None):
     """Compulsory HBM bytes of one launch over all scenes (neighbour-vector
     gathers counted as on-chip hits; every other operand read or written once).
-    w = width of the per-pair and matrix values (8 FP64, 4 mixed)."""
+    w = width of the per-pair and matrix values (8 FP64, 4 mixed).  For the
+    FGMRES column kernels, basis_reads = the mean number of basis vectors a
+    launch reads (j+1 at column j)."""
     w = 4 if precision == "mixed" else 8
     tot = 0.0
     for s in range(ctx.nscenes):
         c = ctx.neighbour_counts(s)
         nnz, n = float(c.sum()), float(len(c))
-        if kernel in ("bicg_it1_spmv", "bicg_it2_spmv"):
+        if kernel == "fg_arnoldi_spmv":
+            # SpMV (FP64 values + index; diag, count, input, output) + v_j + Z_j write + basis reads
+            tot += nnz * (8 + 4) + n * (8 + 4 + 8 + 8) + n * (8 + 8) + basis_reads * n * 8
+        elif kernel == "fg_project":
+            tot += n * (8 + 8) + basis_reads * n * 8
+        elif kernel in ("bicg_it1_spmv", "bicg_it2_spmv"):
             # values (FP64) + column index per nonzero; diag, count, input, output, dot operand per row
             tot += nnz * (8 + 4) + n * (8 + 4 + 8 + 8 + 8)
         elif kernel == "mg_l0_down":
@@ -175,6 +194,22 @@ def algorithmic_bytes(ctx, kernel, precision):
             # coff, gradvx, flags, count; effpor reads/writes
             tot += n * (16 + 8 + 2 + 4) + nnz * (4 + 4 * w) + n * (32 + 8 + 1 + 4) + n * (32 + 40)
     return tot
+
+
+def fp64_flops(ctx, kernel, basis_reads):
+    """Algorithmic FP64 operations of one launch (FMA = 2) for the FGMRES
+    column kernels, whose FP64 work per byte is above the FP64/HBM ratio of
+    the part: SpMV (diagonal + nonzeros), two dots per basis vector (pass 1),
+    one update per basis vector and the norm (pass 2)."""
+    tot = 0.0
+    for s in range(ctx.nscenes):
+        c = ctx.neighbour_counts(s)
+        nnz, n = float(c.sum()), float(len(c))
+        if kernel == "fg_arnoldi_spmv":
+            tot += 2 * nnz + 2 * n + 4 * basis_reads * n
+        elif kernel == "fg_project":
+            tot += 2 * basis_reads * n + 2 * n
+    return tot or None
 
 
 def run_ours(args, D):
@@ -204,11 +239,18 @@ def run_ours(args, D):
     # of the candidate kernels (graphs are off while events are on): the
     # per-launch durations of the roofline
     ids = ctx.kernel_ids()
-    ctx.kernel_timing(sum(1 << ids[k] for k in TIMED_KERNELS))
-    ctx.record(2)
-    ctx.step(args.steps)
-    ctx.record(3)
-    ms_timed = ctx.elapsed_ms(2, 3)
+    ctx.kernel_timing(sum(1 << ids[k] for k in TIMED_KERNELS if k in ids))
+    ms_timed, fg_reads, fg_launches = 0.0, 0, 0
+    restart = int(ctx.get_option("ppe_restart"))
+    for _ in range(args.steps):   # one step at a time: each step's FGMRES column count
+        ctx.record(2)
+        ctx.step(1)
+        ctx.record(3)
+        ms_timed += ctx.elapsed_ms(2, 3)
+        for s in range(ctx.nscenes):
+            it = ctx.info(s)["ppe_iters"]
+            fg_reads += fg_columns(it, restart)
+            fg_launches += it
     kt = ctx.kernel_times()
     ctx.kernel_timing(0)
     value, ms_max = aggregate(D, n_particles, args.steps, ms)
@@ -228,7 +270,7 @@ def run_ours(args, D):
     cands = [(k, v[0], v[1]) for k, v in kt.items() if k in TIMED_KERNELS and v[0]]
     if cands:
         name, cnt, tms = max(cands, key=lambda t: t[2])
-        alg = algorithmic_bytes(ctx, name, args.precision)
+        alg = algorithmic_bytes(ctx, name, args.precision, basis_reads=fg_reads / max(fg_launches, 1))
         avg_s = tms / cnt / 1e3
         pk, src = peaks()
         achieved = alg / avg_s / 1e9
@@ -238,9 +280,16 @@ def run_ours(args, D):
                            "traffic_source": "ncu dram__bytes_read+write on the 0.18 M-particle case, scaled",
                            "algorithmic_bytes_per_launch": alg,
                            "avg_launch_us": round(avg_s * 1e6, 2), "launches": cnt,
+                           "basis_vectors_per_launch": (round(fg_reads / max(fg_launches, 1), 2)
+                                                        if name.startswith("fg_") else None),
                            "share_of_step": round(tms / ms_timed, 3),
                            "note": "durations from a second pass of the same steps with per-launch events",
                            "timed_kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in kt.items()}}
+        fl = fp64_flops(ctx, name, fg_reads / max(fg_launches, 1))
+        if fl:
+            out["roofline"]["fp64"] = {"flops_per_launch": round(fl), "achieved_tflops": round(fl / avg_s / 1e12, 3),
+                                       "nominal_peak_tflops": 1.25,
+                                       "frac": round(fl / avg_s / 1e12 / 1.25, 3)}
     state = ctx.download(0)
     ctx.close()
     if not args.no_e2e:
@@ -282,6 +331,9 @@ def run_fp64_and_accuracy(args, P, S, G, state):
         q.ppe_maxit = 20000
         q.ppe_precond = precond
         cc = api.Context([q], [st], [G[0]], tuning="auto")
+        if not precond:   # the plain solve is the unpreconditioned BiCGStab
+            cc.set_option("ppe_precond", 0)
+            cc.set_option("ppe_solver", abi.SOLVER_BICGSTAB)
         cc.prime()
         cc.step(1)
         o = cc.download(0)
@@ -478,7 +530,7 @@ def main():
     D = Dist()
     config = {"workload": args.workload, "description": WORKLOADS[args.workload], "dt": 1e-4,
               "ppe_tol": 1e-8, "precision": args.precision, "scenes_per_gpu": 1,
-              "ppe_solver": "BiCGStab, multigrid V-cycle right preconditioner",
+              "ppe_solver": None,
               "l2": "state larger than L2, streamed every step (no flush)"}
     base = {"metric": METRIC, "unit": UNIT, "n_gpus": D.world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
@@ -506,6 +558,10 @@ def main():
         line["config"]["ppe_relres_last_step"] = out["ppe_relres_last"]
         line["config"]["err_bits"] = out["err_bits"]
         line["config"]["solver_tuning"] = out["tuning"]
+        tun = out["tuning"] or {}
+        line["config"]["ppe_solver"] = (
+            f"FGMRES({int(tun.get('ppe_restart', 150))}), multigrid right preconditioner"
+            if int(tun.get("ppe_solver", 0)) == 1 else "BiCGStab, multigrid right preconditioner")
         if D.world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(args)
         if not args.no_batch:
