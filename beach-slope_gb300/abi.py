@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("kmax", _i), ("mixed_inner_tol", _d), ("mixed_max_outer", _i), ("ppe_precond", _i),
         ("wc_c0", _d), ("wc_gamma", _d), ("wc_delta", _d), ("wc_ysurf", _d), ("wc_form", _i), ("wc_pad", _i),
         ("ppe_solver", _i), ("ppe_restart", _i),
+        ("buf_release_lo", _d), ("buf_release_hi", _d),
     ]
 
     def as_dict(self):
@@ -96,6 +97,8 @@ def default_params():
     p.wc_ysurf = 0.0        # set per scene (still-water level)
     p.ppe_solver = 0        # BiCGStab
     p.ppe_restart = 150     # FGMRES restart length (MKL's default in the reference's call)
+    p.buf_release_lo = 1e300    # comp_pos buffer release window (empty: never)
+    p.buf_release_hi = -1e300
     return p
 
 
@@ -113,6 +116,39 @@ class State(C.Structure):
 
 class Grains(C.Structure):
     _fields_ = [("n", _i), ("x", _pd), ("y", _pd), ("mass", _pd), ("rho", _pd)]
+
+
+class Inflow(C.Structure):
+    _fields_ = [("n", _i), ("x", _pd), ("y", _pd), ("vx", _pd), ("vy", _pd), ("p", _pd), ("pid", _pi),
+                ("mass", _d), ("rho", _d), ("ovol", _d), ("con", _d), ("period", _d), ("phase", _d),
+                ("remove_x", _d), ("remove_side", _i), ("ncells", _i), ("cell_i", _pi), ("cell_j", _pi)]
+
+
+def inflow_in(zone):
+    """bs_inflow from a dict: template arrays x, y, vx, vy, p (pid optional),
+    scalars mass, rho, ovol, con, period, phase, remove_x, remove_side and
+    cells = [(i, j), ...] (1-based, dpcell(i, j)).  None clears the zone."""
+    z = Inflow()
+    if zone is None:
+        return z
+    keep = {k: np.ascontiguousarray(zone[k], dtype=np.float64) for k in ("x", "y", "vx", "vy", "p")}
+    z.n = int(len(keep["x"]))
+    for k in ("x", "y", "vx", "vy", "p"):
+        setattr(z, k, _ptr(keep[k], C.c_double))
+    if zone.get("pid") is not None:
+        keep["pid"] = np.ascontiguousarray(zone["pid"], dtype=np.int32)
+        z.pid = _ptr(keep["pid"], C.c_int32)
+    for k in ("mass", "rho", "ovol", "con", "period", "phase", "remove_x"):
+        setattr(z, k, float(zone[k]))
+    z.remove_side = int(zone["remove_side"])
+    cells = np.asarray(zone["cells"], dtype=np.int32).reshape(-1, 2)
+    keep["ci"] = np.ascontiguousarray(cells[:, 0])
+    keep["cj"] = np.ascontiguousarray(cells[:, 1])
+    z.ncells = int(len(cells))
+    z.cell_i = _ptr(keep["ci"], C.c_int32)
+    z.cell_j = _ptr(keep["cj"], C.c_int32)
+    z._keep = keep
+    return z
 
 
 class SceneInfo(C.Structure):

@@ -72,6 +72,8 @@ def _load():
         "bs_bicgstab_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, vp, vp]),
         "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
         "bs_fgmres_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, i32, vp, vp]),
+        "bs_set_inflow": (C.c_int, [vp, i32, i32, vp]),
+        "bs_buffer_exchange": (C.c_int, [vp, i32, i32]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
         "bs_kernel_timing": (C.c_int, [vp, C.c_uint64]),
@@ -199,6 +201,15 @@ class Context:
         self._check(lib.bs_get_matrix(self.h, s, diag.ctypes.data, off.ctypes.data, rhs.ctypes.data),
                     "get_matrix")
         return diag, off, rhs
+
+    def set_inflow(self, zone_index, zone, s=0):
+        """Open-boundary buffer zone (0: buffer1, 1: buffer2) of scene s; see
+        abi.inflow_in for the dict; None clears it."""
+        z = abi.inflow_in(zone)
+        self._check(lib.bs_set_inflow(self.h, s, zone_index, C.byref(z)), "set_inflow")
+
+    def buffer_exchange(self, zone_index, s=0):
+        self._check(lib.bs_buffer_exchange(self.h, s, zone_index), "buffer_exchange")
 
     def set_option(self, name, value):
         self._check(lib.bs_set_option(self.h, name.encode(), float(value)), "set_option " + name)

@@ -290,6 +290,135 @@ __global__ void k_derive(Dev D) {
     D.nu[r] = (D.tid[r] == BS_TID_FLUID) ? bs_vis(od) / od : 0.0;
 }
 
+// ------------------------------------------------- open-boundary buffers
+// remove_bufferN + insert_bufferN (internal.f90:447-586) on one scene: the
+// zone's entry cells lose their buffer particles at or beyond remove_x (the
+// others keep their order) and gain the template particles inside them, in
+// template order, after the survivors.  Other cells keep their rows.  The
+// reference compacts plist but not the per-slot pplist, so the porosity that
+// the next projection reads is the one of the cell's slot position: new slot
+// k takes the porosity of old slot k, and a slot beyond the cell's old count
+// the properties' default, 1 (particle.f90:60-69).
+
+__device__ __forceinline__ bool bx_removed(const bs::ZoneDev& Z, double x, uint8_t fl) {
+    if (!(fl & BS_FLAG_BUFFER)) return false;
+    return Z.remove_side > 0 ? (x >= Z.remove_x) : (x <= Z.remove_x);
+}
+
+// one warp per cell of scene s: new cell total; old range kept in cell_start2/end2
+__global__ void k_bx_count(Dev D, int s, bs::ZoneDev Z) {
+    const ScenePar& P = D.par[s];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= P.ncell) return;
+    const int c = P.cell0 + warp;
+    const int r0 = D.cell_start[c], r1 = D.cell_end[c];
+    int keep = r1 - r0, add = 0;
+    if (D.czone[c] & (1u << Z.zone)) {
+        keep = 0;
+        for (int base = r0; base < r1; base += 32) {
+            const int r = base + lane;
+            const bool k = (r < r1) && !bx_removed(Z, D.x[r], D.flags[r]);
+            keep += __popc(__ballot_sync(0xffffffffu, k));
+        }
+        add = D.zcount[Z.zone][c];
+    }
+    if (lane == 0) {
+        D.cell_start2[c] = r0;
+        D.cell_end2[c] = r1;
+        D.cell_total[c] = keep + add;
+        D.bucket[(long)c * BS_NCAT] = keep;
+    }
+}
+
+// the scene's rows (and porosity) into the alternate buffers
+__global__ void k_bx_copyout(Dev D, int s) {
+    const ScenePar& P = D.par[s];
+    const int r = P.row0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.row0 + D.dyn[s].n) return;
+    D.x2[r] = D.x[r]; D.y2[r] = D.y[r]; D.xs2[r] = D.xs[r]; D.ys2[r] = D.ys[r];
+    D.vx2[r] = D.vx[r]; D.vy2[r] = D.vy[r]; D.vxs2[r] = D.vxs[r]; D.vys2[r] = D.vys[r];
+    D.p2[r] = D.p[r]; D.mass2[r] = D.mass[r]; D.rho2[r] = D.rho[r]; D.oden2[r] = D.oden[r];
+    D.ovol2[r] = D.ovol[r]; D.con2[r] = D.con[r]; D.vol2[r] = D.vol[r]; D.nu2[r] = D.nu[r];
+    D.tid2[r] = D.tid[r]; D.flags2[r] = D.flags[r]; D.pid2[r] = D.pid[r];
+    D.sxd[r] = D.por[r];
+}
+
+// one block: exclusive scan of the scene's new cell totals -> cell_start/end, n
+__global__ void k_bx_scan(Dev D, int s) {
+    const ScenePar& P = D.par[s];
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int nb = blockDim.x;
+    for (int base = 0; base < P.ncell; base += nb) {
+        const int q = base + threadIdx.x;
+        const int v = (q < P.ncell) ? D.cell_total[P.cell0 + q] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < nb; o <<= 1) {
+            const int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (q < P.ncell) {
+            const int st = P.row0 + carry + sh[threadIdx.x] - v;
+            D.cell_start[P.cell0 + q] = st;
+            D.cell_end[P.cell0 + q] = st + v;
+        }
+        __syncthreads();
+        if (threadIdx.x == nb - 1) carry += sh[nb - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) D.dyn[s].n = carry;
+}
+
+// one warp per cell: survivors (stable) then the cell's template particles
+__global__ void k_bx_scatter(Dev D, int s, bs::ZoneDev Z) {
+    const ScenePar& P = D.par[s];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= P.ncell) return;
+    const int c = P.cell0 + warp;
+    const int o0 = D.cell_start2[c], o1 = D.cell_end2[c];
+    const int oldn = o1 - o0;
+    const int n0 = D.cell_start[c];
+    const bool zc = D.czone[c] & (1u << Z.zone);
+    const unsigned lt = (1u << lane) - 1u;
+    int kept = 0;
+    for (int base = o0; base < o1; base += 32) {
+        const int r = base + lane;
+        const bool k = (r < o1) && !(zc && bx_removed(Z, D.x2[r], D.flags2[r]));
+        const unsigned m = __ballot_sync(0xffffffffu, k);
+        if (k) {
+            const int slot = kept + __popc(m & lt);
+            const int d = n0 + slot;
+            D.x[d] = D.x2[r]; D.y[d] = D.y2[r]; D.xs[d] = D.xs2[r]; D.ys[d] = D.ys2[r];
+            D.vx[d] = D.vx2[r]; D.vy[d] = D.vy2[r]; D.vxs[d] = D.vxs2[r]; D.vys[d] = D.vys2[r];
+            D.p[d] = D.p2[r]; D.mass[d] = D.mass2[r]; D.rho[d] = D.rho2[r]; D.oden[d] = D.oden2[r];
+            D.ovol[d] = D.ovol2[r]; D.con[d] = D.con2[r]; D.vol[d] = D.vol2[r]; D.nu[d] = D.nu2[r];
+            D.tid[d] = D.tid2[r]; D.flags[d] = D.flags2[r]; D.pid[d] = D.pid2[r]; D.cell[d] = c;
+            D.por[d] = D.sxd[o0 + slot];   // slot position (slot < old count here)
+        }
+        kept += __popc(m);
+    }
+    if (!zc) return;
+    const int t0 = D.zstart[Z.zone][c], tn = D.zcount[Z.zone][c];
+    for (int q = lane; q < tn; q += 32) {
+        const int t = t0 + q;
+        const int slot = kept + q;
+        const int d = n0 + slot;
+        D.x[d] = Z.x[t]; D.y[d] = Z.y[t]; D.xs[d] = 0.0; D.ys[d] = 0.0;
+        D.vx[d] = Z.vx[t]; D.vy[d] = Z.vy[t]; D.vxs[d] = 0.0; D.vys[d] = 0.0;
+        D.p[d] = Z.p[t]; D.mass[d] = Z.mass; D.rho[d] = Z.rho; D.oden[d] = Z.rho;
+        D.ovol[d] = Z.ovol; D.con[d] = Z.con;
+        D.vol[d] = Z.mass / Z.rho;
+        D.nu[d] = bs_vis(Z.rho) / Z.rho;
+        D.tid[d] = BS_TID_FLUID; D.flags[d] = BS_FLAG_BUFFER; D.pid[d] = Z.pid ? Z.pid[t] : 0; D.cell[d] = c;
+        D.por[d] = (slot < oldn) ? D.sxd[o0 + slot] : 1.0;
+    }
+}
+
 inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace
@@ -309,6 +438,16 @@ void rebin(const Dev& D, const Launch& L, int projection, int cutoff) {
     tend(L, q);
     q = tbegin(L, K_PERMUTE);
     k_permute<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, projection);
+    tend(L, q);
+}
+
+void buffer_exchange(const Dev& D, const Launch& L, int s, const ScenePar& P, const ZoneDev& Z) {
+    const int q = tbegin(L, K_BUFX);
+    const unsigned gc = gdiv((long)P.ncell * 32, BS_THREADS);
+    k_bx_count<<<gc, BS_THREADS, 0, L.stream>>>(D, s, Z);
+    k_bx_copyout<<<P.nblk, BS_THREADS, 0, L.stream>>>(D, s);
+    k_bx_scan<<<1, 1024, 0, L.stream>>>(D, s);
+    k_bx_scatter<<<gc, BS_THREADS, 0, L.stream>>>(D, s, Z);
     tend(L, q);
 }
 
@@ -351,7 +490,7 @@ const char* const kernel_names[K_COUNT] = {
     "mx_residual", "mx_convert", "bicg_p_update", "bicg_s_update", "mx_update", "mg_galerkin0",
     "mg_galerkin", "mg_l0_down", "mg_down", "mg_coarse", "mg_up", "mg_l0_up", "mg_l0_prolong",
     "mg_resid", "relpos", "wc_continuity", "wc_rows", "wc_wall_pressure",
-    "fg_start", "fg_put", "fg_arnoldi_spmv", "fg_project", "fg_update"};
+    "fg_start", "fg_put", "fg_arnoldi_spmv", "fg_project", "fg_update", "buffer_exchange"};
 
 // Accumulate the finished launches of the ring in order; with wait, block on
 // the oldest pending end event (used when the ring is full).

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstddef>
@@ -44,6 +45,19 @@ struct bs_ctx {
     std::vector<std::vector<int>> mgrange;   // per scene: cells reserved on each level (fixed at create)
     std::vector<int> cellx_cap, celly_cap;   // per scene: largest cell grid the slot takes
     std::vector<unsigned char> mgneed;   // per level: which launches some scene needs (Launch::mgneed)
+    // open-boundary buffer zones, per scene and zone (0, 1)
+    struct Zone {
+        bool set = false;
+        bs::ZoneDev dev{};
+        double period = 0, phase = 0;
+        long next_k = 1;
+        int n = 0;          // template particles inside entry cells
+        double* mem = nullptr;   // x, y, vx, vy, p of the template, grouped by cell
+        int* pmem = nullptr;     // pid
+    };
+    std::vector<std::array<Zone, 2>> zones;
+    bool any_zone = false;
+    std::vector<SceneDyn> hdyn;   // host copy of the scenes' dynamic state (schedule of the zones)
 };
 
 namespace {
@@ -195,6 +209,7 @@ void fill_par(ScenePar& P, const bs_params& p, int kmax) {
     P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
     P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;
     P.xlcutoff = p.xlcutoff; P.ytcutoff = p.ytcutoff; P.ppe_tol = p.ppe_tol; P.inner_tol = p.mixed_inner_tol;
+    P.buf_lo = p.buf_release_lo; P.buf_hi = p.buf_release_hi;
     P.wc_c0 = p.wc_c0; P.wc_gamma = p.wc_gamma; P.wc_delta = p.wc_delta; P.wc_ysurf = p.wc_ysurf;
     P.wc_form = p.wc_form;
     P.cellx = p.cellx; P.celly = p.celly; P.ncell = p.cellx * p.celly;
@@ -293,6 +308,47 @@ int st_solve(bs_ctx* c) {
     return 0;
 }
 
+// host copy of every scene's dynamic state (t, dt, n for the buffer schedule)
+int read_dyn(bs_ctx* ctx) {
+    ctx->hdyn.resize(ctx->nscene);
+    CK(cudaMemcpyAsync(ctx->hdyn.data(), ctx->D.dyn, sizeof(SceneDyn) * ctx->nscene, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int zone_exchange(bs_ctx* ctx, int s, int z, long n_now) {
+    const auto& Z = ctx->zones[s][z];
+    const ScenePar& P = ctx->hpar[s];
+    if (n_now + Z.n > P.cap) return fail(ctx, BS_E_CAPACITY, "buffer insertion could exceed the scene's row capacity");
+    bs::buffer_exchange(ctx->D, launch_of(ctx), s, P, Z.dev);
+    ctx->assembled = false;
+    return check_launch(ctx);
+}
+
+// main.f90:218-234, after the scalar sub-steps and before projection: zone z
+// of a scene exchanges when (told + phase) < k period <= (told + dt + phase);
+// hdyn holds each scene's t, dt and n from before the step's time advance
+int st_buffers(bs_ctx* ctx) {
+    if (!ctx->any_zone) return 0;
+    for (int s = 0; s < ctx->nscene; ++s) {
+        if (ctx->hdyn[s].hold) continue;
+        const double told = ctx->hdyn[s].t, tn = told + ctx->hdyn[s].dt;
+        long n = ctx->hdyn[s].n;
+        for (int z = 0; z < 2; ++z) {
+            auto& Z = ctx->zones[s][z];
+            if (!Z.set || !(Z.period > 0)) continue;
+            const double kp = (double)Z.next_k * Z.period;
+            if (((told + Z.phase) < kp) && ((tn + Z.phase) >= kp)) {
+                if (int rc = zone_exchange(ctx, s, z, n)) return rc;
+                Z.next_k += 1;
+                n += Z.n;   // an upper bound of the new count
+            }
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -309,6 +365,7 @@ void bs_params_default(bs_params* p) {
     p->kmax = 48; p->mixed_inner_tol = 1e-3; p->mixed_max_outer = 0;
     p->wc_gamma = 7.0; p->wc_delta = 0.1;
     p->ppe_solver = BS_SOLVER_BICGSTAB; p->ppe_restart = 150;
+    p->buf_release_lo = 1e300; p->buf_release_hi = -1e300;   // never
 }
 
 int bs_set_device(int32_t device) {
@@ -324,6 +381,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     bs_ctx* ctx = new bs_ctx();
     ctx->nscene = nscenes;
     ctx->prm.assign(params, params + nscenes);
+    ctx->zones.resize(nscenes);
     ctx->precision = params[0].precision;
     ctx->kmax = 0;
     for (int s = 0; s < nscenes; ++s) {
@@ -872,6 +930,115 @@ int bs_set_rhs(bs_ctx* ctx, int32_t s, const double* b) {
     return 0;
 }
 
+// Buffer zone of a scene (remove_bufferN / insert_bufferN, internal.f90:447-586):
+// entry-cell bits per cell, the template grouped by destination cell (template
+// order within a cell; particles outside the entry cells dropped, as the
+// reference only visits entry cells), uploaded once.
+int bs_set_inflow(bs_ctx* ctx, int32_t s, int32_t zone, const bs_inflow* z) {
+    if (!ctx || s < 0 || s >= ctx->nscene || zone < 0 || zone > 1 || !z || z->n < 0 || z->ncells < 0)
+        return BS_E_ARG;
+    const bool clear = (z->n == 0 && z->ncells == 0);
+    if (!clear && ((z->n && (!z->x || !z->y || !z->vx || !z->vy || !z->p)) || (z->ncells && (!z->cell_i || !z->cell_j)) ||
+                   (z->remove_side != 1 && z->remove_side != -1) || !(z->rho > 0)))
+        return fail(ctx, BS_E_ARG, "bad buffer zone");
+    CK(cudaStreamSynchronize(ctx->stream));
+    Dev& D = ctx->D;
+    if (!D.czone) {
+        int rc = dalloc(ctx, &D.czone, ctx->ncell_total);
+        for (int q = 0; q < 2 && !rc; ++q) {
+            rc = dalloc(ctx, &D.zstart[q], ctx->ncell_total);
+            if (!rc) rc = dalloc(ctx, &D.zcount[q], ctx->ncell_total);
+        }
+        if (rc) return rc;
+    }
+    const ScenePar& P = ctx->hpar[s];
+    const bs_params& p = ctx->prm[s];
+    const uint8_t bit = (uint8_t)(1u << zone);
+    std::vector<uint8_t> cz(P.ncell);
+    CK(cudaMemcpy(cz.data(), D.czone + P.cell0, P.ncell, cudaMemcpyDeviceToHost));
+    for (auto& b : cz) b &= (uint8_t)~bit;
+    std::vector<int> zst(P.ncell, 0), zct(P.ncell, 0);
+    std::vector<double> tf[5];
+    std::vector<int> tpid;
+    if (!clear) {
+        for (int q = 0; q < z->ncells; ++q) {
+            const int i = z->cell_i[q], j = z->cell_j[q];
+            if (i < 2 || i > p.celly - 1 || j < 2 || j > p.cellx - 1)
+                return fail(ctx, BS_E_ARG, "entry cell outside the interior grid");
+            const int lc = (j - 1) * p.celly + (i - 1);
+            if (cz[lc] & bit) return fail(ctx, BS_E_ARG, "entry cell listed twice");
+            cz[lc] |= bit;
+        }
+        std::vector<std::pair<int, int>> order;   // (cell, template index)
+        for (int q = 0; q < z->n; ++q) {
+            int ci, cj;
+            if (!locate(p, z->x[q], z->y[q], &ci, &cj)) continue;
+            const int lc = (cj - 1) * p.celly + (ci - 1);
+            if (cz[lc] & bit) order.push_back({lc, q});
+        }
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+        for (size_t k = 0; k < order.size(); ++k) {
+            const int lc = order[k].first, q = order[k].second;
+            if (zct[lc] == 0) zst[lc] = (int)k;
+            zct[lc]++;
+            tf[0].push_back(z->x[q]);
+            tf[1].push_back(z->y[q]);
+            tf[2].push_back(z->vx[q]);
+            tf[3].push_back(z->vy[q]);
+            tf[4].push_back(z->p[q]);
+            tpid.push_back(z->pid ? z->pid[q] : 0);
+        }
+    }
+    CK(cudaMemcpy(D.czone + P.cell0, cz.data(), P.ncell, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.zstart[zone] + P.cell0, zst.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.zcount[zone] + P.cell0, zct.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    auto& Z = ctx->zones[s][zone];
+    dfree(ctx, Z.mem);
+    dfree(ctx, Z.pmem);
+    Z = bs_ctx::Zone();
+    if (!clear) {
+        const size_t m = tf[0].size();
+        int rc = dalloc(ctx, &Z.mem, 5 * m);
+        if (!rc) rc = dalloc(ctx, &Z.pmem, m);
+        if (rc) return rc;
+        for (int f = 0; f < 5; ++f)
+            if (m) CK(cudaMemcpy(Z.mem + f * m, tf[f].data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+        if (m) CK(cudaMemcpy(Z.pmem, tpid.data(), sizeof(int) * m, cudaMemcpyHostToDevice));
+        bs::ZoneDev& G = Z.dev;
+        G.x = Z.mem;
+        G.y = Z.mem + m;
+        G.vx = Z.mem + 2 * m;
+        G.vy = Z.mem + 3 * m;
+        G.p = Z.mem + 4 * m;
+        G.pid = Z.pmem;
+        G.mass = z->mass;
+        G.rho = z->rho;
+        G.ovol = z->ovol;
+        G.con = z->con;
+        G.remove_x = z->remove_x;
+        G.remove_side = z->remove_side;
+        G.zone = zone;
+        Z.period = z->period;
+        Z.phase = z->phase;
+        Z.next_k = 1;
+        Z.n = (int)m;
+        Z.set = true;
+    }
+    ctx->any_zone = false;
+    for (auto& a : ctx->zones)
+        for (auto& b : a) ctx->any_zone |= b.set;
+    return 0;
+}
+
+int bs_buffer_exchange(bs_ctx* ctx, int32_t s, int32_t zone) {
+    if (!ctx || s < 0 || s >= ctx->nscene || zone < 0 || zone > 1) return BS_E_ARG;
+    if (!ctx->zones[s][zone].set) return fail(ctx, BS_E_STATE, "buffer zone not set");
+    if (int rc = read_dyn(ctx)) return rc;
+    if (int rc = zone_exchange(ctx, s, zone, ctx->hdyn[s].n)) return rc;
+    return bs_sync(ctx);
+}
+
 // Re-use scene slot s for another scene: new parameters (its cell grid no
 // larger than the one the slot was created with), particles and grains.
 int bs_set_scene(bs_ctx* ctx, int32_t s, const bs_params* p, const bs_state* st, const bs_grains* gr) {
@@ -891,6 +1058,12 @@ int bs_set_scene(bs_ctx* ctx, int32_t s, const bs_params* p, const bs_state* st,
     for (int* a : zc) CK(cudaMemset(a + P.cell0, 0, sizeof(int) * nc));
     CK(cudaMemset(D.cell_maxvel + P.cell0, 0, sizeof(double) * nc));
     CK(cudaMemset(D.cell_maxeddy + P.cell0, 0, sizeof(double) * nc));
+    for (int z = 0; z < 2; ++z)   // the slot's buffer zones belong to the old scene
+        if (ctx->zones[s][z].set) {
+            bs_inflow none;
+            std::memset(&none, 0, sizeof(none));
+            if (int rc = bs_set_inflow(ctx, s, z, &none)) return rc;
+        }
     ctx->prm[s] = *p;
     fill_par(P, *p, ctx->kmax);
     ctx->mgdims[s] = mg_dims_of(p->cellx, p->celly);
@@ -1115,6 +1288,8 @@ int bs_wcsph_step(bs_ctx* ctx, int32_t nsteps) {
     Dev& D = ctx->D;
     for (int it = 0; it < nsteps; ++it) {
         bs::Launch L = launch_of(ctx);
+        if (ctx->any_zone)
+            if (int rc = read_dyn(ctx)) return rc;
         bs::advance_time(D, L);
         bool any_scalar = false;
         for (auto& p : ctx->prm) any_scalar |= p.scalar_on != 0;
@@ -1125,6 +1300,7 @@ int bs_wcsph_step(bs_ctx* ctx, int32_t nsteps) {
             }
             for (int j1 = 0; j1 < ctx->max_solsteps; ++j1) st_scalar(ctx, j1);
         }
+        if (int rc = st_buffers(ctx)) return rc;
         st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
         st_search(ctx, 1, 2);                // neighbour + effpor keeping the density
         bs::eddy(D, L, ctx->precision, 1, 1, 0);
@@ -1156,6 +1332,8 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
     Dev& D = ctx->D;
     for (int it = 0; it < nsteps; ++it) {
         bs::Launch L = launch_of(ctx);
+        if (ctx->any_zone)
+            if (int rc = read_dyn(ctx)) return rc;
         bs::advance_time(D, L);
         bool any_scalar = false;
         for (auto& p : ctx->prm) any_scalar |= p.scalar_on != 0;
@@ -1167,6 +1345,7 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
             // solsteps of the previous timestep() (read back at the end of the last step)
             for (int j1 = 0; j1 < ctx->max_solsteps; ++j1) st_scalar(ctx, j1);
         }
+        if (int rc = st_buffers(ctx)) return rc;   // remove_bufferN + insert_bufferN
         st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
         st_search(ctx, 1, 1);                // neighbour + effpor
         bs::eddy(D, L, ctx->precision, 1, 1, 0);  // eddyvis (+ varts of int_vel)

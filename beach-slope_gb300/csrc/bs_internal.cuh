@@ -43,6 +43,7 @@ struct ScenePar {                 // per-scene constants
     double freethr;               // lamfs*maxdivr
     double csh, maxshift, sig1;
     double xlcutoff, ytcutoff;
+    double buf_lo, buf_hi;        // comp_pos buffer release window (integrator.f90:865-872)
     double ppe_tol, inner_tol;
     double wc_c0, wc_gamma, wc_delta, wc_ysurf;   // WCSPH (wcsph.f90)
     int wc_form, wc_pad;
@@ -157,6 +158,10 @@ struct Dev {
     double *fg_V, *fg_Z, *fg_part, *fg_gpart, *fg_small;
     int* fg_gdone;                  // per-group block counters
     int fg_m, fg_small_n, fg_ld;    // restart length, doubles per scene, rows per basis vector
+    // open-boundary buffer zones: per global cell, the zone bits of the entry
+    // cells and, per zone, the cell's template range [zstart, zstart + zcount)
+    uint8_t* czone;
+    int *zstart[2], *zcount[2];
     // cells
     int *cell_start, *cell_end, *cell_start2, *cell_end2;
     int* bucket;                    // [ncell_total*BS_NCAT] counts then starts
@@ -317,7 +322,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -422,6 +427,15 @@ __device__ __forceinline__ void mg_put_input(const Dev& D, int r, double x) {
 }
 void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int* d_all_conv,
                  int* h_all_conv_pinned, cudaEvent_t ev);
+// one scene's buffer zone template and exchange rule (remove_bufferN +
+// insert_bufferN, internal.f90:447-586)
+struct ZoneDev {
+    const double *x, *y, *vx, *vy, *p;
+    const int* pid;                 // may be null (pid 0)
+    double mass, rho, ovol, con, remove_x;
+    int remove_side, zone;
+};
+void buffer_exchange(const Dev& D, const Launch& L, int s, const ScenePar& P, const ZoneDev& Z);
 void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
                   int* d_nconv, int* h_nconv, cudaEvent_t ev);
 // per-scene small FGMRES storage for restart length m (doubles)

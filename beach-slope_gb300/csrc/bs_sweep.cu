@@ -565,8 +565,12 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
     if (do_pos && ti == BS_TID_FLUID) {
         // x = (x + xs + dt*vx/porosity)/2 (integrator.f90:859-863), no FMA
         const double x = D.x[r], y = D.y[r];
-        D.x[r] = __ddiv_rn(__dadd_rn(__dadd_rn(x, D.xs[r]), __ddiv_rn(__dmul_rn(dt, vx), phi)), 2.0);
+        const double xn = __ddiv_rn(__dadd_rn(__dadd_rn(x, D.xs[r]), __ddiv_rn(__dmul_rn(dt, vx), phi)), 2.0);
+        D.x[r] = xn;
         D.y[r] = __ddiv_rn(__dadd_rn(__dadd_rn(y, D.ys[r]), __ddiv_rn(__dmul_rn(dt, vy), phi)), 2.0);
+        // buffer release (integrator.f90:865-872)
+        const ScenePar& P = D.par[R.s];
+        if ((fl & BS_FLAG_BUFFER) && (xn > P.buf_lo) && (xn < P.buf_hi)) D.flags[r] = fl & ~BS_FLAG_BUFFER;
     }
 }
 

@@ -252,3 +252,54 @@ BEACH_N_DX2 = 712460 * 0.00125 ** 2
 def dx_for_particles(n):
     """Lattice spacing that gives a beach scene of about n particles."""
     return float(np.sqrt(BEACH_N_DX2 / n))
+
+
+def cell_of(p, x, y):
+    """(i, j) of the interior cell that holds (x, y) by the half-open bounds
+    of setup.f90:120-123 (xleft = (j-2) 4h, ytop = (celly - i) 4h), or None."""
+    cw = 4.0 * p.h
+    j = int(math.floor(x / cw)) + 2
+    i = p.celly - 1 - int(math.floor(y / cw))
+    for di in (0, -1, 1):
+        for dj in (0, -1, 1):
+            ii, jj = i + di, j + dj
+            if ((jj - 2) * cw <= x < (jj - 1) * cw) and ((-ii + p.celly - 1) * cw <= y < (-ii + p.celly) * cw):
+                if 2 <= ii <= p.celly - 1 and 2 <= jj <= p.cellx - 1:
+                    return ii, jj
+    return None
+
+
+def with_inflow(p, st, ncol=5, ntemplate=2, entry_vel=-0.05, period=0.0, phase=0.0, release_gap=None):
+    """An open-boundary buffer zone on the right of a scene's fluid, shaped as
+    the reference's right-hand buffer (internal.f90:98-215): the last `ncol`
+    fluid columns become buffer particles moving at entry_vel, the last
+    `ntemplate` columns are the template (buffer1: column by column, top row
+    first), the entry cells are the cells holding the zone, and buffer
+    particles at or beyond 0.75 spacing left of the first template column are
+    removed at an exchange (rv_buf_r).  Inserted particles take the lattice
+    mass, rho, ovol and con = -0.5 (insert_buffer1).  With release_gap, buffer
+    particles that move left of the zone's first column minus the gap become
+    fluid (comp_pos, integrator.f90:865-872).  Changes st in place; returns
+    the zone dict for set_inflow."""
+    fl = st["tid"] == abi.TID_FLUID
+    xr = np.round(st["x"] / p.dl * 8.0) / 8.0   # lattice columns (unjittered scenes)
+    cols = np.unique(xr[fl])
+    zone_cols, tmpl_cols = cols[-ncol:], cols[-ntemplate:]
+    inz = fl & np.isin(xr, zone_cols)
+    st["flags"] = st["flags"] | np.where(inz, abi.FLAG_BUFFER, 0).astype(np.uint8)
+    st["vx"] = np.where(inz, entry_vel, st["vx"])
+    st["vy"] = np.where(inz, 0.0, st["vy"])
+    tq = np.nonzero(fl & np.isin(xr, tmpl_cols))[0]
+    tq = tq[np.lexsort((-st["y"][tq], xr[tq]))]   # column by column, top row first
+    cells = sorted({cell_of(p, st["x"][q], st["y"][q]) for q in np.nonzero(inz)[0]} - {None},
+                   key=lambda c: (c[1], c[0]))
+    dx = p.dl
+    x_first = float(st["x"][inz].min())
+    if release_gap is not None:
+        p.buf_release_lo = float(st["x"][fl].min())
+        p.buf_release_hi = x_first - release_gap
+    return {"x": st["x"][tq].copy(), "y": st["y"][tq].copy(), "vx": np.full(len(tq), entry_vel),
+            "vy": np.zeros(len(tq)), "p": st["p"][tq].copy(), "pid": None,
+            "mass": p.rho * dx * dx, "rho": p.rho, "ovol": dx * dx, "con": -0.5,
+            "period": period, "phase": phase, "remove_x": float(st["x"][tq].min()) - 0.75 * dx,
+            "remove_side": 1, "cells": cells}

@@ -147,6 +147,12 @@ typedef struct bs_params {
      * ppe_maxit counting Arnoldi columns over all restart cycles */
     int32_t ppe_solver;
     int32_t ppe_restart;
+    /* comp_pos buffer release (integrator.f90:865-872): a buffer particle
+     * whose new x lies in (buf_release_lo, buf_release_hi) becomes fluid --
+     * the reference's window is (8 prrealx + brrealx + 0.001, xrcutoff).  The
+     * default (lo > hi) never releases. */
+    double buf_release_lo;
+    double buf_release_hi;
 } bs_params;
 
 /*
@@ -172,6 +178,34 @@ typedef struct bs_grains {
     int32_t n;
     double *x, *y, *mass, *rho;
 } bs_grains;
+
+/*
+ * Open-boundary buffer zone of a scene: the reference's remove_bufferN +
+ * insert_bufferN (internal.f90:447-586) with the schedule of main.f90:218-234.
+ * Zone 0 / 1 stand for buffer1 / buffer2.  At an exchange, every buffer
+ * particle of the zone's entry cells whose x is at or beyond remove_x
+ * (remove_side +1: x >= remove_x, rv_buf_r; -1: x <= remove_x, rv_buf_l) is
+ * removed, the survivors keeping their order, then every template particle
+ * is appended to the entry cell that contains it, in template order (give the
+ * template column by column, as the reference's loops visit bufferN(k,i)),
+ * as a buffer fluid particle with the template's position, velocity,
+ * pressure and pid (NULL: 0, as the reference's templates) and the zone's
+ * mass, density (also oden), ovol and con; xs, ys, vxs, vys = 0.  bs_step
+ * runs the exchange after the scalar sub-steps and before projection when
+ * (t_old + phase) < k period <= (t_old + dt + phase), k = 1, 2, ... counted
+ * per zone from bs_set_inflow (period 0: never).
+ */
+typedef struct bs_inflow {
+    int32_t n;
+    const double *x, *y, *vx, *vy, *p;
+    const int32_t* pid;
+    double mass, rho, ovol, con;
+    double period, phase;
+    double remove_x;
+    int32_t remove_side;
+    int32_t ncells;                /* entry cells, dpcell(i, j): 1-based row i, column j */
+    const int32_t *cell_i, *cell_j;
+} bs_inflow;
 
 /* per-scene scalars reported back to the host */
 typedef struct bs_scene_info {
@@ -227,6 +261,13 @@ int bs_set_scene(struct bs_ctx* ctx, int32_t scene, const bs_params* params, con
 /* bs_prime for one scene only; the other scenes are left exactly as they
  * are, so a scene joining a running batch does not perturb the others. */
 int bs_prime_scene(struct bs_ctx* ctx, int32_t scene);
+
+/* Set (or, with z->n = 0 and z->ncells = 0, clear) buffer zone `zone` (0 or
+ * 1) of a scene; the template is copied.  entrycell1/2 of the reference. */
+int bs_set_inflow(struct bs_ctx* ctx, int32_t scene, int32_t zone, const bs_inflow* z);
+/* remove_bufferN + insert_bufferN of one zone now (outside the schedule).
+ * BS_E_CAPACITY if the scene could exceed its row capacity. */
+int bs_buffer_exchange(struct bs_ctx* ctx, int32_t scene, int32_t zone);
 
 /* combined, output.f90:188-222: the scene's fluid particles as text, one
  * line each in the reference's order and format (F10.3 x, y, p; ES10.3 vx,

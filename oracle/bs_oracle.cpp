@@ -141,8 +141,18 @@ inline double vis(double oden) {
 
 }  // namespace
 
+struct OrZone {      // one open-boundary buffer zone (buffer1 / buffer2 + entrycell1 / 2)
+    bool set = false;
+    std::vector<Particle> tmpl;
+    std::vector<std::pair<int, int>> cells;
+    double period = 0, phase = 0, remove_x = 0;
+    int side = 1;
+    long next_k = 1;
+};
+
 struct or_scene {
     bs_params P;
+    OrZone zones[2];
     int cellx, celly;
     double h, lam, dl, cw;
     std::vector<Cell> cells;
@@ -955,7 +965,8 @@ void comp_vel(or_scene* s) {
 }
 
 // --------------------------------------------------------------- comp_pos
-// integrator.f90:845-883 (buffer release needs the buffer geometry: out of scope)
+// integrator.f90:845-883; the release window (8 prrealx + brrealx + 0.001,
+// xrcutoff) of 865-872 is the parameter pair buf_release_lo / hi
 void comp_pos(or_scene* s) {
     const double dt = s->dt;
     for_interior(s, [&](int i, int j) {
@@ -966,6 +977,7 @@ void comp_pos(or_scene* s) {
             if (p.tid == 3) {
                 p.x = (p.x + p.xs + dt * p.vx / pp.porosity) / 2.0;
                 p.y = (p.y + p.ys + dt * p.vy / pp.porosity) / 2.0;
+                if (p.buffer && (p.x > s->P.buf_release_lo) && (p.x < s->P.buf_release_hi)) p.buffer = false;
             }
         }
     });
@@ -1326,10 +1338,58 @@ void prime(or_scene* s) {
 }
 
 // one production step, main.f90:199-272 (buffers excluded)
+// remove_bufferN (internal.f90:516-584) then insert_bufferN (447-514) of one
+// zone: entry cells drop their buffer particles at or beyond remove_x (plist
+// compacted, pplist left in place -- the slot keeps its properties), then
+// every template particle inside an entry cell is appended to it in template
+// order.  A slot beyond the cell's count before the exchange starts from the
+// properties' defaults (the reference would read whatever the slot last held).
+void buffer_exchange(or_scene* s, int z) {
+    OrZone& Z = s->zones[z];
+    std::vector<int> oldn(Z.cells.size());
+    for (size_t q = 0; q < Z.cells.size(); ++q) {
+        Cell& c = s->C(Z.cells[q].first, Z.cells[q].second);
+        oldn[q] = c.ptot;
+        int keep = 0;
+        for (int k = 0; k < c.ptot; ++k) {
+            const Particle& p = c.plist[k];
+            const bool rm = p.buffer && (Z.side > 0 ? (p.x >= Z.remove_x) : (p.x <= Z.remove_x));
+            if (!rm) c.plist[keep++] = p;
+        }
+        c.ptot = keep;
+    }
+    for (size_t q = 0; q < Z.cells.size(); ++q) {
+        Cell& c = s->C(Z.cells[q].first, Z.cells[q].second);
+        for (const Particle& t : Z.tmpl) {
+            if (!((t.x >= c.xleft) && (t.x < c.xright) && (t.y >= c.ybot) && (t.y < c.ytop))) continue;
+            const int k = c.ptot++;
+            if ((int)c.plist.size() < c.ptot) c.plist.resize(c.ptot);
+            if ((int)c.pplist.size() < c.ptot) c.pplist.resize(c.ptot);
+            c.plist[k] = t;
+            if (k >= oldn[q]) c.pplist[k] = Props();
+        }
+    }
+}
+
+// main.f90:218-234: zone z exchanges when (told + phase) < k*period <= (t + phase)
+void buffer_schedule(or_scene* s, double told) {
+    for (int z = 0; z < 2; ++z) {
+        OrZone& Z = s->zones[z];
+        if (!Z.set || !(Z.period > 0)) continue;
+        const double kp = (double)Z.next_k * Z.period;
+        if (((told + Z.phase) < kp) && ((s->t + Z.phase) >= kp)) {
+            buffer_exchange(s, z);
+            Z.next_k += 1;
+        }
+    }
+}
+
 void step(or_scene* s) {
+    const double told = s->t;
     s->t = s->t + s->dt;
     if (s->P.scalar_on)
         for (int j1 = 1; j1 <= s->solsteps; ++j1) scalar_substep(s);
+    buffer_schedule(s, told);
     projection(s);
     cellshift(s, false);
     resetid(s);
@@ -1356,9 +1416,11 @@ void step(or_scene* s) {
 // WCSPH step: the production step with continuity + Tait EOS + wall
 // pressure in place of the PPE, density kept from the continuity equation
 void wcsph_step(or_scene* s) {
+    const double told = s->t;
     s->t = s->t + s->dt;
     if (s->P.scalar_on)
         for (int j1 = 1; j1 <= s->solsteps; ++j1) scalar_substep(s);
+    buffer_schedule(s, told);
     projection(s);
     cellshift(s, false);
     resetid(s);
@@ -1671,6 +1733,55 @@ int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_pa
 
 int or_wcsph_step(or_scene* s, int32_t nsteps) {
     for (int k = 0; k < nsteps; ++k) wcsph_step(s);
+    return 0;
+}
+
+int or_set_inflow(or_scene* s, int32_t zone, const bs_inflow* z) {
+    if (!s || zone < 0 || zone > 1 || !z || z->n < 0 || z->ncells < 0) return BS_E_ARG;
+    OrZone Z;
+    if (z->n == 0 && z->ncells == 0) {
+        s->zones[zone] = Z;
+        return 0;
+    }
+    if ((z->n && (!z->x || !z->y || !z->vx || !z->vy || !z->p)) || (z->ncells && (!z->cell_i || !z->cell_j)) ||
+        (z->remove_side != 1 && z->remove_side != -1) || !(z->rho > 0))
+        return BS_E_ARG;
+    for (int q = 0; q < z->ncells; ++q) {
+        const int i = z->cell_i[q], j = z->cell_j[q];
+        if (i < 2 || i > s->celly - 1 || j < 2 || j > s->cellx - 1) return BS_E_ARG;
+        for (int u = 0; u < q; ++u)
+            if (z->cell_i[u] == i && z->cell_j[u] == j) return BS_E_ARG;
+        Z.cells.push_back({i, j});
+    }
+    for (int q = 0; q < z->n; ++q) {   // bufferN(k,i) with insert_bufferN's assignments
+        Particle t;
+        t.x = z->x[q];
+        t.y = z->y[q];
+        t.vx = z->vx[q];
+        t.vy = z->vy[q];
+        t.pressure = z->p[q];
+        t.pid = z->pid ? z->pid[q] : 0;
+        t.tid = 3;
+        t.buffer = true;
+        t.mass = z->mass;
+        t.density = z->rho;
+        t.oden = z->rho;
+        t.ovol = z->ovol;
+        t.con = z->con;
+        Z.tmpl.push_back(t);
+    }
+    Z.period = z->period;
+    Z.phase = z->phase;
+    Z.remove_x = z->remove_x;
+    Z.side = z->remove_side;
+    Z.set = true;
+    s->zones[zone] = Z;
+    return 0;
+}
+
+int or_buffer_exchange(or_scene* s, int32_t zone) {
+    if (!s || zone < 0 || zone > 1 || !s->zones[zone].set) return BS_E_ARG;
+    buffer_exchange(s, zone);
     return 0;
 }
 

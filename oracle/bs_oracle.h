@@ -59,6 +59,9 @@ int or_wcsph_step(or_scene* s, int32_t nsteps);
 int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_path);
 /* overwrite pressures (used to pin a common PPE guess in tests) */
 int or_set_pressure(or_scene* s, const double* p);
+/* open-boundary buffer zones (internal.f90:447-586, main.f90:218-234) */
+int or_set_inflow(or_scene* s, int32_t zone, const bs_inflow* z);
+int or_buffer_exchange(or_scene* s, int32_t zone);
 int or_bicgstab_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
                     const double* b, double* x, double tol, int32_t maxit, int32_t rule,
                     int32_t* iters, double* relres);

@@ -62,6 +62,8 @@ def lib():
         L.or_wcsph_step.argtypes = [vp, C.c_int32]
         L.or_write_combined.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.or_set_pressure.argtypes = [vp, vp]
+        L.or_set_inflow.argtypes = [vp, C.c_int32, vp]
+        L.or_buffer_exchange.argtypes = [vp, C.c_int32]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_ppe_fgmres.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32, vp, vp]
         L.or_fgmres_csr.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_int32, C.c_int32,
@@ -170,6 +172,15 @@ class Oracle:
     def write_combined(self, fluid_path, buffer_path=None):
         return lib().or_write_combined(self.h, fluid_path.encode(),
                                        buffer_path.encode() if buffer_path else None)
+
+    def set_inflow(self, zone_index, zone):
+        z = self.abi.inflow_in(zone)
+        rc = lib().or_set_inflow(self.h, zone_index, C.byref(z))
+        if rc != 0:
+            raise RuntimeError(f"or_set_inflow failed ({rc})")
+
+    def buffer_exchange(self, zone_index):
+        return lib().or_buffer_exchange(self.h, zone_index)
 
     def set_pressure(self, p):
         p = np.ascontiguousarray(p, dtype=np.float64)
