@@ -73,6 +73,7 @@ def _load():
         "bs_bicgstab_csr_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, vp, vp]),
         "bs_fgmres_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, i32, vp, vp]),
         "bs_set_inflow": (C.c_int, [vp, i32, i32, vp]),
+        "bs_ghost": (C.c_int, [vp, i32]),
         "bs_buffer_exchange": (C.c_int, [vp, i32, i32]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
@@ -92,7 +93,7 @@ lib = _load()
 
 STAGE_FUNCS = ["prime", "scalar_substep", "projection", "search", "porosity", "eddy", "int_vel",
                "ppe_assemble", "ppe_solve", "comp_vel", "comp_pos", "free_surface", "shift",
-               "density_update", "timestep"]
+               "density_update", "timestep", "boun_vel"]
 
 
 class Context:
@@ -207,6 +208,10 @@ class Context:
         abi.inflow_in for the dict; None clears it."""
         z = abi.inflow_in(zone)
         self._check(lib.bs_set_inflow(self.h, s, zone_index, C.byref(z)), "set_inflow")
+
+    def ghost(self, use_mls=False):
+        """comp_ghost + ghost_en (mls.f90:114-263); use_mls: the MLS branch."""
+        self._check(lib.bs_ghost(self.h, 1 if use_mls else 0), "ghost")
 
     def buffer_exchange(self, zone_index, s=0):
         self._check(lib.bs_buffer_exchange(self.h, s, zone_index), "buffer_exchange")

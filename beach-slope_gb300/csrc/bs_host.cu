@@ -1236,6 +1236,16 @@ int bs_free_surface(bs_ctx* ctx) {
     bs::freesurf(ctx->D, launch_of(ctx));
     return check_launch(ctx);
 }
+int bs_boun_vel(bs_ctx* ctx) {
+    if (!ctx) return BS_E_ARG;
+    bs::boun_vel(ctx->D, launch_of(ctx), ctx->precision);
+    return check_launch(ctx);
+}
+int bs_ghost(bs_ctx* ctx, int32_t use_mls) {
+    if (!ctx || (use_mls != 0 && use_mls != 1)) return BS_E_ARG;
+    bs::ghost(ctx->D, launch_of(ctx), ctx->precision, use_mls);
+    return check_launch(ctx);
+}
 int bs_shift(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     bs::shift(ctx->D, launch_of(ctx), ctx->precision);

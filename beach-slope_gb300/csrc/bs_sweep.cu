@@ -852,6 +852,125 @@ __global__ void __launch_bounds__(BS_THREADS) k_wc_wallp(Dev D) {
     D.p[r] = den > 0.0 ? num / den : 0.0;
 }
 
+// ------------------------------------------------ wall / ghost velocity
+// boun_vel (integrator.f90:394-457, compiled but never called) and
+// comp_ghost + ghost_en (mls.f90:114-263, not compiled): wall and ghost rows
+// take minus the Shepard average of their fluid neighbours (no-slip mirror);
+// products in the reference's evaluation order, no contraction.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_boun_vel(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    if (D.tid[r] > 2) return;
+    const ScenePar& P = D.par[R.s];
+    double vx = 0.0, vy = 0.0, t1 = 0.0;
+    const int n = D.ncount[r];
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, D.kmax);
+        const int j = D.nidx[e];
+        if (D.tid[j] != BS_TID_FLUID) continue;
+        const double w = bs_W((double)ld<T>(D.ndist, e), P);
+        const double mw = __dmul_rn(D.mass[j], w), rj = D.rho[j];
+        vx = __dsub_rn(vx, __ddiv_rn(__dmul_rn(mw, D.vx[j]), rj));
+        vy = __dsub_rn(vy, __ddiv_rn(__dmul_rn(mw, D.vy[j]), rj));
+        t1 = __dadd_rn(t1, __ddiv_rn(mw, rj));
+    }
+    if (t1 >= BS_SP1EM6) {
+        vx = __ddiv_rn(vx, t1);
+        vy = __ddiv_rn(vy, t1);
+    }
+    D.vx[r] = vx;
+    D.vy[r] = vy;
+    D.vxs[r] = 0.0;
+    D.vys[r] = 0.0;
+}
+
+// use_mls: the velocity by the module's commented-out moving-least-squares
+// branch, weights W (b1 + b2 dx + b3 dy) V, b = first column of the inverse
+// of the moment matrix over all neighbours (Wmls, mls.f90:16-111;
+// invertmat3D, functions.f90:134-165), where its determinant reaches 1e-5
+// (single literal); the Shepard average elsewhere.  tke and nut always by
+// Shepard (ghost_en).  A zero Shepard sum leaves 0.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_ghost(Dev D, int use_mls) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    if (D.tid[r] > 2) return;
+    const ScenePar& P = D.par[R.s];
+    const int n = D.ncount[r];
+    const double xi = D.x[r], yi = D.y[r];
+    double vx = 0.0, vy = 0.0, tke = 0.0, nut = 0.0;
+    bool err = true;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    if (n > 0 && use_mls) {
+        double a00 = 0, a10 = 0, a20 = 0, a01 = 0, a11 = 0, a21 = 0, a02 = 0, a12 = 0, a22 = 0;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, D.kmax);
+            const int j = D.nidx[e];
+            const double w = bs_W((double)ld<T>(D.ndist, e), P);
+            const double v = __ddiv_rn(D.mass[j], D.rho[j]);
+            const double dx = __dsub_rn(xi, D.x[j]), dy = __dsub_rn(yi, D.y[j]);
+            const double wdx = __dmul_rn(w, dx), wdy = __dmul_rn(w, dy);
+            a00 = __dadd_rn(a00, __dmul_rn(w, v));
+            a10 = __dadd_rn(a10, __dmul_rn(wdx, v));
+            a20 = __dadd_rn(a20, __dmul_rn(wdy, v));
+            a01 = __dadd_rn(a01, __dmul_rn(wdx, v));
+            a11 = __dadd_rn(a11, __dmul_rn(__dmul_rn(w, __dmul_rn(dx, dx)), v));
+            a21 = __dadd_rn(a21, __dmul_rn(__dmul_rn(wdx, dy), v));
+            a02 = __dadd_rn(a02, __dmul_rn(wdy, v));
+            a12 = __dadd_rn(a12, __dmul_rn(__dmul_rn(wdx, dy), v));
+            a22 = __dadd_rn(a22, __dmul_rn(__dmul_rn(w, __dmul_rn(dy, dy)), v));
+        }
+        auto mul = [](double a, double b) { return __dmul_rn(a, b); };
+        auto sub = [](double a, double b) { return __dsub_rn(a, b); };
+        const double det = __dadd_rn(__dsub_rn(mul(a00, sub(mul(a11, a22), mul(a21, a12))),
+                                               mul(a01, sub(mul(a10, a22), mul(a20, a12)))),
+                                     mul(a02, sub(mul(a10, a21), mul(a20, a11))));
+        if (!(det < (double)1e-5f) && isfinite(det)) {
+            err = false;
+            b0 = __ddiv_rn(sub(mul(a11, a22), mul(a21, a12)), det);
+            b1 = __ddiv_rn(-sub(mul(a01, a22), mul(a21, a02)), det);
+            b2 = __ddiv_rn(sub(mul(a01, a12), mul(a11, a02)), det);
+        }
+    }
+    double t1 = 0.0, te = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, D.kmax);
+        const int j = D.nidx[e];
+        if (D.tid[j] != BS_TID_FLUID) continue;
+        const double w = bs_W((double)ld<T>(D.ndist, e), P);
+        const double mj = D.mass[j], rj = D.rho[j];
+        if (!err) {
+            const double corr = __dadd_rn(__dadd_rn(b0, __dmul_rn(b1, __dsub_rn(xi, D.x[j]))),
+                                          __dmul_rn(b2, __dsub_rn(yi, D.y[j])));
+            const double q = __dmul_rn(__dmul_rn(w, corr), __ddiv_rn(mj, rj));
+            vx = __dsub_rn(vx, __dmul_rn(D.vx[j], q));
+            vy = __dsub_rn(vy, __dmul_rn(D.vy[j], q));
+        } else {
+            vx = __dsub_rn(vx, __ddiv_rn(__dmul_rn(__dmul_rn(w, D.vx[j]), mj), rj));
+            vy = __dsub_rn(vy, __ddiv_rn(__dmul_rn(__dmul_rn(w, D.vy[j]), mj), rj));
+            t1 = __dadd_rn(t1, __ddiv_rn(__dmul_rn(mj, w), rj));
+        }
+        tke = __dsub_rn(tke, __ddiv_rn(__dmul_rn(__dmul_rn(w, D.tke[j]), mj), rj));
+        nut = __dsub_rn(nut, __ddiv_rn(__dmul_rn(__dmul_rn(w, D.nut[j]), mj), rj));
+        te = __dadd_rn(te, __ddiv_rn(__dmul_rn(mj, w), rj));
+    }
+    if (err && t1 > 0.0) {
+        vx = __ddiv_rn(vx, t1);
+        vy = __ddiv_rn(vy, t1);
+    }
+    if (te > 0.0) {
+        tke = __ddiv_rn(tke, te);
+        nut = __ddiv_rn(nut, te);
+    }
+    D.vx[r] = vx;
+    D.vy[r] = vy;
+    D.tke[r] = tke;
+    D.nut[r] = nut;
+}
+
 #define BS_DISPATCH(id, prec, kern, ...)                                                          \
     do {                                                                                          \
         const int q_ = tbegin(L, id);                                                             \
@@ -895,6 +1014,11 @@ void wc_continuity(const Dev& D, const Launch& L, int precision) {
 void wc_rows(const Dev& D, const Launch& L, int mode) { BS_PLAIN(K_WC_ROWS, k_wc_rows, D, mode); }
 void wc_wall_pressure(const Dev& D, const Launch& L, int precision) {
     BS_DISPATCH(K_WC_WALLP, precision, k_wc_wallp, D);
+}
+
+void boun_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_GHOST, precision, k_boun_vel, D); }
+void ghost(const Dev& D, const Launch& L, int precision, int use_mls) {
+    BS_DISPATCH(K_GHOST, precision, k_ghost, D, use_mls);
 }
 
 }  // namespace bs

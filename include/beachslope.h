@@ -262,6 +262,24 @@ int bs_set_scene(struct bs_ctx* ctx, int32_t scene, const bs_params* params, con
  * are, so a scene joining a running batch does not perturb the others. */
 int bs_prime_scene(struct bs_ctx* ctx, int32_t scene);
 
+/* boun_vel, integrator.f90:394-457 (compiled in the reference, never
+ * called): wall and ghost particles (tid 1, 2) take minus the Shepard average
+ * of their fluid neighbours' velocity (a no-slip mirror), divided only when
+ * the Shepard sum reaches 1e-6 (single literal); vxs = vys = 0.  Uses the
+ * neighbour lists of the last bs_search. */
+int bs_boun_vel(struct bs_ctx* ctx);
+/* comp_ghost + ghost_en, mls.f90:114-263 (not compiled in the reference):
+ * the same mirror of the velocity, tke and nut onto wall and ghost particles
+ * that have neighbours, over their fluid neighbours (the module's list2 is
+ * never built; the neighbour list restricted to fluid stands in), 0 where the
+ * Shepard sum is 0.  use_mls = 1: the velocity by the module's commented-out
+ * moving-least-squares branch -- weights W (b1 + b2 dx + b3 dy) m/rho with b
+ * the first column of the inverse 3x3 moment matrix over all neighbours
+ * (Wmls, mls.f90:16-111; invertmat3D, functions.f90:134-165), the Shepard
+ * average where that determinant is below 1e-5 (single literal), which at the
+ * reference's particle sizes is every particle. */
+int bs_ghost(struct bs_ctx* ctx, int32_t use_mls);
+
 /* Set (or, with z->n = 0 and z->ncells = 0, clear) buffer zone `zone` (0 or
  * 1) of a scene; the template is copied.  entrycell1/2 of the reference. */
 int bs_set_inflow(struct bs_ctx* ctx, int32_t scene, int32_t zone, const bs_inflow* z);

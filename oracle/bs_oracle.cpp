@@ -1316,6 +1316,144 @@ void wall_pressure(or_scene* s) {
     });
 }
 
+// boun_vel, integrator.f90:394-457 (compiled, never called): wall and ghost
+// particles take minus the Shepard average of their fluid neighbours'
+// velocity, divided only when the Shepard sum reaches 1e-6 (single literal);
+// vxs = vys = 0.
+void boun_vel(or_scene* s) {
+    const double h1 = s->h;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            if (p.tid > 2) continue;
+            double t1 = 0.0;
+            p.vx = 0.0;
+            p.vy = 0.0;
+            p.vxs = 0.0;
+            p.vys = 0.0;
+            const Verlet& L = c.list[k];
+            for (int m = 0; m < L.count; ++m) {
+                const Particle& x = s->cells[L.nh[m].cell].plist[L.nh[m].slot];
+                if (x.tid != 3) continue;
+                const double w = Wab(L.dist[m], h1);
+                p.vx = p.vx - x.mass * w * x.vx / x.density;
+                p.vy = p.vy - x.mass * w * x.vy / x.density;
+                t1 = t1 + x.mass * w / x.density;
+            }
+            if (t1 >= SP_1EM6) {
+                p.vx = p.vx / t1;
+                p.vy = p.vy / t1;
+            }
+        }
+    });
+}
+
+// invertmat3D, functions.f90:134-165: adjugate over the determinant; err when
+// det < 1e-5 (single literal) or not finite
+bool invertmat3D(double a[3][3]) {
+    const double det = a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) -
+                       a[0][1] * (a[1][0] * a[2][2] - a[2][0] * a[1][2]) +
+                       a[0][2] * (a[1][0] * a[2][1] - a[2][0] * a[1][1]);
+    if (det < (double)1e-5f || !std::isfinite(det)) {
+        for (int u = 0; u < 3; ++u)
+            for (int v = 0; v < 3; ++v) a[u][v] = 0.0;
+        return true;
+    }
+    double r[3][3];
+    r[0][0] = (a[1][1] * a[2][2] - a[2][1] * a[1][2]);
+    r[1][0] = -(a[0][1] * a[2][2] - a[2][1] * a[0][2]);
+    r[2][0] = (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+    r[0][1] = -(a[1][0] * a[2][2] - a[2][0] * a[1][2]);
+    r[1][1] = (a[0][0] * a[2][2] - a[2][0] * a[0][2]);
+    r[2][1] = -(a[0][0] * a[1][2] - a[1][0] * a[0][2]);
+    r[0][2] = (a[1][0] * a[2][1] - a[2][0] * a[1][1]);
+    r[1][2] = -(a[0][0] * a[2][1] - a[2][0] * a[0][1]);
+    r[2][2] = (a[1][1] * a[0][0] - a[1][0] * a[0][1]);
+    for (int u = 0; u < 3; ++u)
+        for (int v = 0; v < 3; ++v) a[u][v] = r[u][v] / det;
+    return false;
+}
+
+// comp_ghost + ghost_en, mls.f90:114-263 (not compiled).  Wall and ghost
+// particles with neighbours take minus the Shepard average of their fluid
+// neighbours' velocity, tke and nut (list2 of the module is never built: the
+// neighbour list restricted to fluid stands in; a zero Shepard sum leaves 0
+// where the module would divide by it).  use_mls: the module's commented-out
+// moving-least-squares branch for the velocity -- weights
+// W (b1 + b2 dx + b3 dy) V with b the first column of the inverse moment
+// matrix over all neighbours (Wmls, mls.f90:16-111) -- where invertmat3D
+// succeeds, the Shepard average elsewhere.
+void ghost(or_scene* s, bool use_mls) {
+    const double h1 = s->h;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            Props& pp = c.pplist[k];
+            if (p.tid > 2) continue;
+            p.vx = 0.0;
+            p.vy = 0.0;
+            pp.tke = 0.0;
+            pp.nut = 0.0;
+            const Verlet& L = c.list[k];
+            if (L.count == 0) continue;
+            bool err = true;
+            double b[3] = {0, 0, 0};
+            if (use_mls) {
+                double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                for (int m = 0; m < L.count; ++m) {
+                    const Particle& x = s->cells[L.nh[m].cell].plist[L.nh[m].slot];
+                    const double w = Wab(L.dist[m], h1), v = x.mass / x.density;
+                    const double dx = p.x - x.x, dy = p.y - x.y;
+                    a[0][0] = a[0][0] + w * v;
+                    a[1][0] = a[1][0] + w * dx * v;
+                    a[2][0] = a[2][0] + w * dy * v;
+                    a[0][1] = a[0][1] + w * dx * v;
+                    a[1][1] = a[1][1] + w * (dx * dx) * v;
+                    a[2][1] = a[2][1] + w * dx * dy * v;
+                    a[0][2] = a[0][2] + w * dy * v;
+                    a[1][2] = a[1][2] + w * dx * dy * v;
+                    a[2][2] = a[2][2] + w * (dy * dy) * v;
+                }
+                err = invertmat3D(a);
+                if (!err) {
+                    b[0] = a[0][0];
+                    b[1] = a[1][0];
+                    b[2] = a[2][0];
+                }
+            }
+            double t1 = 0.0, te = 0.0;
+            for (int m = 0; m < L.count; ++m) {
+                const Particle& x = s->cells[L.nh[m].cell].plist[L.nh[m].slot];
+                if (x.tid != 3) continue;
+                const Props& y = s->cells[L.nh[m].cell].pplist[L.nh[m].slot];
+                const double w = Wab(L.dist[m], h1);
+                if (!err) {
+                    const double q = w * (b[0] + b[1] * (p.x - x.x) + b[2] * (p.y - x.y)) * (x.mass / x.density);
+                    p.vx = p.vx - x.vx * q;
+                    p.vy = p.vy - x.vy * q;
+                } else {
+                    p.vx = p.vx - w * x.vx * x.mass / x.density;
+                    p.vy = p.vy - w * x.vy * x.mass / x.density;
+                    t1 = t1 + x.mass * w / x.density;
+                }
+                pp.tke = pp.tke - w * y.tke * x.mass / x.density;
+                pp.nut = pp.nut - w * y.nut * x.mass / x.density;
+                te = te + x.mass * w / x.density;
+            }
+            if (err && t1 > 0.0) {
+                p.vx = p.vx / t1;
+                p.vy = p.vy / t1;
+            }
+            if (te > 0.0) {
+                pp.tke = pp.tke / te;
+                pp.nut = pp.nut / te;
+            }
+        }
+    });
+}
+
 void prime(or_scene* s) {
     resetid(s);
     neighbour(s);
@@ -1630,6 +1768,9 @@ int or_stage(or_scene* s, int32_t stage) {
         case OR_PRESSTODEN: presstoden(s); break;
         case OR_WALL_PRESSURE: wall_pressure(s); break;
         case OR_EFFPOR_KEEP: effpor(s, true); break;
+        case OR_BOUN_VEL: boun_vel(s); break;
+        case OR_GHOST: ghost(s, false); break;
+        case OR_GHOST_MLS: ghost(s, true); break;
         default: return BS_E_ARG;
     }
     return 0;

@@ -31,7 +31,10 @@ enum {
     /* wcsph.f90 */
     OR_CALMASSCONS, OR_UPDATEDEN, OR_DENTOPRESS, OR_PRESSTODEN,
     OR_WALL_PRESSURE,   /* the WCSPH step's wall rule (no reference counterpart) */
-    OR_EFFPOR_KEEP      /* effpor without its density write (WCSPH step)        */
+    OR_EFFPOR_KEEP,     /* effpor without its density write (WCSPH step)        */
+    OR_BOUN_VEL,        /* boun_vel, integrator.f90:394-457 (never called)      */
+    OR_GHOST,           /* comp_ghost + ghost_en, mls.f90:114-263 (Shepard)     */
+    OR_GHOST_MLS        /* the same with the MLS branch for the velocity        */
 };
 
 or_scene* or_create(const bs_params* p, const bs_state* st, const bs_grains* gr);
