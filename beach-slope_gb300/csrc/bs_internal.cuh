@@ -228,6 +228,18 @@ __device__ __forceinline__ void fast_r64(double s, double& r, double& ir) {
     ir = y;
     r = s * y;
 }
+// Compensated FP32 sum (Neumaier's variant of Kahan summation): the running
+// error term keeps the sum of n terms within ~1 ulp instead of ~n/2 ulp.
+struct Kahan32 {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = __fadd_rn(s, x);
+        c = __fadd_rn(c, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x) : __fadd_rn(__fsub_rn(x, t), s));
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // 1/d in FP64 from an FP32 reciprocal seed and one Newton step (~1e-14)
 __device__ __forceinline__ double fast_rcp64(double d) {
     double y = (double)__frcp_rn((float)d);

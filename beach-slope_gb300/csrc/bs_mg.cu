@@ -173,6 +173,26 @@ __global__ void k_mg_galc(Dev D, int l) {
 // the half-cells: r1[h] = sum_{i in h} (in_i - (A0 z0)_i).  One warp per
 // cell, four sums (one per quadrant); every half-cell is written, empty
 // ones with 0.
+// sum over the row's off-diagonal nonzeros of A * u (sliced ELL), four
+// independent index/value loads in flight before the gathers
+template <typename T>
+__device__ __forceinline__ T ell_dot(const T* __restrict__ A, const int* __restrict__ idx,
+                                     const T* __restrict__ u, int r, int n, int kmax, T acc) {
+    long e = ell(r, 0, kmax);
+    int k = 0;
+    for (; k + 4 <= n; k += 4, e += 128) {
+        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32), j2 = __ldg(idx + e + 64), j3 = __ldg(idx + e + 96);
+        const T a0 = __ldg(A + e), a1 = __ldg(A + e + 32), a2 = __ldg(A + e + 64), a3 = __ldg(A + e + 96);
+        const T u0 = u[j0], u1 = u[j1], u2 = u[j2], u3 = u[j3];
+        acc += a0 * u0;
+        acc += a1 * u1;
+        acc += a2 * u2;
+        acc += a3 * u3;
+    }
+    for (; k < n; ++k, e += 32) acc += __ldg(A + e) * u[__ldg(idx + e)];
+    return acc;
+}
+
 template <typename T>
 __global__ void k_mg_l0_down(Dev D) {
     BS_PDL_ENTRY();
@@ -191,13 +211,7 @@ __global__ void k_mg_l0_down(Dev D) {
     T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
     for (int r = r0 + lane; r < r1; r += 32) {
         T v = xin[r];
-        if (D.mg.pre0) {
-            T ax = ad[r] * u[r];
-            const int n = D.ncount[r];
-            long e = ell(r, 0, D.kmax);
-            for (int k = 0; k < n; ++k, e += 32) ax += __ldg(A + e) * u[__ldg(idx + e)];
-            v -= ax;
-        }
+        if (D.mg.pre0) v -= ell_dot<T>(A, idx, u, r, D.ncount[r], D.kmax, ad[r] * u[r]);
         const int t = sub[r];
         q0 += (t == 0) ? v : (T)0;
         q1 += (t == 1) ? v : (T)0;
@@ -436,17 +450,7 @@ __global__ void k_mg_l0_up(Dev D, double* __restrict__ out) {
     const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
     const int* __restrict__ idx = D.nidx;
     const T zr = zz[r];
-    T ax = ((const T*)D.mg.adiagT)[r] * zr;
-    const int n = D.ncount[r];
-    long e = ell(r, 0, D.kmax);
-    int k = 0;
-    for (; k + 2 <= n; k += 2, e += 64) {
-        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32);
-        const T a0 = __ldg(A + e), a1 = __ldg(A + e + 32);
-        ax += a0 * zz[j0];
-        ax += a1 * zz[j1];
-    }
-    if (k < n) ax += __ldg(A + e) * zz[__ldg(idx + e)];
+    const T ax = ell_dot<T>(A, idx, zz, r, D.ncount[r], D.kmax, ((const T*)D.mg.adiagT)[r] * zr);
     const T x = ((const T*)D.mg.xin)[r];
     out[r] = (double)(zr + (T)D.mg.omega * ((const T*)D.mg.dinv0)[r] * (x - ax));
 }

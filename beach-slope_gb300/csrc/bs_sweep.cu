@@ -148,7 +148,51 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         // Phase 2 (uniform over the accepted neighbours): pair quantities and
         // the gradient-correction sums (search.f90:61-85).
         double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
-        for (int k = 0; k < n; ++k) {
+        if (sizeof(T) == 4) {
+            // mixed: the pair quantities are stored in FP32.  r, 1/r and
+            // 2 - r/h come from FP64 (offsets exact, Newton square root): near
+            // the cut-off the kernel gradient goes as (2 - r/h)^2 and an FP32
+            // r would put errors of 1e-4 relative into it; the rest of the
+            // pair math is FP32 (the FP64 pipe of this part is the search's
+            // bound).  The correction sums are compensated FP32 sums.
+            Kahan32 f00, f01, f10, f11;
+            const float ihf = (float)P.inv_h, ih2f = (float)P.inv_h2, ih3f = (float)P.inv_h3;
+            const float c1f = (float)P.cn1, c2f = (float)P.cn2;
+            for (int k = 0; k < n; ++k) {
+                const long e = ell(r, k, kmax);
+                const int rj = D.nidx[e];
+                const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
+                const double s2d = dx * dx + dy * dy;
+                double radd, ird;
+                fast_r64(s2d, radd, ird);
+                const float fx = (float)dx, fy = (float)dy;
+                const float rad = (float)radd, ir = (float)ird;
+                const float rinv = __frcp_rn((float)s2d + (float)P.lam);
+                float F;
+                if (radd < P.h) {
+                    F = c1f * (9.0f * rad * ih3f - 12.0f * ih2f) + c2f * (3.0f * rad * ih3f - 6.0f * ihf * ir);
+                } else {
+                    const float a = (float)(2.0 - radd * P.inv_h);
+                    F = -(c1f + c2f) * (3.0f * ihf * ir) * a * a;
+                }
+                const float kx = F * (-fx), ky = F * (-fy);
+                st<T>(D.ndist, e, (T)rad);
+                st<T>(D.nrinv, e, (T)rinv);
+                st<T>(D.nkx, e, (T)kx);
+                st<T>(D.nky, e, (T)ky);
+                const float vj = (float)D.vol[rj];
+                const float res1 = vj * fx, res3 = vj * fy;
+                f00.add(kx * res1);
+                f01.add(ky * res1);
+                f10.add(kx * res3);
+                f11.add(ky * res3);
+            }
+            a00 = f00.value();
+            a01 = f01.value();
+            a10 = f10.value();
+            a11 = f11.value();
+        }
+        for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
             const long e = ell(r, k, kmax);
             const int rj = D.nidx[e];
             const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
@@ -217,6 +261,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 else if (own_q == 1) { ord[0] = cc[1]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[3]; }
                 else { ord[0] = cc[3]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[1]; }
                 const double wsolid = 1.0 - P.por * 1.0;
+                const float wsf = (float)wsolid, t2c = (float)(P.twoh * P.twoh);
+                Kahan32 sff;
                 const float t2f = (float)(P.twoh * P.twoh) * (1.0f + 1e-5f);
                 const float xri = D.xr[r], yri = D.yr[r];
                 for (int q = 0; q < 4; ++q) {
@@ -229,12 +275,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                         const float fx = (__ldg(D.gxr + g) + ox) - xri, fy = (__ldg(D.gyr + g) + oy) - yri;
                         if (fx * fx + fy * fy > t2f) continue;
                         const double dx = xi - D.gx[g], dy = yi - D.gy[g];
-                        if (sizeof(T) == 4) {   // mixed: Newton sqrt (W(2h) = 0: the cut needs no exact test)
-                            const double s2 = dx * dx + dy * dy;
-                            if (s2 < P.twoh * P.twoh) {
-                                double rad = 0.0, ir;   // grains may coincide with pore particles
-                                if (s2 > 0.0) fast_r64(s2, rad, ir);
-                                sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
+                        if (sizeof(T) == 4) {   // mixed: FP32 (W(2h) = 0: the cut needs no exact test)
+                            const float ex = (float)dx, ey = (float)dy;
+                            const float s2 = ex * ex + ey * ey;
+                            if (s2 < t2c) {
+                                float rad = 0.0f;   // grains may coincide with pore particles
+                                if (s2 > 0.0f) {
+                                    float ir = rsqrtf(s2);
+                                    ir = ir * (1.5f - 0.5f * s2 * ir * ir);
+                                    rad = s2 * ir;
+                                }
+                                sff.add(wsf * bs_Wf(rad, P) * (float)D.gv[g]);
                             }
                         } else {
                             const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
@@ -242,6 +293,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                         }
                     }
                 }
+                if (sizeof(T) == 4) sf = sff.value();
             }
             if (sf > (1.0 - P.por)) sf = 1.0 - P.por;
             phi = 1.0 - sf;
