@@ -471,6 +471,24 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
 // ------------------------------------------------------------- assembly
 // ppesolve, isph.f90:136-444: rows in the neighbour-list order (ascending
 // row = matid, so already column-sorted as after qsort), Jacobi-scaled.
+// Per-particle quotients of the assembly (FP64 division is the costly
+// operation on this part): sr = rho/phi, srhat = vxs/phi, sp = vys/phi,
+// sxd = 1/phi (solver scratch vectors, free until the solve)
+__global__ void k_asm_prep(Dev D) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    const double ip = 1.0 / D.por[r];
+    D.sr[r] = D.rho[r] * ip;
+    D.srhat[r] = D.vxs[r] * ip;
+    D.sp[r] = D.vys[r] * ip;
+    D.sxd[r] = ip;
+}
+
+// ppesolve assembly (isph.f90:115-456) with the quotients of k_asm_prep:
+// rho_ij = 2 a_j a_i / (a_j + a_i) with a = rho/phi, the velocity terms as
+// rho_ij (vxs_j/phi_j - vxs_i/phi_i) -- the reference's expressions
+// regrouped, one division per fluid pair
 template <typename T>
 __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     const RowCtx R = row_ctx(D);
@@ -479,11 +497,14 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     const int r = R.r;
     const int ti = D.tid[r];
     const uint8_t fl = D.flags[r];
-    const double dt = D.dyn[R.s].dt;
+    const double idt = 1.0 / D.dyn[R.s].dt;
     const double xi = D.x[r], yi = D.y[r];
-    const double rhoi = D.rho[r], phii = D.por[r];
-    const double rho_i = rhoi * (1.0 / phii);
-    const double vxsi = D.vxs[r], vysi = D.vys[r], mi = D.mass[r];
+    const double rhoi = D.rho[r];
+    const double ai = D.sr[r], ipi = D.sxd[r];          // rho_i/phi_i, 1/phi_i
+    const double wxi = D.srhat[r], wyi = D.sp[r];       // vxs_i/phi_i, vys_i/phi_i
+    const double bi = ai * ipi;                         // rho_i/phi_i^2
+    const double vxsi = D.vxs[r], vysi = D.vys[r];
+    const double voli = D.mass[r] / rhoi;
     const double c0 = D.c0[r], c1 = D.c1[r], c2 = D.c2[r], c3 = D.c3[r];
     const bool freei = fl & BS_FLAG_FREE;
     const double lampf = 1.0 / (P.rho * P.rel_den);
@@ -505,18 +526,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
             const double t12 = 2 * pvol * (Lx * dxi + Ly * dyi) * pd;
             off = -t12;
             dia += t12 * lamp;
-            const double phij = D.por[j];
             double ax, ay;
             if (tj == BS_TID_FLUID) {
-                const double rhoj = D.rho[j];
-                const double rho_ij = 2 * rhoj * rhoi * (1.0 / (phij * phii)) * (1.0 / ((rhoj / phij) + (rhoi / phii)));
-                ax = D.vxs[j] * rho_ij / phij - vxsi * rho_ij / phii;
-                ay = D.vys[j] * rho_ij / phij - vysi * rho_ij / phii;
+                const double aj = D.sr[j];
+                const double rho_ij = 2 * aj * ai / (aj + ai);
+                ax = rho_ij * (D.srhat[j] - wxi);
+                ay = rho_ij * (D.sp[j] - wyi);
             } else {
-                ax = D.vxs[j] * rho_i / phii - vxsi * rho_i / phii;
-                ay = D.vys[j] * rho_i / phii - vysi * rho_i / phii;
+                ax = bi * (D.vxs[j] - vxsi);
+                ay = bi * (D.vys[j] - vysi);
             }
-            fv += (pvol * (ax * Lx + ay * Ly)) / dt;
+            fv += (pvol * (ax * Lx + ay * Ly)) * idt;
         } else if (ti == BS_TID_GHOST) {
             if (tj <= 2) {
                 const double t12 = 2 * D.vol[j] * (z1 * dxi + z2 * dyi) * pd;
@@ -527,14 +547,13 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
             if (tj == BS_TID_FLUID) {
                 const double d0 = D.c0[j], d1 = D.c1[j], d2 = D.c2[j], d3 = D.c3[j];
                 const double Lx = d0 * z1 + d1 * z2, Ly = d2 * z1 + d3 * z2;
-                const double t12 = 2 * mi * (Lx * dxi + Ly * dyi) * pd / rhoi;
+                const double t12 = 2 * voli * (Lx * dxi + Ly * dyi) * pd;
                 off = -t12;
                 dia += t12;
-                const double phij = D.por[j];
-                const double rho_j = D.rho[j] * (1.0 / phij);
-                const double ax = D.vxs[j] * rho_j / phij - vxsi * rho_j / phii;
-                const double ay = D.vys[j] * rho_j / phij - vysi * rho_j / phii;
-                fv += (mi * (ax * Lx + ay * Ly)) / rhoi / dt;
+                const double aj = D.sr[j];
+                const double ax = aj * (D.srhat[j] - vxsi * ipi);
+                const double ay = aj * (D.sp[j] - vysi * ipi);
+                fv += (voli * (ax * Lx + ay * Ly)) * idt;
             } else {
                 const double t12 = 2 * D.vol[j] * (z1 * dxi + z2 * dyi) * pd;
                 off = -t12;
@@ -546,21 +565,20 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     // Jacobi scaling (isph.f90:432-440).  A ghost row whose first neighbour
     // is a lower-numbered fluid particle keeps the row initialiser's
     // val(1)=1.0 at col=row (isph.f90:125-128): an extra 1/dia on the diagonal.
-    const double inv = 1.0 / dia;
     double extra = 0.0;
     if (ti == BS_TID_GHOST && n > 0) {
         const int j0 = D.nidx[ell(r, 0, kmax)];
         if (j0 < r && D.tid[j0] == BS_TID_FLUID) extra = 1.0;
     }
     if (!(dia != 0.0) || !isfinite(dia)) set_err(D, R.s, BS_ERR_ZERO_DIAG);
-    D.adiag[r] = dia / dia + extra / dia;
-    D.rhs[r] = fv / dia;
+    const double inv = 1.0 / dia;
+    D.adiag[r] = dia / dia + extra * inv;
+    D.rhs[r] = fv * inv;
+    double* a = (double*)D.aval;
     for (int k = 0; k < n; ++k) {
         const long e = ell(r, k, kmax);
-        double* a = (double*)D.aval;
-        a[e] = a[e] / dia;
+        a[e] = a[e] * inv;
     }
-    (void)inv;
 }
 
 // ---------------------------------------------------- comp_vel + comp_pos
@@ -1046,7 +1064,10 @@ void eddy(const Dev& D, const Launch& L, int precision, int with_eddy, int with_
     BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_eddy, with_varts, with_disp);
 }
 void int_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_INTVEL, precision, k_intvel, D); }
-void assemble(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D); }
+void assemble(const Dev& D, const Launch& L, int precision) {
+    BS_PLAIN(K_ASSEMBLE, k_asm_prep, D);
+    BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D);
+}
 void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_pos) {
     BS_DISPATCH(K_COMPVEL, precision, k_compvel, D, do_vel, do_pos);
 }
