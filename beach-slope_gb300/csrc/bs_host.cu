@@ -435,6 +435,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(por, R); A(resx, R); A(resy, R); A(nut, R); A(tke, R); A(varts, R); A(gradvx, R); A(vel, R); A(cdiff, R);
     A(c0, R); A(c1, R); A(c2, R); A(c3, R); A(Dp0, R); A(Dp1, R); A(Dp2, R); A(Dp3, R); A(Dt, R);
     A(rho_new, R); A(vol_new, R); A(con_new, R); A(tden, R); A(whyd, R);
+    A(qa, R); A(qu, R); A(qw, R); A(qi, R);
     A(ncount, R); A(nidx, E);
     A(adiag, R); A(rhs, R);
     A(sr, R); A(srhat, R); A(sp, R); A(sp2, R); A(sv, R); A(sv2, R); A(ss, R); A(st, R); A(sxd, R);

@@ -133,6 +133,7 @@ struct Dev {
     double *Dp0, *Dp1, *Dp2, *Dp3, *Dt;   // scalar dispersion per particle
     double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
     double *tden, *whyd;            // WCSPH: continuity density, hydrostatic Tait density per row
+    double *qa, *qu, *qw, *qi;      // per-row quotients of the sweeps (k_quot): rho/phi, u/phi, w/phi, 1/phi
     double *con_new;
     // neighbour lists (ELL)
     int* ncount;

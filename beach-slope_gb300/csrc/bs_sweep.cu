@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
     const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
     const double phi = D.por[r];
     const double vx = D.vx[r], vy = D.vy[r];
-    const T ui = (T)(vx / phi), wi = (T)(vy / phi);
+    const T ui = (T)D.qu[r], wi = (T)D.qw[r];   // vx/phi, vy/phi (k_quot)
     T t1 = 0, t2 = 0, t3 = 0;
     const int n = D.ncount[r];
     const int kmax = D.kmax;
@@ -366,8 +366,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
         const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
-        const double pj = D.por[j];
-        const T a = (T)(D.vx[j] / pj) - ui, b = (T)(D.vy[j] / pj) - wi;
+        const T a = (T)D.qu[j] - ui, b = (T)D.qw[j] - wi;
         const T V = (T)D.vol[j];
         const T Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
         t1 += V * a * Lx;
@@ -433,9 +432,9 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
         const T pd = ld<T>(D.nrinv, e);
         const int tj = D.tid[j];
         T cmu;
-        if (tj == BS_TID_FLUID) {
-            const double nuj = D.nu[j];
-            cmu = (T)(2.0 * nui * nuj / (nui + nuj));
+        if (tj == BS_TID_FLUID) {   // harmonic mean (FP32 in the mixed form)
+            const T nuj = (T)D.nu[j];
+            cmu = (T)2 * (T)nui * nuj / ((T)nui + nuj);
         } else {
             cmu = (T)nui;
         }
@@ -453,7 +452,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
             const double nutj = D.nut[j];
             T mix;
             if ((nuti < BS_SP1EM6) && (nutj < BS_SP1EM6)) mix = (T)((nuti + nutj) * 0.50);
-            else mix = (T)((2 * nuti * nutj) / (nuti + nutj));
+            else mix = ((T)2 * (T)nuti * (T)nutj) / ((T)nuti + (T)nutj);
             sx += ax * mix;
             sy += ay * mix;
         }
@@ -471,21 +470,33 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
 // ------------------------------------------------------------- assembly
 // ppesolve, isph.f90:136-444: rows in the neighbour-list order (ascending
 // row = matid, so already column-sorted as after qsort), Jacobi-scaled.
-// Per-particle quotients of the assembly (FP64 division is the costly
-// operation on this part): sr = rho/phi, srhat = vxs/phi, sp = vys/phi,
-// sxd = 1/phi (solver scratch vectors, free until the solve)
-__global__ void k_asm_prep(Dev D) {
+// Per-particle quotients of the neighbour sweeps (FP64 division is the
+// costly operation on this part; one division per particle instead of one
+// or more per pair).  mode 0 (assembly): qa = rho/phi, qu = vxs/phi,
+// qw = vys/phi, qi = 1/phi; mode 1 (eddyvis): qu = vx/phi, qw = vy/phi;
+// mode 2 (comp_vel): qa = rho/phi.
+__global__ void k_quot(Dev D, int mode) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
     const int r = R.r;
-    const double ip = 1.0 / D.por[r];
-    D.sr[r] = D.rho[r] * ip;
-    D.srhat[r] = D.vxs[r] * ip;
-    D.sp[r] = D.vys[r] * ip;
-    D.sxd[r] = ip;
+    const double phi = D.por[r];
+    if (mode == 1) {
+        D.qu[r] = D.vx[r] / phi;
+        D.qw[r] = D.vy[r] / phi;
+        return;
+    }
+    if (mode == 2) {
+        D.qa[r] = D.rho[r] / phi;
+        return;
+    }
+    const double ip = 1.0 / phi;
+    D.qa[r] = D.rho[r] * ip;
+    D.qu[r] = D.vxs[r] * ip;
+    D.qw[r] = D.vys[r] * ip;
+    D.qi[r] = ip;
 }
 
-// ppesolve assembly (isph.f90:115-456) with the quotients of k_asm_prep:
+// ppesolve assembly (isph.f90:115-456) with the quotients of k_quot:
 // rho_ij = 2 a_j a_i / (a_j + a_i) with a = rho/phi, the velocity terms as
 // rho_ij (vxs_j/phi_j - vxs_i/phi_i) -- the reference's expressions
 // regrouped, one division per fluid pair
@@ -500,8 +511,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     const double idt = 1.0 / D.dyn[R.s].dt;
     const double xi = D.x[r], yi = D.y[r];
     const double rhoi = D.rho[r];
-    const double ai = D.sr[r], ipi = D.sxd[r];          // rho_i/phi_i, 1/phi_i
-    const double wxi = D.srhat[r], wyi = D.sp[r];       // vxs_i/phi_i, vys_i/phi_i
+    const double ai = D.qa[r], ipi = D.qi[r];           // rho_i/phi_i, 1/phi_i
+    const double wxi = D.qu[r], wyi = D.qw[r];          // vxs_i/phi_i, vys_i/phi_i
     const double bi = ai * ipi;                         // rho_i/phi_i^2
     const double vxsi = D.vxs[r], vysi = D.vys[r];
     const double voli = D.mass[r] / rhoi;
@@ -528,10 +539,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
             dia += t12 * lamp;
             double ax, ay;
             if (tj == BS_TID_FLUID) {
-                const double aj = D.sr[j];
+                const double aj = D.qa[j];
                 const double rho_ij = 2 * aj * ai / (aj + ai);
-                ax = rho_ij * (D.srhat[j] - wxi);
-                ay = rho_ij * (D.sp[j] - wyi);
+                ax = rho_ij * (D.qu[j] - wxi);
+                ay = rho_ij * (D.qw[j] - wyi);
             } else {
                 ax = bi * (D.vxs[j] - vxsi);
                 ay = bi * (D.vys[j] - vysi);
@@ -550,9 +561,9 @@ __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
                 const double t12 = 2 * voli * (Lx * dxi + Ly * dyi) * pd;
                 off = -t12;
                 dia += t12;
-                const double aj = D.sr[j];
-                const double ax = aj * (D.srhat[j] - vxsi * ipi);
-                const double ay = aj * (D.sp[j] - vysi * ipi);
+                const double aj = D.qa[j];
+                const double ax = aj * (D.qu[j] - vxsi * ipi);
+                const double ay = aj * (D.qw[j] - vysi * ipi);
                 fv += (voli * (ax * Lx + ay * Ly)) * idt;
             } else {
                 const double t12 = 2 * D.vol[j] * (z1 * dxi + z2 * dyi) * pd;
@@ -598,6 +609,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
         if (ti == BS_TID_FLUID && !(fl & BS_FLAG_BUFFER)) {
             const T c0 = (T)D.c0[r], c1 = (T)D.c1[r], c2 = (T)D.c2[r], c3 = (T)D.c3[r];
             const double pi = D.p[r], rhoi = D.rho[r];
+            const double ai = D.qa[r];   // rho_i/phi_i (k_quot)
+            const double qf = 2.0 * (phi * phi) / rhoi;
             const T phi2 = (T)(phi * phi);
             T ax = 0, ay = 0;
             const int n = D.ncount[r];
@@ -610,9 +623,9 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
                 const double pj = D.p[j];
                 T q;
                 if (D.tid[j] == BS_TID_FLUID) {
-                    const double rhoj = D.rho[j], phij = D.por[j];
-                    q = (T)(2.0 * D.vol[j] * (phi * phi) * ((pj * rhoi / phi) + (pi * rhoj / phij)) /
-                            ((rhoi) * ((rhoi / phi) + (rhoj / phij))));
+                    // 2 V_j phi_i^2 (p_j rho_i/phi_i + p_i rho_j/phi_j) / (rho_i (rho_i/phi_i + rho_j/phi_j))
+                    const double aj = D.qa[j];
+                    q = (T)(qf * D.vol[j] * (pj * ai + pi * aj) / (ai + aj));
                 } else {
                     q = (T)D.vol[j] * phi2 * (T)(pj + pi) / (T)rhoi;
                 }
@@ -774,7 +787,43 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep) {
     double cd = 0.0;
     const int n = D.ncount[r];
     const int kmax = D.kmax;
-    for (int k = 0; k < n; ++k) {
+    if (sizeof(T) == 4) {
+        // mixed: the pair terms in FP32 from the FP32-stored pair data (the
+        // porosity thresholds on the FP64 values), summed in FP32
+        const float capf = (float)cap, ovf = (float)ovoli, phif = (float)phii, cof = (float)coni;
+        const float P0 = (float)Pi0, P1 = (float)Pi1, P2 = (float)Pi2, P3 = (float)Pi3, Dtf = (float)Dti;
+        const bool nsmall = nuti < BS_SP1EM6;
+        float cdf = 0.0f;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, kmax);
+            const int j = D.nidx[e];
+            if (D.tid[j] != BS_TID_FLUID) continue;
+            const double phij = D.por[j];
+            const float pj = (float)phij;
+            const float dm = (float)ld<T>(D.ndist, e);
+            const float dx = (float)(xi - D.x[j]), dy = (float)(yi - D.y[j]);
+            float t1x;
+            if ((phii < thr) && (phij < thr)) {
+                const float Dxx = P0 + (float)D.Dp0[j], Dxy = P1 + (float)D.Dp1[j];
+                const float Dyx = P2 + (float)D.Dp2[j], Dyy = P3 + (float)D.Dp3[j];
+                const float ph = 0.5f / dm;
+                const float A = Dxx * dx * ph + Dxy * dy * ph, B = Dyx * dx * ph + Dyy * dy * ph;
+                t1x = 1.0f / (A * A + B * B);
+                t1x = (t1x <= capf) ? t1x : capf;
+            } else {
+                const float Dj = (float)D.Dt[j];
+                if (nsmall && (D.nut[j] < BS_SP1EM6)) t1x = (Dtf + Dj) * 0.5f;
+                else t1x = 2.0f * Dtf * Dj / (Dtf + Dj);
+            }
+            const float t3 = ovf * (phif + pj) / (phif * pj);
+            const float F = bs_Ff(dm, P);
+            const float pd = (float)ld<T>(D.nrinv, e);
+            const float dc = cof - (float)D.con[j];
+            cdf += t1x * t3 * dc * (dx * (F * dx) + dy * (F * dy)) * pd;
+        }
+        cd = cdf;
+    }
+    for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
         if (D.tid[j] != BS_TID_FLUID) continue;
@@ -1061,14 +1110,16 @@ void search(const Dev& D, const Launch& L, int precision, int do_search, int do_
 }
 void freesurf(const Dev& D, const Launch& L) { BS_PLAIN(K_FREESURF, k_freesurf, D); }
 void eddy(const Dev& D, const Launch& L, int precision, int with_eddy, int with_varts, int with_disp) {
+    BS_PLAIN(K_EDDY, k_quot, D, 1);
     BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_eddy, with_varts, with_disp);
 }
 void int_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_INTVEL, precision, k_intvel, D); }
 void assemble(const Dev& D, const Launch& L, int precision) {
-    BS_PLAIN(K_ASSEMBLE, k_asm_prep, D);
+    BS_PLAIN(K_ASSEMBLE, k_quot, D, 0);
     BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D);
 }
 void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_pos) {
+    if (do_vel) BS_PLAIN(K_COMPVEL, k_quot, D, 2);
     BS_DISPATCH(K_COMPVEL, precision, k_compvel, D, do_vel, do_pos);
 }
 void shift(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_SHIFT, precision, k_shift, D); }
