@@ -58,6 +58,8 @@ struct bs_ctx {
     std::vector<std::array<Zone, 2>> zones;
     bool any_zone = false;
     std::vector<SceneDyn> hdyn;   // host copy of the scenes' dynamic state (schedule of the zones)
+    // multigrid levels run as one clustered launch per visit (mg_sub option)
+    int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
 };
 
 namespace {
@@ -146,6 +148,8 @@ bs::Launch launch_of(bs_ctx* c) {
     L.graph = &c->graph;
     L.mglev = c->mglev.empty() ? nullptr : c->mglev.data();
     L.mgneed = c->mgneed.empty() ? nullptr : c->mgneed.data();
+    L.mgsub_level = c->mgsub_level;
+    L.mgsub_cs = c->mgsub_cs;
     return L;
 }
 
@@ -162,6 +166,42 @@ std::vector<std::pair<int, int>> mg_dims_of(int cellx, int celly) {
         d.push_back({nx, ny});
     }
     return d;
+}
+
+// Operations of one visit of level l (the recursion of the cycle)
+int mg_sub_nops(const bs_ctx* c, int l) {
+    const unsigned char need = c->mgneed[l];
+    if (!(need & 1)) return 0;
+    int n = (need & 4) ? 1 : 0;
+    if (!(need & 2)) return n;
+    n += 2 + mg_sub_nops(c, l + 1);
+    if (l <= c->D.mg.wlev) n += 1 + mg_sub_nops(c, l + 1);
+    return n;
+}
+
+// First level from which the cycle runs as one clustered launch: the
+// shallowest level whose largest scene fits one cluster of up to 16 blocks
+// of 1024 threads (a cell per thread), all scenes' clusters fit on the SMs at
+// once, the levels below fit the launch's tables and the visit's op list its
+// array; 0 when there is none (or the option is off).
+void mg_sub_choose(bs_ctx* c) {
+    c->mgsub_level = 0;
+    c->mgsub_cs = 1;
+    const MgDev& M = c->D.mg;
+    if (!c->mgsub_on || c->mglev.empty() || M.nlev < 1) return;
+    for (int l = 1; l <= M.nlev; ++l) {
+        if (!(c->mgneed[l] & 1)) break;
+        int mx = 0;
+        for (int s = 0; s < c->nscene; ++s) mx = std::max(mx, c->mglev[l].nx[s] * c->mglev[l].ny[s]);
+        const int cs = std::max(1, (mx + 1023) / 1024);
+        if (cs > 16 || (long)cs * c->nscene > c->sm_count) continue;
+        if (M.nlev - l + 1 > BS_MG_SUBL || mg_sub_nops(c, l) > BS_MG_MAXOPS) continue;
+        const size_t smem = 2 * (size_t)M.coarse_max * (c->precision == BS_PREC_MIXED ? sizeof(float) : sizeof(double));
+        if (bs::mg_sub_max_clusters(c->precision, cs, smem) < 1) continue;
+        c->mgsub_level = l;
+        c->mgsub_cs = cs;
+        return;
+    }
 }
 
 // Level tables (kernel arguments), the launches each level needs, and the
@@ -196,6 +236,7 @@ void mg_tables(bs_ctx* c) {
         cudaMemcpy((void*)M.ny[l], nyv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
     }
     for (int s = 0; s < ns; ++s) c->hpar[s].mg_lev = (int)c->mgdims[s].size();
+    mg_sub_choose(c);
 }
 
 // per-scene constants that do not depend on the layout
@@ -380,6 +421,12 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     if (nscenes > BS_MG_MAXS) return BS_E_CAPACITY;   // multigrid level tables hold BS_MG_MAXS scenes
     bs_ctx* ctx = new bs_ctx();
     ctx->nscene = nscenes;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, dev);
+        cudaGetLastError();
+    }
     ctx->prm.assign(params, params + nscenes);
     ctx->zones.resize(nscenes);
     ctx->precision = params[0].precision;
@@ -892,6 +939,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
     else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
+    else if (k == "mg_sub" && (value == 0 || value == 1)) ctx->mgsub_on = (int)value;
     else if (k == "ppe_solver" && (value == BS_SOLVER_BICGSTAB || value == BS_SOLVER_FGMRES))
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
@@ -899,6 +947,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
     if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
         if (int rc = fg_ensure(ctx)) return rc;
+    mg_sub_choose(ctx);   // the W depth changes the visits' op lists
     ctx->graph.valid = false;   // the captured iteration holds the old values
     return 0;
 }
@@ -916,6 +965,8 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "mg_levels") *value = M.nlev;
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
     else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;
+    else if (k == "mg_sub") *value = ctx->mgsub_on;
+    else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
     else return BS_E_ARG;
     return 0;

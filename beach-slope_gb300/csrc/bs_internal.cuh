@@ -335,7 +335,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_MG_SUB, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -356,6 +356,16 @@ struct IterGraph {
     int64_t nkernels = 0;
     bool valid = false;
 };
+// The multigrid levels from `l0` down as one clustered launch per visit:
+// the op list of the visit (built on the host from the cycle's recursion)
+// and the tables of the levels it touches.
+#define BS_MG_SUBL 8
+#define BS_MG_MAXOPS 128
+struct MgSub {
+    int l0, nops;
+    unsigned char op[BS_MG_MAXOPS], lv[BS_MG_MAXOPS], acc[BS_MG_MAXOPS];   // op: 0 down, 1 resid, 2 up, 3 coarse
+    MgLevel G[BS_MG_SUBL];           // levels l0 .. l0 + BS_MG_SUBL - 1
+};
 struct Launch {
     cudaStream_t stream;
     int nblk_rows;      // total row blocks
@@ -366,6 +376,7 @@ struct Launch {
     const MgLevel* mglev;          // host tables of the multigrid levels, indexed by level
     const unsigned char* mgneed;   // per level: bit0 some scene visits it, bit1 restriction and
                                    // prolongation to the next level, bit2 coarsest-level solve
+    int mgsub_level, mgsub_cs;     // first level of the clustered subtree (0: per-level launches), CTAs per cluster
 };
 // Programmatic dependent launch: a kernel launched by launch_pdl may be
 // scheduled while its predecessor in the stream still runs.  Its first
@@ -451,6 +462,7 @@ struct ZoneDev {
     int remove_side, zone;
 };
 void buffer_exchange(const Dev& D, const Launch& L, int s, const ScenePar& P, const ZoneDev& Z);
+int mg_sub_max_clusters(int mg_precision, int cs, size_t smem);
 void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
                   int* d_nconv, int* h_nconv, cudaEvent_t ev);
 // per-scene small FGMRES storage for restart length m (doubles)

@@ -437,6 +437,60 @@ __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
     op_coarse<T>(D.mg, view_of(F, k), acc, (T*)smem);
 }
 
+// ---- the levels from l0 down in one launch: one thread-block cluster per
+// scene (cluster rank r, nt threads over the cluster, one cell per thread
+// on the first level), the visit's level operations in order, a cluster
+// barrier (release / acquire: the level arrays in global memory, L2
+// resident) between them in place of a kernel boundary.  The coarsest-level
+// solve runs in the cluster's first block.  Every thread reaches every
+// barrier (no early exit).
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_size() {
+    unsigned n;
+    asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+    return n;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_sub(Dev D, __grid_constant__ const MgSub S) {
+    BS_PDL_ENTRY();
+    extern __shared__ unsigned char smem[];
+    const int cs = (int)cluster_size();
+    const int k = blockIdx.x / cs, rank = blockIdx.x % cs;
+    const int t = rank * blockDim.x + threadIdx.x, nt = cs * blockDim.x;
+    for (int o = 0; o < S.nops; ++o) {
+        const int l = S.lv[o];
+        const MgLevel& F = S.G[l - S.l0];
+        const LevelS f = view_of(F, k);
+        switch (S.op[o]) {
+            case 0: {   // down l -> l+1
+                const LevelS c = view_of(S.G[l + 1 - S.l0], k);
+                const int m = c.nx * c.ny;
+                for (int q = t; q < m; q += nt) op_down<T>(D.mg, f, c, q);
+                break;
+            }
+            case 1: {   // residual on l
+                const int m = f.nx * f.ny;
+                for (int q = t; q < m; q += nt) op_resid<T>(D.mg, f, q);
+                break;
+            }
+            case 2: {   // up l+1 -> l (the coarse solve wrote the scene's coarsest level)
+                if (l >= F.lev[k]) break;
+                const LevelS c = view_of(S.G[l + 1 - S.l0], k);
+                const int m = f.nx * f.ny;
+                for (int q = t; q < m; q += nt) op_up<T>(D.mg, f, c, S.acc[o], q);
+                break;
+            }
+            default:   // coarsest-level solve of the scenes whose coarsest level is l
+                if (rank == 0 && F.lev[k] == l) op_coarse<T>(D.mg, f, S.acc[o], (T*)smem);
+                break;
+        }
+        cluster_sync_all();
+    }
+}
+
 // Level 0 post-sweep after the prolongation; writes the preconditioned
 // vector (FP64).
 template <typename T>
@@ -471,15 +525,64 @@ void setup_t(const Dev& D, const Launch& L) {
     }
 }
 
+// op list of one visit of level l (the recursion of cycle_t)
+void sub_ops(const Dev& D, const Launch& L, int l, int acc, MgSub& S) {
+    const unsigned char need = L.mgneed[l];
+    if (!(need & 1)) return;
+    auto push = [&](int op, int lv, int a) {
+        if (S.nops < BS_MG_MAXOPS) {
+            S.op[S.nops] = (unsigned char)op;
+            S.lv[S.nops] = (unsigned char)lv;
+            S.acc[S.nops] = (unsigned char)a;
+        }
+        S.nops++;
+    };
+    if (need & 4) push(3, l, acc);
+    if (!(need & 2)) return;
+    push(0, l, 0);
+    sub_ops(D, L, l + 1, 0, S);
+    if (l <= D.mg.wlev) {
+        push(1, l + 1, 0);
+        sub_ops(D, L, l + 1, 1, S);
+    }
+    push(2, l, acc);
+}
+
 // Cycle on level l >= 1 (input r[l], output z[l]); acc: add to z[l].
 // Levels 1..wlev visit level l+1 twice (W), deeper levels once (V).
-// Levels no scene needs launch nothing.
+// Levels no scene needs launch nothing.  From the subtree level down, one
+// clustered launch per visit.
 template <typename T>
 void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     const MgLevel* G = L.mglev;
     const unsigned char need = L.mgneed[l];
     if (!(need & 1)) return;
     int q;
+    if (l == L.mgsub_level) {   // this level and everything below: one clustered launch
+        MgSub S;
+        S.l0 = l;
+        S.nops = 0;
+        sub_ops(D, L, l, acc, S);
+        for (int u = 0; u < BS_MG_SUBL && l + u <= D.mg.nlev; ++u) S.G[u] = G[l + u];
+        q = tbegin(L, K_MG_SUB);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(D.nscene * L.mgsub_cs));
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = 2 * D.mg.coarse_max * sizeof(T);
+        cfg.stream = L.stream;
+        cudaLaunchAttribute at[2];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)L.mgsub_cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 2;
+        cudaLaunchKernelEx(&cfg, k_mg_sub<T>, D, S);
+        tend(L, q);
+        return;
+    }
     if (need & 4) {
         q = tbegin(L, K_MG_COARSE);
         launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
@@ -519,6 +622,36 @@ void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
 }  // namespace
 
 namespace bs {
+
+// clusters of `cs` blocks of k_mg_sub that fit on the device at once (0: the
+// cluster shape cannot be launched)
+int mg_sub_max_clusters(int mg_precision, int cs, size_t smem) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cs);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    cudaError_t e;
+    if (mg_precision == BS_PREC_MIXED) {
+        if (cs > 8) cudaFuncSetAttribute(k_mg_sub<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        e = cudaOccupancyMaxActiveClusters(&n, k_mg_sub<float>, &cfg);
+    } else {
+        if (cs > 8) cudaFuncSetAttribute(k_mg_sub<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        e = cudaOccupancyMaxActiveClusters(&n, k_mg_sub<double>, &cfg);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
 
 void mg_setup(const Dev& D, const Launch& L, int mg_precision) {
     if (mg_precision == BS_PREC_MIXED) setup_t<float>(D, L);

@@ -344,3 +344,24 @@ def test_error_paths(api):
     ctx.int_vel()
     ctx.ppe_assemble()
     assert ctx.info()["err_bits"] & 0x02
+
+
+@pytest.mark.parametrize("precision,dx", [(1, 0.01), (0, 0.01), (1, 0.0025)])
+def test_multigrid_cluster_subtree_equals_level_launches(api, precision, dx):
+    """The coarse multigrid levels run as one clustered launch per visit
+    (option mg_sub) or as one launch per level operation: the same arithmetic
+    per cell, so the steps are bit-identical."""
+    from beachslope_gb300 import abi, scene
+    p, st, gr = scene.beach_scene(dx=dx, precision=precision)
+    a = api.Context([p], [st], [gr], tuning="auto")
+    b = api.Context([p], [st], [gr], tuning="auto")
+    a.set_option("mg_sub", 1)
+    b.set_option("mg_sub", 0)
+    assert a.get_option("mg_sub_level") >= 1 and b.get_option("mg_sub_level") == 0
+    for c in (a, b):
+        c.prime()
+        c.step(2)
+    ga, gb = a.download(), b.download()
+    for f in ("x", "y", "vx", "vy", "p"):
+        assert np.array_equal(ga[f], gb[f]), f
+    assert a.info()["ppe_iters"] == b.info()["ppe_iters"]
