@@ -17,7 +17,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
-OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_omega", "mg_cscale",
+OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_post0", "mg_omega", "mg_cscale",
            "mg_coarse_sweeps", "mg_sub")
 
 
@@ -84,7 +84,7 @@ def tune(ctx, grains, steps=2, verbose=True):
         return ms if ok else math.inf
 
     base = {"ppe_restart": 30, "ppe_solver": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9,
-            "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0}
+            "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0, "mg_post0": 1}
     best, best_ms = dict(base), run(base)
     solver_stage = [{"ppe_solver": 0}] + [{"ppe_solver": 1, "ppe_restart": r} for r in (20, 30, 50, 80, 120)]
     stages = [
@@ -95,6 +95,7 @@ def tune(ctx, grains, steps=2, verbose=True):
         [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],
         [{"mg_coarse_sweeps": c} for c in (5, 10, 20)],
         [{"mg_sub": 1}],
+        [{"mg_post0": 2}],
         solver_stage,
     ]
     for stage in stages:

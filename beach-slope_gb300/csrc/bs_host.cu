@@ -523,6 +523,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         M.pre0 = 1;
         M.prec = 1;
         M.wlev = 2;
+        M.post0 = 1;
         // each scene reserves the levels of its creation grid (the largest
         // grid the slot takes, bs_set_scene)
         std::vector<std::vector<std::pair<int, int>>> dims(nscenes);
@@ -938,6 +939,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_prec") M.prec = value != 0;
     else if (k == "mg_coarse_sweeps" && value >= 1 && value <= 1000) M.coarse_sweeps = (int)value;
     else if (k == "mg_wlev" && value >= 0 && value <= BS_MG_MAXL) M.wlev = (int)value;
+    else if (k == "mg_post0" && (value == 1 || value == 2)) M.post0 = (int)value;
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else if (k == "mg_sub" && (value == 0 || value == 1)) ctx->mgsub_on = (int)value;
     else if (k == "ppe_solver" && (value == BS_SOLVER_BICGSTAB || value == BS_SOLVER_FGMRES))
@@ -962,6 +964,7 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "mg_prec") *value = M.prec;
     else if (k == "mg_coarse_sweeps") *value = M.coarse_sweeps;
     else if (k == "mg_wlev") *value = M.wlev;
+    else if (k == "mg_post0") *value = M.post0;
     else if (k == "mg_levels") *value = M.nlev;
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
     else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;

@@ -95,6 +95,7 @@ struct MgDev {
     int coarse_sweeps, coarse_max;
     int pre0, prec;                   // pre-smoothing at level 0 / on the cell levels (0 or 1)
     int wlev;                         // levels 1..wlev recurse twice
+    int post0;                        // level-0 post-sweeps (1 or 2)
     uint8_t* sub;                     // level 0: quadrant of the row in its cell (bit0 lower, bit1 right)
     int* agg1;                        // level 0: global level-1 index of the row's half-cell
 };

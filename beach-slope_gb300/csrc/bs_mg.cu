@@ -493,20 +493,24 @@ __global__ void __launch_bounds__(1024) k_mg_sub(Dev D, __grid_constant__ const 
 
 // Level 0 post-sweep after the prolongation; writes the preconditioned
 // vector (FP64).
+// mode 0: one sweep from zz into out; with two post-sweeps (mg_post0 = 2)
+// mode 1 sweeps zz into u (free after the prolongation) and mode 2 u into out.
 template <typename T>
-__global__ void k_mg_l0_up(Dev D, double* __restrict__ out) {
+__global__ void k_mg_l0_up(Dev D, double* __restrict__ out, int mode) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
-    const T* __restrict__ zz = (const T*)D.mg.zz;
+    const T* __restrict__ zz = (const T*)(mode == 2 ? D.mg.u : D.mg.zz);
     const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
     const int* __restrict__ idx = D.nidx;
     const T zr = zz[r];
     const T ax = ell_dot<T>(A, idx, zz, r, D.ncount[r], D.kmax, ((const T*)D.mg.adiagT)[r] * zr);
     const T x = ((const T*)D.mg.xin)[r];
-    out[r] = (double)(zr + (T)D.mg.omega * ((const T*)D.mg.dinv0)[r] * (x - ax));
+    const T v = zr + (T)D.mg.omega * ((const T*)D.mg.dinv0)[r] * (x - ax);
+    if (mode == 1) ((T*)D.mg.u)[r] = v;
+    else out[r] = (double)v;
 }
 
 inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }
@@ -615,7 +619,12 @@ void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
     launch_pdl(L, k_mg_l0_prolong<T>, L.nblk_rows, BS_THREADS, 0, D);
     tend(L, q);
     q = tbegin(L, K_MG_L0UP);
-    launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out);
+    if (D.mg.post0 == 2) {
+        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 1);
+        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 2);
+    } else {
+        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 0);
+    }
     tend(L, q);
 }
 
