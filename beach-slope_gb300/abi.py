@@ -28,6 +28,7 @@ FLAG_FREE, FLAG_VICINITY, FLAG_BUFFER = 0x01, 0x02, 0x04
 PREC_FP64, PREC_MIXED = 0, 1
 STOP_RELRES, STOP_REFERENCE, STOP_R0 = 0, 1, 2
 SOLVER_BICGSTAB, SOLVER_FGMRES = 0, 1
+STEP_SCALAR, STEP_BUFFERS, STEP_DENSITY, STEP_EDDY_END, STEP_ALL = 0x1, 0x2, 0x4, 0x8, 0xF
 
 _d = C.c_double
 _i = C.c_int32
@@ -178,6 +179,18 @@ def state_in(arrs):
         setattr(st, f, _ptr(keep[f], C.c_int32))
     keep["flags"] = np.ascontiguousarray(arrs.get("flags", np.zeros(n, np.uint8)), dtype=np.uint8)
     st.flags = _ptr(keep["flags"], C.c_uint8)
+    st._keep = keep
+    return st
+
+
+def fields_in(fields):
+    """bs_state carrying the given in-place fields (bs_set_fields)."""
+    keys = ("vx", "vy", "p", "mass", "rho", "oden", "ovol", "con")
+    keep = {k: np.ascontiguousarray(fields[k], dtype=np.float64) for k in keys if k in fields}
+    st = State()
+    st.n = int(len(next(iter(keep.values()))))
+    for k, v in keep.items():
+        setattr(st, k, _ptr(v, C.c_double))
     st._keep = keep
     return st
 

@@ -74,6 +74,9 @@ def _load():
         "bs_fgmres_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, i32, vp, vp]),
         "bs_set_inflow": (C.c_int, [vp, i32, i32, vp]),
         "bs_ghost": (C.c_int, [vp, i32]),
+        "bs_step_flags": (C.c_int, [vp, i32, i32]),
+        "bs_set_fields": (C.c_int, [vp, i32, vp]),
+        "bs_set_time": (C.c_int, [vp, i32, C.c_double]),
         "bs_buffer_exchange": (C.c_int, [vp, i32, i32]),
         "bs_event_record": (C.c_int, [vp, i32]),
         "bs_event_elapsed_ms": (C.c_int, [vp, i32, i32, C.POINTER(C.c_float)]),
@@ -208,6 +211,19 @@ class Context:
         abi.inflow_in for the dict; None clears it."""
         z = abi.inflow_in(zone)
         self._check(lib.bs_set_inflow(self.h, s, zone_index, C.byref(z)), "set_inflow")
+
+    def step_flags(self, n, flags):
+        """The step without the parts the flags leave out (abi.STEP_*)."""
+        self._check(lib.bs_step_flags(self.h, int(n), int(flags)), "step_flags")
+
+    def set_fields(self, fields, s=0):
+        """Overwrite vx, vy, p, mass, rho, oden, ovol, con (the keys given) in
+        place, in download order."""
+        st = abi.fields_in(fields)
+        self._check(lib.bs_set_fields(self.h, s, C.byref(st)), "set_fields")
+
+    def set_time(self, t, s=0):
+        self._check(lib.bs_set_time(self.h, s, float(t)), "set_time")
 
     def ghost(self, use_mls=False):
         """comp_ghost + ghost_en (mls.f90:114-263); use_mls: the MLS branch."""

@@ -1392,8 +1392,12 @@ int bs_wcsph_step(bs_ctx* ctx, int32_t nsteps) {
 }
 
 // Full production step, main.f90:199-272 (open-boundary buffers excluded).
-int bs_step(bs_ctx* ctx, int32_t nsteps) {
-    if (!ctx || nsteps < 0) return BS_E_ARG;
+int bs_step(bs_ctx* ctx, int32_t nsteps) { return bs_step_flags(ctx, nsteps, BS_STEP_ALL); }
+
+// The production step of main.f90:199-272; the flags drop the parts the
+// reference's settling phases (main.f90:39-67, 95-155) do not run.
+int bs_step_flags(bs_ctx* ctx, int32_t nsteps, int32_t flags) {
+    if (!ctx || nsteps < 0 || (flags & ~BS_STEP_ALL)) return BS_E_ARG;
     Dev& D = ctx->D;
     for (int it = 0; it < nsteps; ++it) {
         bs::Launch L = launch_of(ctx);
@@ -1402,7 +1406,7 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
         bs::advance_time(D, L);
         bool any_scalar = false;
         for (auto& p : ctx->prm) any_scalar |= p.scalar_on != 0;
-        if (any_scalar) {
+        if (any_scalar && (flags & BS_STEP_SCALAR)) {
             if (!ctx->disp_ready) {
                 bs::disp(D, L);
                 ctx->disp_ready = true;
@@ -1410,7 +1414,8 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
             // solsteps of the previous timestep() (read back at the end of the last step)
             for (int j1 = 0; j1 < ctx->max_solsteps; ++j1) st_scalar(ctx, j1);
         }
-        if (int rc = st_buffers(ctx)) return rc;   // remove_bufferN + insert_bufferN
+        if (flags & BS_STEP_BUFFERS)
+            if (int rc = st_buffers(ctx)) return rc;   // remove_bufferN + insert_bufferN
         st_rebin(ctx, 1, 0);                 // projection + cellshift + resetid
         st_search(ctx, 1, 1);                // neighbour + effpor
         bs::eddy(D, L, ctx->precision, 1, 1, 0);  // eddyvis (+ varts of int_vel)
@@ -1424,15 +1429,48 @@ int bs_step(bs_ctx* ctx, int32_t nsteps) {
         st_search(ctx, 1, 1);                // neighbour + effpor
         bs::freesurf(D, L);
         bs::shift(D, L, ctx->precision);     // opt2_shift
-        bs::apply_density(D, L, 1, 1);       // shift apply + densityupdate
+        bs::apply_density(D, L, 1, (flags & BS_STEP_DENSITY) ? 1 : 0);   // shift apply + densityupdate
         bs::cell_max_timestep(D, L, 0, 1);   // timestep
-        bs::eddy(D, L, ctx->precision, 1, 0, 1);  // eddyvis (+ dispersion for the next scalar)
-        ctx->disp_ready = true;
+        if (flags & BS_STEP_EDDY_END) {
+            bs::eddy(D, L, ctx->precision, 1, 0, 1);  // eddyvis (+ dispersion for the next scalar)
+            ctx->disp_ready = true;
+        } else {
+            ctx->disp_ready = false;
+        }
         int rc = check_launch(ctx);
         if (rc) return rc;
         rc = read_solsteps(ctx);   // next step's scalar sub-step count
         if (rc) return rc;
     }
+    return 0;
+}
+
+// Overwrite fields of a scene in place, in the context's particle order
+// (bs_download's): the host edits of the reference's driver between phases
+// (main.f90:69-92, 156-191).  Non-NULL among vx, vy, p, mass, rho, oden,
+// ovol, con; st->n must equal the scene's particle count.
+int bs_set_fields(bs_ctx* ctx, int32_t s, const bs_state* st) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !st) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    Dev& D = ctx->D;
+    SceneDyn hd;
+    CK(cudaMemcpy(&hd, D.dyn + s, sizeof(hd), cudaMemcpyDeviceToHost));
+    if (st->n != hd.n) return fail(ctx, BS_E_ARG, "bs_set_fields: particle count differs from the scene's");
+    const size_t off = ctx->hpar[s].row0, n = hd.n;
+    const double* src[] = {st->vx, st->vy, st->p, st->mass, st->rho, st->oden, st->ovol, st->con};
+    double* dst[] = {D.vx, D.vy, D.p, D.mass, D.rho, D.oden, D.ovol, D.con};
+    for (int f = 0; f < 8; ++f)
+        if (src[f] && n) CK(cudaMemcpy(dst[f] + off, src[f], sizeof(double) * n, cudaMemcpyHostToDevice));
+    bs::derive_fields(D, launch_of(ctx));   // vol = m/rho, nu from oden
+    ctx->assembled = false;
+    return check_launch(ctx);
+}
+
+// Set a scene's time (the reference restarts t at 0 for its production phase, main.f90:193-197)
+int bs_set_time(bs_ctx* ctx, int32_t s, double t) {
+    if (!ctx || s < 0 || s >= ctx->nscene) return BS_E_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&ctx->D.dyn[s].t, &t, sizeof(double), cudaMemcpyHostToDevice));
     return 0;
 }
 

@@ -329,6 +329,22 @@ int bs_timestep(struct bs_ctx* ctx);        /* timestep, integrator.f90:885     
 /* Full production step (main.f90:199-272) with fused kernels, nsteps times. */
 int bs_step(struct bs_ctx* ctx, int32_t nsteps);
 
+/* The step with parts left out, as the reference's settling phases run it:
+ * phase 1 (main.f90:39-67) with 0, phase 2 (main.f90:95-155) with
+ * BS_STEP_BUFFERS; bs_step = BS_STEP_ALL. */
+#define BS_STEP_SCALAR    0x1   /* scalar sub-steps at the start of the step          */
+#define BS_STEP_BUFFERS   0x2   /* the buffer-zone schedule (bs_set_inflow)           */
+#define BS_STEP_DENSITY   0x4   /* densityupdate after the shift                     */
+#define BS_STEP_EDDY_END  0x8   /* eddyvis (and the dispersion) at the end of the step */
+#define BS_STEP_ALL       0xf
+int bs_step_flags(struct bs_ctx* ctx, int32_t nsteps, int32_t flags);
+/* Overwrite vx, vy, p, mass, rho, oden, ovol, con (the non-NULL ones) of a
+ * scene in place, in bs_download's particle order; st->n = the scene's
+ * count.  The host edits of the reference's driver between its phases. */
+int bs_set_fields(struct bs_ctx* ctx, int32_t scene, const bs_state* st);
+/* Set a scene's time t (the reference restarts it at 0 for production). */
+int bs_set_time(struct bs_ctx* ctx, int32_t scene, double t);
+
 /* ---- WCSPH (wcsph.f90, a module the reference ships but does not call) --- */
 int bs_wcsph_continuity(struct bs_ctx* ctx);   /* calmasscons, wcsph.f90:65-129: tden of fluid rows */
 int bs_wcsph_update_density(struct bs_ctx* ctx); /* updateden, wcsph.f90:131-154: density = tden   */

@@ -1522,12 +1522,14 @@ void buffer_schedule(or_scene* s, double told) {
     }
 }
 
-void step(or_scene* s) {
+// one step of main.f90's loops; flags (BS_STEP_*) select the parts the
+// settling phases (main.f90:39-67, 95-155) leave out
+void step(or_scene* s, int flags = BS_STEP_ALL) {
     const double told = s->t;
     s->t = s->t + s->dt;
-    if (s->P.scalar_on)
+    if (s->P.scalar_on && (flags & BS_STEP_SCALAR))
         for (int j1 = 1; j1 <= s->solsteps; ++j1) scalar_substep(s);
-    buffer_schedule(s, told);
+    if (flags & BS_STEP_BUFFERS) buffer_schedule(s, told);
     projection(s);
     cellshift(s, false);
     resetid(s);
@@ -1546,9 +1548,9 @@ void step(or_scene* s) {
     freesurf(s);
     effpor(s);
     opt2_shift(s);
-    densityupdate(s);
+    if (flags & BS_STEP_DENSITY) densityupdate(s);
     timestep(s);
-    eddyvis(s);
+    if (flags & BS_STEP_EDDY_END) eddyvis(s);
 }
 
 // WCSPH step: the production step with continuity + Tait EOS + wall
@@ -1655,6 +1657,40 @@ int or_get_threads(void) {
 #else
     return 1;
 #endif
+}
+
+int or_step_flags(or_scene* s, int32_t nsteps, int32_t flags) {
+    if (!s || nsteps < 0 || (flags & ~BS_STEP_ALL)) return BS_E_ARG;
+    for (int k = 0; k < nsteps; ++k) step(s, flags);
+    return 0;
+}
+
+// bs_set_fields: overwrite particle fields in or_get's order
+int or_set_fields(or_scene* s, const bs_state* st) {
+    if (!s || !st || st->n != count_particles(s)) return BS_E_ARG;
+    size_t q = 0;
+    for (int j = 1; j <= s->cellx; ++j)
+        for (int i = 1; i <= s->celly; ++i) {
+            Cell& c = s->C(i, j);
+            for (int k = 0; k < c.ptot; ++k, ++q) {
+                Particle& p = c.plist[k];
+                if (st->vx) p.vx = st->vx[q];
+                if (st->vy) p.vy = st->vy[q];
+                if (st->p) p.pressure = st->p[q];
+                if (st->mass) p.mass = st->mass[q];
+                if (st->rho) p.density = st->rho[q];
+                if (st->oden) p.oden = st->oden[q];
+                if (st->ovol) p.ovol = st->ovol[q];
+                if (st->con) p.con = st->con[q];
+            }
+        }
+    return 0;
+}
+
+int or_set_time(or_scene* s, double t) {
+    if (!s) return BS_E_ARG;
+    s->t = t;
+    return 0;
 }
 
 int or_get(or_scene* s, bs_state* o) {

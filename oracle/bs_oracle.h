@@ -57,6 +57,10 @@ int or_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const d
                   const double* b, double* x, double tol, int32_t maxit, int32_t restart,
                   int32_t rule, int32_t* iters, double* relres);
 int or_step(or_scene* s, int32_t nsteps);
+/* the step with parts left out (BS_STEP_* flags, main.f90:39-67, 95-155) */
+int or_step_flags(or_scene* s, int32_t nsteps, int32_t flags);
+int or_set_fields(or_scene* s, const bs_state* st);
+int or_set_time(or_scene* s, double t);
 int or_wcsph_step(or_scene* s, int32_t nsteps);
 /* combined, output.f90:188-222 (fluid / buffer text files) */
 int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_path);

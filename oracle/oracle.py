@@ -63,6 +63,9 @@ def lib():
         L.or_write_combined.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.or_set_pressure.argtypes = [vp, vp]
         L.or_set_inflow.argtypes = [vp, C.c_int32, vp]
+        L.or_step_flags.argtypes = [vp, C.c_int32, C.c_int32]
+        L.or_set_fields.argtypes = [vp, vp]
+        L.or_set_time.argtypes = [vp, C.c_double]
         L.or_buffer_exchange.argtypes = [vp, C.c_int32]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_ppe_fgmres.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32, vp, vp]
@@ -178,6 +181,18 @@ class Oracle:
         rc = lib().or_set_inflow(self.h, zone_index, C.byref(z))
         if rc != 0:
             raise RuntimeError(f"or_set_inflow failed ({rc})")
+
+    def step_flags(self, n, flags):
+        return lib().or_step_flags(self.h, int(n), int(flags))
+
+    def set_fields(self, fields):
+        st = self.abi.fields_in(fields)
+        rc = lib().or_set_fields(self.h, C.byref(st))
+        if rc != 0:
+            raise RuntimeError(f"or_set_fields failed ({rc})")
+
+    def set_time(self, t):
+        lib().or_set_time(self.h, float(t))
 
     def buffer_exchange(self, zone_index):
         return lib().or_buffer_exchange(self.h, zone_index)
