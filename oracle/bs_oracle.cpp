@@ -888,9 +888,13 @@ int ppe_solve(or_scene* s, double tol, int maxit, int rule, int* iters, double* 
     s->fsol.assign(n, 0.0);
     for (auto& c : s->cells)
         for (int k = 0; k < c.ptot; ++k) s->fsol[c.plist[k].matid - 1] = c.plist[k].pressure;
-    int st = bicgstab(
-        n, [&](const std::vector<double>& b, std::vector<double>& r) { spmv2(s, b, r); }, s->fvec, s->fsol, tol,
-        maxit, rule, iters, relres);
+    // the solver the parameters name: BiCGStab, or fgmres as the reference's
+    // live ppesolve (solver.f90:306-350)
+    const auto spmv = [&](const std::vector<double>& b, std::vector<double>& r) { spmv2(s, b, r); };
+    int st = (s->P.ppe_solver == BS_SOLVER_FGMRES)
+                 ? fgmres(n, spmv, s->fvec, s->fsol, tol, maxit, std::max(1, (int)s->P.ppe_restart), rule, iters,
+                          relres)
+                 : bicgstab(n, spmv, s->fvec, s->fsol, tol, maxit, rule, iters, relres);
     // pressure scatter, isph.f90:468-486
     for_interior(s, [&](int i, int j) {
         Cell& c = s->C(i, j);
