@@ -74,6 +74,7 @@ def _load():
         "bs_fgmres_csr": (C.c_int, [i32, vp, vp, vp, vp, vp, C.c_double, i32, i32, i32, vp, vp]),
         "bs_set_inflow": (C.c_int, [vp, i32, i32, vp]),
         "bs_ghost": (C.c_int, [vp, i32]),
+        "bs_collision_shift": (C.c_int, [vp, i32, C.c_double, C.c_double, C.c_double, C.c_double]),
         "bs_step_flags": (C.c_int, [vp, i32, i32]),
         "bs_set_fields": (C.c_int, [vp, i32, vp]),
         "bs_set_time": (C.c_int, [vp, i32, C.c_double]),
@@ -228,6 +229,12 @@ class Context:
     def ghost(self, use_mls=False):
         """comp_ghost + ghost_en (mls.f90:114-263); use_mls: the MLS branch."""
         self._check(lib.bs_ghost(self.h, 1 if use_mls else 0), "ghost")
+
+    def collision_shift(self, mode, prx, pry, brx, bry):
+        """coll_pos_shift (mode 0) / coll_shift (mode 1), part_shift.f90:193-410;
+        prx .. bry: the half particle spacings prrealx, prrealy, brrealx, brrealy."""
+        self._check(lib.bs_collision_shift(self.h, int(mode), float(prx), float(pry), float(brx), float(bry)),
+                    "collision_shift")
 
     def buffer_exchange(self, zone_index, s=0):
         self._check(lib.bs_buffer_exchange(self.h, s, zone_index), "buffer_exchange")

@@ -1301,6 +1301,11 @@ int bs_ghost(bs_ctx* ctx, int32_t use_mls) {
     bs::ghost(ctx->D, launch_of(ctx), ctx->precision, use_mls);
     return check_launch(ctx);
 }
+int bs_collision_shift(bs_ctx* ctx, int32_t mode, double prx, double pry, double brx, double bry) {
+    if (!ctx || (mode != 0 && mode != 1) || !(prx > 0) || !(pry > 0) || !(brx > 0) || !(bry > 0)) return BS_E_ARG;
+    bs::collision_shift(ctx->D, launch_of(ctx), ctx->precision, mode, prx, pry, brx, bry);
+    return check_launch(ctx);
+}
 int bs_shift(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     bs::shift(ctx->D, launch_of(ctx), ctx->precision);

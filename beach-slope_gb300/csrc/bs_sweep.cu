@@ -1005,6 +1005,89 @@ __global__ void __launch_bounds__(BS_THREADS) k_boun_vel(Dev D) {
     D.vys[r] = 0.0;
 }
 
+// ------------------------------------------------ collision shifts
+// coll_pos_shift (mode 0, part_shift.f90:193-292) and coll_shift (mode 1,
+// 294-410), compiled but never called.  Pass 1 (k_coll): every row's xs, ys
+// (mode 0) or vxs, vys (mode 1) zeroed; for fluid rows with neighbours,
+// gradvx >= 0.7 and not in a buffer, per axis t1 = sum m_j and t2 = sum of
+// the pushes of the neighbours closer than
+// dcol = pr/sqrt(phi_i) + (fluid_j ? pr : br)/sqrt(phi_j); the shift is
+// t2 / (m_i + t1).  The push is -(m_j (1 + cr) (d - dcol)) (x_i - x_j)/d
+// (mode 0) or, where the relative pore velocity approaches (t3 < 0),
+// -(m_j (1 + cr) t3) (x_i - x_j)/d^2 (mode 1); cr = 0.  Pass 2
+// (k_coll_apply) moves or accelerates the rows after every shift is known.
+// Products in the reference's evaluation order, no contraction; a failed
+// condition adds 0.0 as merge() does.
+template <typename T>
+__global__ void __launch_bounds__(BS_THREADS) k_coll(Dev D, int mode, double prx, double pry, double brx,
+                                                     double bry) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    double* sxp = mode ? D.vxs : D.xs;
+    double* syp = mode ? D.vys : D.ys;
+    const int n = D.ncount[r];
+    if (!(n != 0 && D.gradvx[r] >= 0.70 && D.tid[r] == BS_TID_FLUID && !(D.flags[r] & BS_FLAG_BUFFER))) {
+        sxp[r] = 0.0;
+        syp[r] = 0.0;
+        return;
+    }
+    const double cr = 0.0, disfac = 1.0;
+    const double xi = D.x[r], yi = D.y[r], phi = D.por[r], mi = D.mass[r];
+    const double isq = __ddiv_rn(1.0, __dsqrt_rn(phi)), iphi = __ddiv_rn(1.0, phi);
+    const double vxi = __dmul_rn(D.vx[r], iphi), vyi = __dmul_rn(D.vy[r], iphi);
+    double out[2];
+    for (int ax = 0; ax < 2; ++ax) {
+        const double pr = ax ? pry : prx, br = ax ? bry : brx;
+        double t1 = 0.0, t2 = 0.0;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, D.kmax);
+            const int j = D.nidx[e];
+            const double d = (double)ld<T>(D.ndist, e);
+            const double phj = D.por[j];
+            const double dcol = __dmul_rn(disfac, __dadd_rn(__dmul_rn(pr, isq),
+                __dmul_rn(D.tid[j] == BS_TID_FLUID ? pr : br, __ddiv_rn(1.0, __dsqrt_rn(phj)))));
+            const double mj = D.mass[j];
+            t1 = __dadd_rn(t1, mj);
+            const double rel = ax ? __dsub_rn(yi, D.y[j]) : __dsub_rn(xi, D.x[j]);
+            double term = 0.0;
+            if (mode == 0) {
+                if (d < dcol)
+                    term = __dmul_rn(__dmul_rn(-1.0, __dmul_rn(__dmul_rn(mj, 1.0 + cr), __dsub_rn(d, dcol))),
+                                     __ddiv_rn(rel, d));
+            } else {
+                const double iphj = __ddiv_rn(1.0, phj);
+                const double t3 = __dadd_rn(
+                    __dmul_rn(__dsub_rn(xi, D.x[j]), __dsub_rn(vxi, __dmul_rn(D.vx[j], iphj))),
+                    __dmul_rn(__dsub_rn(yi, D.y[j]), __dsub_rn(vyi, __dmul_rn(D.vy[j], iphj))));
+                if (d < dcol && t3 < 0.0)
+                    term = __dmul_rn(__dmul_rn(-1.0, __dmul_rn(__dmul_rn(mj, 1.0 + cr), t3)),
+                                     __ddiv_rn(rel, __dmul_rn(d, d)));
+            }
+            t2 = __dadd_rn(t2, term);
+        }
+        out[ax] = __ddiv_rn(t2, __dadd_rn(mi, t1));
+    }
+    sxp[r] = out[0];
+    syp[r] = out[1];
+}
+
+__global__ void __launch_bounds__(BS_THREADS) k_coll_apply(Dev D, int mode) {
+    const RowCtx R = row_ctx(D);
+    if (!R.active) return;
+    const int r = R.r;
+    if (D.tid[r] != BS_TID_FLUID || (D.flags[r] & BS_FLAG_BUFFER)) return;
+    if (mode == 0) {
+        if (D.gradvx[r] >= 0.70) {
+            D.x[r] = __dadd_rn(D.x[r], D.xs[r]);
+            D.y[r] = __dadd_rn(D.y[r], D.ys[r]);
+        }
+    } else {
+        D.vx[r] = __dadd_rn(D.vx[r], __dmul_rn(D.vxs[r], D.por[r]));
+        D.vy[r] = __dadd_rn(D.vy[r], __dmul_rn(D.vys[r], D.por[r]));
+    }
+}
+
 // use_mls: the velocity by the module's commented-out moving-least-squares
 // branch, weights W (b1 + b2 dx + b3 dy) V, b = first column of the inverse
 // of the moment matrix over all neighbours (Wmls, mls.f90:16-111;
@@ -1141,6 +1224,11 @@ void wc_wall_pressure(const Dev& D, const Launch& L, int precision) {
 }
 
 void boun_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_GHOST, precision, k_boun_vel, D); }
+void collision_shift(const Dev& D, const Launch& L, int precision, int mode, double prx, double pry, double brx,
+                     double bry) {
+    BS_DISPATCH(K_COLL, precision, k_coll, D, mode, prx, pry, brx, bry);
+    BS_PLAIN(K_COLL, k_coll_apply, D, mode);
+}
 void ghost(const Dev& D, const Launch& L, int precision, int use_mls) {
     BS_DISPATCH(K_GHOST, precision, k_ghost, D, use_mls);
 }

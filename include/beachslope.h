@@ -279,6 +279,19 @@ int bs_boun_vel(struct bs_ctx* ctx);
  * average where that determinant is below 1e-5 (single literal), which at the
  * reference's particle sizes is every particle. */
 int bs_ghost(struct bs_ctx* ctx, int32_t use_mls);
+/* coll_pos_shift (mode 0, part_shift.f90:193-292) and coll_shift (mode 1,
+ * 294-410), compiled in the reference and never called.  Every particle's
+ * xs, ys (mode 0) or vxs, vys (mode 1) are set to 0; a fluid particle with
+ * neighbours, gradvx >= 0.7 and not in a buffer gets, per axis, the
+ * mass-weighted push of the neighbours closer than the collision distance
+ * pr/sqrt(phi_i) + (fluid ? pr : br)/sqrt(phi_j) (pr, br = prx, brx along x
+ * and pry, bry along y: the half particle spacings prrealx, prrealy, brrealx,
+ * brrealy of the reference) -- from the overlap (mode 0) or the approaching
+ * relative pore velocity (mode 1) -- over m_i + the sum of the neighbour
+ * masses.  Then mode 0 moves those particles by (xs, ys); mode 1 adds
+ * phi (vxs, vys) to the velocity of every fluid particle not in a buffer.
+ * Uses the neighbour lists and stored pair distances of the last bs_search. */
+int bs_collision_shift(struct bs_ctx* ctx, int32_t mode, double prx, double pry, double brx, double bry);
 
 /* Set (or, with z->n = 0 and z->ncells = 0, clear) buffer zone `zone` (0 or
  * 1) of a scene; the template is copied.  entrycell1/2 of the reference. */

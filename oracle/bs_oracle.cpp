@@ -1353,6 +1353,75 @@ void boun_vel(or_scene* s) {
     });
 }
 
+// coll_pos_shift (mode 0, part_shift.f90:193-292) and coll_shift (mode 1,
+// 294-410), compiled but never called.  Pass 1: every particle's xs, ys
+// (mode 0) or vxs, vys (mode 1) set to 0; for fluid particles with
+// neighbours, gradvx >= 0.7 and not in a buffer, per axis a mass-weighted
+// push from the neighbours closer than the collision distance
+// dcol = pr/sqrt(phi_i) + (fluid ? pr : br)/sqrt(phi_j) -- the overlap
+// (mode 0) or the approaching relative pore velocity (mode 1, t3 < 0) --
+// over m_i + sum m_j.  Pass 2: mode 0 moves those particles by (xs, ys);
+// mode 1 adds phi (vxs, vys) to the velocity of every fluid particle not in
+// a buffer.  cr = 0, disfac = 1 as the module's parameters; merge() adds
+// 0.0 where the condition fails, so the sums are kept the same way.
+void collision_shift(or_scene* s, int mode, double prx, double pry, double brx, double bry) {
+    const double cr = 0.0, disfac = 1.0;
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            const Props& pp = c.pplist[k];
+            const Verlet& L = c.list[k];
+            double& sx = mode ? p.vxs : p.xs;
+            double& sy = mode ? p.vys : p.ys;
+            sx = 0.0;
+            sy = 0.0;
+            if (!((L.count != 0) && (pp.gradvx >= 0.70) && (p.tid == 3) && !p.buffer)) continue;
+            for (int ax = 0; ax < 2; ++ax) {
+                const double pr = ax ? pry : prx, br = ax ? bry : brx;
+                double t1 = 0.0, t2 = 0.0;
+                for (int m = 0; m < L.count; ++m) {
+                    const Cell& oc = s->cells[L.nh[m].cell];
+                    const Particle& x = oc.plist[L.nh[m].slot];
+                    const Props& y = oc.pplist[L.nh[m].slot];
+                    const double d = L.dist[m];
+                    const double dcol = disfac * (pr * (1.0 / std::sqrt(pp.porosity)) +
+                                                  (x.tid == 3 ? pr : br) * (1.0 / std::sqrt(y.porosity)));
+                    t1 = t1 + x.mass;
+                    const double rel = ax ? (p.y - x.y) : (p.x - x.x);
+                    double term = 0.0;
+                    if (mode == 0) {
+                        if (d < dcol) term = (-1.0 * (x.mass * (1.0 + cr) * (d - dcol))) * (rel / d);
+                    } else {
+                        const double t3 = (p.x - x.x) * (p.vx * (1.0 / pp.porosity) - x.vx * (1.0 / y.porosity)) +
+                                          (p.y - x.y) * (p.vy * (1.0 / pp.porosity) - x.vy * (1.0 / y.porosity));
+                        if ((d < dcol) && (t3 < 0.0)) term = (-1.0 * (x.mass * (1.0 + cr) * t3)) * (rel / (d * d));
+                    }
+                    t2 = t2 + term;
+                }
+                (ax ? sy : sx) = t2 / (p.mass + t1);
+            }
+        }
+    });
+    for_interior(s, [&](int i, int j) {
+        Cell& c = s->C(i, j);
+        for (int k = 0; k < c.ptot; ++k) {
+            Particle& p = c.plist[k];
+            const Props& pp = c.pplist[k];
+            if (p.tid != 3 || p.buffer) continue;
+            if (mode == 0) {
+                if (pp.gradvx >= 0.70) {
+                    p.x = p.x + p.xs;
+                    p.y = p.y + p.ys;
+                }
+            } else {
+                p.vx = p.vx + p.vxs * pp.porosity;
+                p.vy = p.vy + p.vys * pp.porosity;
+            }
+        }
+    });
+}
+
 // invertmat3D, functions.f90:134-165: adjugate over the determinant; err when
 // det < 1e-5 (single literal) or not finite
 bool invertmat3D(double a[3][3]) {
@@ -1688,6 +1757,12 @@ int or_set_fields(or_scene* s, const bs_state* st) {
                 if (st->con) p.con = st->con[q];
             }
         }
+    return 0;
+}
+
+int or_collision_shift(or_scene* s, int32_t mode, double prx, double pry, double brx, double bry) {
+    if (!s || (mode != 0 && mode != 1)) return BS_E_ARG;
+    collision_shift(s, mode, prx, pry, brx, bry);
     return 0;
 }
 

@@ -61,6 +61,10 @@ int or_step(or_scene* s, int32_t nsteps);
 int or_step_flags(or_scene* s, int32_t nsteps, int32_t flags);
 int or_set_fields(or_scene* s, const bs_state* st);
 int or_set_time(or_scene* s, double t);
+/* coll_pos_shift (mode 0) / coll_shift (mode 1), part_shift.f90:193-410;
+ * prx, pry, brx, bry: the half particle spacings prrealx, prrealy, brrealx,
+ * brrealy the routines read */
+int or_collision_shift(or_scene* s, int32_t mode, double prx, double pry, double brx, double bry);
 int or_wcsph_step(or_scene* s, int32_t nsteps);
 /* combined, output.f90:188-222 (fluid / buffer text files) */
 int or_write_combined(or_scene* s, const char* fluid_path, const char* buffer_path);

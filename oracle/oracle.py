@@ -66,6 +66,7 @@ def lib():
         L.or_step_flags.argtypes = [vp, C.c_int32, C.c_int32]
         L.or_set_fields.argtypes = [vp, vp]
         L.or_set_time.argtypes = [vp, C.c_double]
+        L.or_collision_shift.argtypes = [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double]
         L.or_buffer_exchange.argtypes = [vp, C.c_int32]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_ppe_fgmres.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32, vp, vp]
@@ -196,6 +197,12 @@ class Oracle:
 
     def buffer_exchange(self, zone_index):
         return lib().or_buffer_exchange(self.h, zone_index)
+
+    def collision_shift(self, mode, prx, pry, brx, bry):
+        """coll_pos_shift (mode 0) / coll_shift (mode 1)."""
+        rc = lib().or_collision_shift(self.h, int(mode), prx, pry, brx, bry)
+        if rc != 0:
+            raise RuntimeError(f"or_collision_shift failed ({rc})")
 
     def set_pressure(self, p):
         p = np.ascontiguousarray(p, dtype=np.float64)
