@@ -203,23 +203,31 @@ def empty_state():
     return st
 
 
-def state_out(n, full=True):
-    """Allocate numpy arrays for a download and a bs_state pointing at them."""
+def state_out(n, full=True, into=None):
+    """numpy arrays for a download and a bs_state pointing at them; into: a
+    dict of arrays with at least n rows to fill instead (views returned)."""
+    def arr(f, dtype, shape=()):
+        if into is not None:
+            a = into[f]
+            if a.dtype != np.dtype(dtype) or len(a) < n or not a.flags.c_contiguous:
+                raise ValueError(f"download buffer {f}: need {n} contiguous rows of {np.dtype(dtype)}")
+            return a[:n]
+        return np.zeros((n,) + shape, dtype)
     out = {}
     st = State()
     st.n = n
     for f in STATE_FIELDS_F64 + (EXTRA_F64 if full else []):
-        out[f] = np.zeros(n, np.float64)
+        out[f] = arr(f, np.float64)
         setattr(st, f, _ptr(out[f], C.c_double))
     for f in STATE_FIELDS_I32:
-        out[f] = np.zeros(n, np.int32)
+        out[f] = arr(f, np.int32)
         setattr(st, f, _ptr(out[f], C.c_int32))
-    out["flags"] = np.zeros(n, np.uint8)
+    out["flags"] = arr("flags", np.uint8)
     st.flags = _ptr(out["flags"], C.c_uint8)
     if full:
-        out["coff"] = np.zeros((n, 4), np.float64)
+        out["coff"] = arr("coff", np.float64, (4,))
         st.coff = _ptr(out["coff"], C.c_double)
-        out["cell"] = np.zeros(n, np.int32)
+        out["cell"] = arr("cell", np.int32)
         st.cell = _ptr(out["cell"], C.c_int32)
     st._keep = out
     return st, out

@@ -8,6 +8,7 @@ CPU fallback: if the library cannot be loaded, importing this module fails.
 """
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -37,6 +38,8 @@ def _load():
         "bs_prime_scene": (C.c_int, [vp, i32]),
         "bs_write_combined": (C.c_int, [vp, i32, C.c_char_p, C.c_char_p]),
         "bs_download": (C.c_int, [vp, i32, vp]),
+        "bs_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(vp)]),
+        "bs_host_free": (C.c_int, [vp]),
         "bs_scene_info_get": (C.c_int, [vp, i32, vp]),
         "bs_clear_errors": (C.c_int, [vp]),
         "bs_sync": (C.c_int, [vp]),
@@ -172,11 +175,14 @@ class Context:
         self._check(lib.bs_scene_info_get(self.h, s, C.byref(si)), "scene_info")
         return si.as_dict()
 
-    def download(self, s=0, full=True):
+    def download(self, s=0, full=True, out=None):
+        """Scene s's particle fields in the library's row order.  out: a dict
+        from pinned_state() (or a previous download) to fill instead of new
+        arrays; the result is views of its first n rows."""
         n = self.info(s)["n"]
-        st, out = abi.state_out(n, full)
+        st, res = abi.state_out(n, full, out)
         self._check(lib.bs_download(self.h, s, C.byref(st)), "download")
-        return out
+        return res
 
     def neighbours(self, s=0):
         n = self.info(s)["n"]
@@ -315,6 +321,44 @@ for _name in STAGE_FUNCS:
         f.__name__ = nm
         return f
     setattr(Context, _name, _mk(_name))
+
+
+def pinned_empty(n, dtype=np.float64):
+    """A numpy array in page-locked host memory (bs_host_alloc), freed with
+    the array: uploads from and downloads into it run at the host link's
+    rate."""
+    dt = np.dtype(dtype)
+    nbytes = max(int(n) * dt.itemsize, 1)
+    p = C.c_void_p()
+    rc = lib.bs_host_alloc(nbytes, C.byref(p))
+    if rc != 0 or not p.value:
+        raise BeachSlopeError(f"bs_host_alloc({nbytes}) failed ({rc})")
+    buf = (C.c_char * nbytes).from_address(p.value)
+    weakref.finalize(buf, lib.bs_host_free, p.value)
+    return np.frombuffer(buf, dtype=dt, count=int(n))
+
+
+def pinned_state(n, full=False):
+    """Pinned arrays for Context.download(out=...) of up to n rows."""
+    out = {f: pinned_empty(n) for f in abi.STATE_FIELDS_F64 + (abi.EXTRA_F64 if full else [])}
+    for f in abi.STATE_FIELDS_I32:
+        out[f] = pinned_empty(n, np.int32)
+    out["flags"] = pinned_empty(n, np.uint8)
+    if full:
+        out["coff"] = pinned_empty(4 * n).reshape(n, 4)
+        out["cell"] = pinned_empty(n, np.int32)
+    return out
+
+
+def pinned_copy(state):
+    """A copy of a state dict (upload input) in pinned memory."""
+    out = {}
+    for k, v in state.items():
+        v = np.asarray(v)
+        a = pinned_empty(v.size, v.dtype).reshape(v.shape)
+        a[...] = v
+        out[k] = a
+    return out
 
 
 def set_device(device):

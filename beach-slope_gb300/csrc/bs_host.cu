@@ -672,17 +672,21 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     const ScenePar& P = ctx->hpar[s];
     const int n = st->n;
     if (n > P.cap) return fail(ctx, BS_E_CAPACITY, "scene larger than its capacity");
-    // bin: (cell key, walls first, input order) -- boundary.f90:140-190, internal.f90:73-95
-    std::vector<long long> key(n);
+    // bin: (cell key, walls first, input order) -- boundary.f90:140-190,
+    // internal.f90:73-95 -- as a stable counting sort over 2 buckets per cell
+    std::vector<int> bucket(n), ord(n), bstart(2 * (size_t)P.ncell + 1, 0);
     for (int q = 0; q < n; ++q) {
         int ci, cj;
         if (!locate(p, st->x[q], st->y[q], &ci, &cj)) return fail(ctx, BS_E_DOMAIN, "particle outside the interior cell grid");
-        const long long k = (long long)(cj - 1) * p.celly + (ci - 1);
-        key[q] = (k << 33) | ((long long)(st->tid[q] == BS_TID_FLUID ? 1 : 0) << 32) | q;
+        const int k = (cj - 1) * p.celly + (ci - 1);
+        bucket[q] = 2 * k + (st->tid[q] == BS_TID_FLUID ? 1 : 0);
+        bstart[bucket[q] + 1]++;
     }
-    std::vector<int> ord(n);
-    for (int q = 0; q < n; ++q) ord[q] = q;
-    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return key[a] < key[b]; });
+    for (size_t b = 0; b < 2 * (size_t)P.ncell; ++b) bstart[b + 1] += bstart[b];
+    {
+        std::vector<int> fill(bstart.begin(), bstart.end() - 1);
+        for (int q = 0; q < n; ++q) ord[fill[bucket[q]]++] = q;
+    }
     std::vector<double> f64[16];
     const double* src[] = {st->x, st->y, st->vx, st->vy, st->p, st->mass, st->rho, st->oden, st->ovol, st->con};
     for (int f = 0; f < 10; ++f) {
@@ -697,7 +701,7 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
         tid[q] = (int8_t)st->tid[ord[q]];
         flags[q] = st->flags ? st->flags[ord[q]] : 0;
         pid[q] = st->pid ? st->pid[ord[q]] : ord[q] + 1;
-        cellv[q] = (int)(key[ord[q]] >> 33) + P.cell0;
+        cellv[q] = bucket[ord[q]] / 2 + P.cell0;
     }
     {   // cell ranges (empty cells: start == end, ranges stay monotone)
         std::vector<int> cnt(P.ncell, 0);
@@ -730,13 +734,20 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     const int ng = gr ? gr->n : 0;
     if (ng > ctx->gcap[s]) return fail(ctx, BS_E_CAPACITY, "more grains than the grain capacity");
     {
-        std::vector<std::pair<int, int>> gk;
-        for (int q = 0; q < ng; ++q) {
-            int ci, cj;
-            if (!locate(p, gr->x[q], gr->y[q], &ci, &cj)) continue;
-            gk.push_back({(cj - 1) * p.celly + (ci - 1), q});
+        std::vector<std::pair<int, int>> gk;   // (cell, grain) by cell, input order within (counting sort)
+        {
+            std::vector<int> gc(ng, -1), gstart((size_t)P.ncell + 1, 0);
+            for (int q = 0; q < ng; ++q) {
+                int ci, cj;
+                if (!locate(p, gr->x[q], gr->y[q], &ci, &cj)) continue;
+                gc[q] = (cj - 1) * p.celly + (ci - 1);
+                gstart[gc[q] + 1]++;
+            }
+            for (int c = 0; c < P.ncell; ++c) gstart[c + 1] += gstart[c];
+            gk.resize(gstart[P.ncell]);
+            for (int q = 0; q < ng; ++q)
+                if (gc[q] >= 0) gk[gstart[gc[q]]++] = {gc[q], q};
         }
-        std::stable_sort(gk.begin(), gk.end());
         const int m = (int)gk.size();
         std::vector<double> gx(m), gy(m), gv(m);
         std::vector<float> gxr(m), gyr(m);
@@ -782,6 +793,24 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     return check_launch(ctx);
 }
 
+int bs_host_alloc(size_t bytes, void** p) {
+    if (!p) return BS_E_ARG;
+    *p = nullptr;
+    if (cudaMallocHost(p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return BS_E_NOMEM;
+    }
+    return 0;
+}
+int bs_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) {
+        cudaGetLastError();
+        return BS_E_CUDA;
+    }
+    return 0;
+}
+
 int bs_download(bs_ctx* ctx, int32_t s, bs_state* o) {
     if (!ctx || s < 0 || s >= ctx->nscene || !o) return BS_E_ARG;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -792,9 +821,11 @@ int bs_download(bs_ctx* ctx, int32_t s, bs_state* o) {
     o->n = n;
     const size_t off = ctx->hpar[s].row0;
     Dev& D = ctx->D;
+    // stream-ordered copies and one synchronisation: into pinned buffers
+    // (bs_host_alloc) they overlap and run at the host link's rate
     auto get = [&](double* dst, const double* src) -> int {
         if (!dst) return 0;
-        cudaError_t e = cudaMemcpy(dst, src + off, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        cudaError_t e = cudaMemcpyAsync(dst, src + off, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
         return e == cudaSuccess ? 0 : BS_E_CUDA;
     };
     int rc = 0;
@@ -805,13 +836,14 @@ int bs_download(bs_ctx* ctx, int32_t s, bs_state* o) {
     rc |= get(o->resy, D.resy); rc |= get(o->nut, D.nut); rc |= get(o->tke, D.tke); rc |= get(o->varts, D.varts);
     rc |= get(o->gradvx, D.gradvx); rc |= get(o->vel, D.vel); rc |= get(o->cdiff, D.cdiff);
     if (rc) return fail(ctx, BS_E_CUDA, "download copy failed");
+    if (o->flags) CK(cudaMemcpyAsync(o->flags, D.flags + off, n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (o->pid) CK(cudaMemcpyAsync(o->pid, D.pid + off, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     if (o->tid) {
         std::vector<int8_t> t(n);
         CK(cudaMemcpy(t.data(), D.tid + off, n, cudaMemcpyDeviceToHost));
         for (int q = 0; q < n; ++q) o->tid[q] = t[q];
     }
-    if (o->flags) CK(cudaMemcpy(o->flags, D.flags + off, n, cudaMemcpyDeviceToHost));
-    if (o->pid) CK(cudaMemcpy(o->pid, D.pid + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
     if (o->cell) {
         CK(cudaMemcpy(o->cell, D.cell + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
         for (int q = 0; q < n; ++q) o->cell[q] -= ctx->hpar[s].cell0;

@@ -23,6 +23,7 @@
 #ifndef BEACHSLOPE_H
 #define BEACHSLOPE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -236,6 +237,11 @@ int bs_destroy(struct bs_ctx* ctx);
 /* Upload one scene's particles and grains (bins them into cells with the
  * reference's comparison rule; walls first in a cell, then fluid). */
 int bs_upload(struct bs_ctx* ctx, int32_t scene, const bs_state* st, const bs_grains* gr);
+/* Page-locked host memory for the arrays of bs_upload / bs_download
+ * (cudaMallocHost): copies from and to it run at the host link's full rate
+ * and overlap.  Any host memory works with both calls; this is the fast kind. */
+int bs_host_alloc(size_t bytes, void** p);
+int bs_host_free(void* p);
 int bs_download(struct bs_ctx* ctx, int32_t scene, bs_state* st);
 int bs_scene_info_get(struct bs_ctx* ctx, int32_t scene, bs_scene_info* out);
 int bs_clear_errors(struct bs_ctx* ctx);

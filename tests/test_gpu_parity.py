@@ -365,3 +365,24 @@ def test_multigrid_cluster_subtree_equals_level_launches(api, precision, dx):
     for f in ("x", "y", "vx", "vy", "p"):
         assert np.array_equal(ga[f], gb[f]), f
     assert a.info()["ppe_iters"] == b.info()["ppe_iters"]
+
+
+def test_pinned_upload_and_download_into_buffers(api):
+    """Uploading from pinned arrays and downloading into reused pinned
+    buffers gives the same rows as plain numpy arrays."""
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.02)
+    a = api.Context([p], [st], [gr])
+    b = api.Context([p], [api.pinned_copy(st)], [gr])
+    for c in (a, b):
+        c.prime()
+        c.step(2)
+    want = a.download(full=True)
+    buf = api.pinned_state(len(st["x"]) + 100, full=True)
+    for _ in range(2):
+        got = b.download(full=True, out=buf)
+        for f, v in want.items():
+            assert np.array_equal(got[f], v), f
+    assert np.shares_memory(got["x"], buf["x"]) and len(got["x"]) == len(st["x"])
+    with pytest.raises(ValueError):
+        b.download(out=api.pinned_state(10))
