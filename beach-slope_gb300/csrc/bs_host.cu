@@ -60,6 +60,8 @@ struct bs_ctx {
     std::vector<SceneDyn> hdyn;   // host copy of the scenes' dynamic state (schedule of the zones)
     // multigrid levels run as one clustered launch per visit (mg_sub option)
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
+    // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
+    int fg_df_on = 1;
 };
 
 namespace {
@@ -339,6 +341,9 @@ int st_solve(bs_ctx* c) {
     for (auto& p : c->prm) maxit = std::max(maxit, (int)p.ppe_maxit);
     if (c->prm[0].ppe_solver == BS_SOLVER_FGMRES) {
         if (int rc = fg_ensure(c)) return rc;
+        // the double-float basis serves the preconditioned mixed solve (the
+        // basis is only read by the Gram-Schmidt passes there)
+        c->D.fg_df = (c->fg_df_on && c->precision == BS_PREC_MIXED && c->prm[0].ppe_precond) ? 1 : 0;
         bs::solve_fgmres(c->D, L, maxit, c->prm[0].ppe_precond ? 2 : 8, c->prm[0].ppe_precond, c->precision,
                          c->d_nconv, c->h_pinned, c->evsync);
     } else if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
@@ -974,6 +979,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "mg_post0" && (value == 1 || value == 2)) M.post0 = (int)value;
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else if (k == "mg_sub" && (value == 0 || value == 1)) ctx->mgsub_on = (int)value;
+    else if (k == "fg_df" && (value == 0 || value == 1)) ctx->fg_df_on = (int)value;
     else if (k == "ppe_solver" && (value == BS_SOLVER_BICGSTAB || value == BS_SOLVER_FGMRES))
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
@@ -1001,6 +1007,7 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "ppe_precond") *value = ctx->prm[0].ppe_precond;
     else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;
     else if (k == "mg_sub") *value = ctx->mgsub_on;
+    else if (k == "fg_df") *value = ctx->fg_df_on;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
     else return BS_E_ARG;
@@ -1561,6 +1568,7 @@ static int krylov_csr(int solver, int32_t n, const int32_t* row_ptr, const int32
     CK(cudaMemcpy(D.nidx, idx.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(D.aval, aval.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
     ctx->assembled = true;
+    D.fg_df = 0;
     if (solver == BS_SOLVER_FGMRES)
         bs::solve_fgmres(D, launch_of(ctx), maxit, 1, 0, BS_PREC_FP64, ctx->d_nconv, ctx->h_pinned, ctx->evsync);
     else

@@ -160,6 +160,7 @@ struct Dev {
     double *fg_V, *fg_Z, *fg_part, *fg_gpart, *fg_small;
     int* fg_gdone;                  // per-group block counters
     int fg_m, fg_small_n, fg_ld;    // restart length, doubles per scene, rows per basis vector
+    int fg_df;                      // 1: basis stored as (hi, lo) FP32 pairs, dots on the FP32 pipe
     // open-boundary buffer zones: per global cell, the zone bits of the entry
     // cells and, per zone, the cell's template range [zstart, zstart + zcount)
     uint8_t* czone;

@@ -562,6 +562,43 @@ __device__ __forceinline__ double warp_sum(double a) {
     return a;
 }
 
+// Double-float arithmetic (a value as an unevaluated sum hi + lo of two FP32
+// numbers, 48 significant bits; Dekker 1971, Knuth's TwoSum, the FMA form of
+// TwoProduct) for the Gram-Schmidt passes of the mixed solve: a basis element
+// is 8 bytes as in FP64, and its products and sums run on the FP32 pipe, which
+// on this part is ~60x faster than the FP64 pipe that bounds the FP64 form.
+// Intrinsics keep every rounding explicit (no contraction).
+__device__ __forceinline__ float2 df_split(double a) {
+    const float h = __double2float_rn(a);
+    return make_float2(h, __double2float_rn(__dsub_rn(a, (double)h)));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return __dadd_rn((double)a.x, (double)a.y); }
+// s += a * b (products to ~2^-48 relative: TwoProduct of the high parts plus
+// the cross terms; TwoSum into the running high part, errors into the low)
+__device__ __forceinline__ void df_fma(float2& s, float2 a, float2 b) {
+    const float ph = __fmul_rn(a.x, b.x);
+    float pe = __fmaf_rn(a.x, b.x, -ph);
+    pe = __fmaf_rn(a.x, b.y, pe);
+    pe = __fmaf_rn(a.y, b.x, pe);
+    const float t = __fadd_rn(s.x, ph);
+    const float v = __fsub_rn(t, s.x);
+    const float e = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, v)), __fsub_rn(ph, v));
+    s.y = __fadd_rn(s.y, __fadd_rn(e, pe));
+    s.x = t;
+}
+// a + b, renormalised
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float t = __fadd_rn(a.x, b.x);
+    const float v = __fsub_rn(t, a.x);
+    float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(t, v)), __fsub_rn(b.x, v));
+    e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    const float h = __fadd_rn(t, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, t)));
+}
+__device__ __forceinline__ float2 df_shfl_xor(float2 a, int m) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, a.x, m), __shfl_xor_sync(0xffffffffu, a.y, m));
+}
+
 // Sum `cnt` rows of nv partials (row stride ld) in a fixed order: thread t
 // takes value t % nv over rows q, q+Q, ... (q = t / nv, Q = 256 / nv), the
 // Q sub-sums are added in q order.  Rows of zeros at the end change nothing,
@@ -699,9 +736,69 @@ __global__ void k_fg_put(Dev D, int mgmode) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + Y.n) return;
     const double v = D.ss[r] / Y.rho_old;
-    D.fg_V[(long)Y.fg_j * D.fg_ld + r] = v;
+    if (D.fg_df) reinterpret_cast<float2*>(D.fg_V)[(long)Y.fg_j * D.fg_ld + r] = df_split(v);
+    else D.fg_V[(long)Y.fg_j * D.fg_ld + r] = v;
     if (mgmode == 1) bs::mg_put_input<double>(D, r, v);
     else if (mgmode == 2) bs::mg_put_input<float>(D, r, v);
+}
+
+// Pass 1's dots with a double-float basis: the block's w and v_j split into
+// (hi, lo) pairs in shared memory, each lane keeps its 8 rows of both in
+// registers; warp `warp` takes basis vectors warp + 8 (4g + u) as in the FP64
+// form, the 8 double-float values of a lane summed across the warp by the
+// same transposing butterfly in double-float, each block's value converted to
+// FP64 once (into dsh) for the FP64 scene sums.
+__device__ __forceinline__ void fg_arn1_dots_df(const Dev& D, float2 wd, float2 vjd, int nv, long r0, int rend,
+                                                double* dsh) {
+    __shared__ float2 wsd[BS_THREADS], vsd[BS_THREADS];
+    wsd[threadIdx.x] = wd;
+    vsd[threadIdx.x] = vjd;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    constexpr int RPL = BS_THREADS / 32;   // rows per lane
+    const float2* Vb = reinterpret_cast<const float2*>(D.fg_V);
+    for (int base = warp; base < nv; base += 4 * (BS_THREADS / 32)) {
+        // per vector: the lane's 8 rows loaded first, then two accumulation
+        // chains; w and v_j read from shared memory (few registers: the grid
+        // fits the SMs in one wave)
+        float2 x[8];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = base + (BS_THREADS / 32) * u;
+            float2 a = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
+            if (i < nv) {
+                const float2* v = Vb + (long)i * D.fg_ld + r0;
+                float2 vv[RPL];
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) {
+                    const int t = lane + 32 * k;
+                    vv[k] = (r0 + t < rend) ? v[t] : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) {
+                    const int t = lane + 32 * k;
+                    df_fma(a, vv[k], wsd[t]);
+                    df_fma(c, vv[k], vsd[t]);
+                }
+            }
+            x[2 * u] = a;
+            x[2 * u + 1] = c;
+        }
+        float2 y[4], z[2];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) y[k] = df_add(b4 ? x[k + 4] : x[k], df_shfl_xor(b4 ? x[k] : x[k + 4], 16));
+#pragma unroll
+        for (int k = 0; k < 2; ++k) z[k] = df_add(b3 ? y[k + 2] : y[k], df_shfl_xor(b3 ? y[k] : y[k + 2], 8));
+        float2 tv = df_add(b2 ? z[1] : z[0], df_shfl_xor(b2 ? z[0] : z[1], 4));
+        tv = df_add(tv, df_shfl_xor(tv, 2));
+        tv = df_add(tv, df_shfl_xor(tv, 1));
+        if ((lane & 3) == 0) {
+            const int q = lane >> 2;
+            const int i = base + (BS_THREADS / 32) * (q >> 1);
+            if (i < nv) dsh[(q & 1) ? nv + i : i] = df_to_double(tv);
+        }
+    }
 }
 
 // Column j, pass 1: w = A z_j (z_j = the V-cycle output in sp2, kept as Z_j;
@@ -710,7 +807,8 @@ __global__ void k_fg_put(Dev D, int mgmode) {
 // hc = (2I - Gm) h -- classical Gram-Schmidt applied twice,
 // (I - V V^T)^2 = I - V (2I - V^T V) V^T, with the second projection
 // taken from the Gram matrix instead of a second pass over V.
-__global__ void k_fg_arn1(Dev D, int precond) {
+template <int DF>
+__global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (!fg_running(D, s)) return;
@@ -724,15 +822,20 @@ __global__ void k_fg_arn1(Dev D, int precond) {
     const long col = (long)j * D.fg_ld;
     const double* u = precond ? D.sp2 : D.fg_V + col;
     double w = 0.0, vj = 0.0;
+    float2 vjd = make_float2(0.f, 0.f);
     if (r < rend) {
         w = spmv_row64(D, u, r);
         D.sv[r] = w;
-        vj = D.fg_V[col + r];
+        if (DF) vjd = reinterpret_cast<const float2*>(D.fg_V)[col + r];
+        else vj = D.fg_V[col + r];
         if (precond) D.fg_Z[col + r] = D.sp2[r];
     }
-    ws[threadIdx.x] = w;
-    vs[threadIdx.x] = vj;
-    __syncthreads();
+    if (DF) {
+        fg_arn1_dots_df(D, df_split(w), vjd, nv, r0, rend, dsh);
+    } else {
+        ws[threadIdx.x] = w;
+        vs[threadIdx.x] = vj;
+        __syncthreads();
     // Warp w takes basis vectors w + 8 (4g + u), u = 0..3: lanes across the
     // block's rows (coalesced), 8 values per lane (4 vectors x 2 dots), summed
     // over the lanes by a transposing butterfly -- 9 FP64 adds per lane for
@@ -774,6 +877,7 @@ __global__ void k_fg_arn1(Dev D, int precond) {
             if (i < nv) dsh[(q & 1) ? nv + i : i] = tv;
         }
     }
+    }
     __syncthreads();
     if (!fg_scene_sum(D, s, 2 * nv, dsh, tsh)) return;
     const FgSmall f = fg_small(D, s);
@@ -793,20 +897,42 @@ __global__ void k_fg_arn1(Dev D, int precond) {
 
 // Column j, pass 2: w -= V hc (the pending vector, into ss), h_{j+1,j} = ||w||;
 // finisher: rotations, residual estimate, cycle end
+template <int DF>
 __global__ void k_fg_arn2(Dev D, int* nconv) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (!fg_running(D, s)) return;
     __shared__ double hs[BS_FG_MAXM + 1];
+    __shared__ float2 hsd[BS_FG_MAXM + 1];
     const ScenePar& P = D.par[s];
     const int j = D.dyn[s].fg_j;
     const int rend = P.row0 + D.dyn[s].n;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const FgSmall f = fg_small(D, s);
-    for (int i = threadIdx.x; i <= j; i += BS_THREADS) hs[i] = f.hc[i];
+    for (int i = threadIdx.x; i <= j; i += BS_THREADS) {
+        hs[i] = f.hc[i];
+        if (DF) hsd[i] = df_split(hs[i]);
+    }
     __syncthreads();
     double q[1] = {0.0};
-    if (r < rend) {
+    if (r < rend && DF) {   // w -= (V hc) summed in double-float
+        double w = D.sv[r];
+        const float2* v = reinterpret_cast<const float2*>(D.fg_V) + r;
+        const long ld = D.fg_ld;
+        float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+        int i = 0;
+        for (; i + 4 <= j + 1; i += 4) {   // four loads in flight, four chains
+            const float2 v0 = v[i * ld], v1 = v[(i + 1) * ld], v2 = v[(i + 2) * ld], v3 = v[(i + 3) * ld];
+            df_fma(a0, hsd[i], v0);
+            df_fma(a1, hsd[i + 1], v1);
+            df_fma(a2, hsd[i + 2], v2);
+            df_fma(a3, hsd[i + 3], v3);
+        }
+        for (; i <= j; ++i) df_fma(a0, hsd[i], v[i * ld]);
+        w = __dsub_rn(w, df_to_double(df_add(df_add(a0, a1), df_add(a2, a3))));
+        D.ss[r] = w;
+        q[0] = w * w;
+    } else if (r < rend) {
         double w = D.sv[r];
         const double* v = D.fg_V + r;
         int i = 0;
@@ -1047,10 +1173,12 @@ void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int
         tend(L, q2);
         if (precond) mg_apply(D, L, mg_prec, D.fg_V, D.sp2);
         q2 = tbegin(L, K_FG_ARN);
-        launch_pdl(L, k_fg_arn1, L.nblk_rows, BS_THREADS, 0, D, precond);
+        if (D.fg_df) launch_pdl(L, k_fg_arn1<1>, L.nblk_rows, BS_THREADS, 0, D, precond);
+        else launch_pdl(L, k_fg_arn1<0>, L.nblk_rows, BS_THREADS, 0, D, precond);
         tend(L, q2);
         q2 = tbegin(L, K_FG_ORTH);
-        launch_pdl(L, k_fg_arn2, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
+        if (D.fg_df) launch_pdl(L, k_fg_arn2<1>, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
+        else launch_pdl(L, k_fg_arn2<0>, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
         tend(L, q2);
     };
     IterGraph* G = L.graph;

@@ -175,3 +175,29 @@ def test_fgmres_options(api):
     assert ctx.info()["err_bits"] == 0
     with pytest.raises(Exception):
         ctx.set_option("ppe_restart", 151)
+
+
+@pytest.mark.parametrize("tol", [1e-8, 1e-12])
+def test_fgmres_double_float_basis(api, tol):
+    """The mixed solve's double-float basis (fg_df = 1: (hi, lo) FP32 pairs,
+    dots and projection on the FP32 pipe) against the FP64 basis (fg_df = 0)
+    on the same system: the same column count within one, pressures within
+    1e-6 (tolerance 1e-8) and 1e-9 (tolerance 1e-12)."""
+    from beachslope_gb300 import abi, scene
+    p, st, gr = scene.beach_scene(dx=0.01, precision=abi.PREC_MIXED)
+    p.ppe_solver = abi.SOLVER_FGMRES
+    p.ppe_restart = 40
+    p.ppe_tol = tol
+    p.ppe_maxit = 400
+    res = []
+    for df in (0, 1):
+        c = api.Context([p], [st], [gr])
+        c.set_option("fg_df", df)
+        assert c.get_option("fg_df") == df
+        for name in ("search", "porosity", "int_vel", "ppe_assemble", "ppe_solve"):
+            c.stage(name)
+        res.append((c.info(), c.download()["p"]))
+    (i0, p0), (i1, p1) = res
+    assert i0["err_bits"] == 0 and i1["err_bits"] == 0
+    assert i1["ppe_relres"] <= tol and abs(i1["ppe_iters"] - i0["ppe_iters"]) <= 1
+    assert relL2(p1, p0) < (1e-6 if tol > 1e-10 else 1e-9)
