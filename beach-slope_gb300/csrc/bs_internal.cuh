@@ -67,6 +67,7 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     // FGMRES: Arnoldi column of the current cycle, cycle state (0 running,
     // 1 restart, 2 converged, 3 iteration cap) and the columns the update applies
     int fg_j, fg_state, fg_k, fg_pad;
+    double fg_rinv;                // 1 / the norm of the vector the next column normalises
 };
 
 // Aggregation multigrid over the cell grid.  Level 1 = half-cells (2h x 2h,

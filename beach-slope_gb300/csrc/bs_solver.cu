@@ -707,6 +707,7 @@ __global__ void k_fg_start(Dev D, int first, int* nconv) {
         }
         Y.rnorm2 = tot[0];
         Y.rho_old = beta;   // norm of the vector the next column normalises
+        Y.fg_rinv = beta > 0.0 ? 1.0 / beta : 0.0;
         Y.fg_j = 0;
         Y.fg_k = 0;
         fg_small(D, s).g[0] = beta;
@@ -727,7 +728,9 @@ __global__ void k_fg_start(Dev D, int first, int* nconv) {
     }
 }
 
-// v_j = pending / its norm (into V), plus the V-cycle input (mgmode 1: FP64, 2: FP32)
+// v_j = pending / its norm (into V), plus the V-cycle input (mgmode 1: FP64,
+// 2: FP32); the scene's reciprocal norm is formed once by the producer (an
+// FP64 division per row would bound this pass on this part)
 __global__ void k_fg_put(Dev D, int mgmode) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
@@ -735,11 +738,73 @@ __global__ void k_fg_put(Dev D, int mgmode) {
     const SceneDyn& Y = D.dyn[s];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= D.par[s].row0 + Y.n) return;
-    const double v = D.ss[r] / Y.rho_old;
+    const double v = D.ss[r] * Y.fg_rinv;
     if (D.fg_df) reinterpret_cast<float2*>(D.fg_V)[(long)Y.fg_j * D.fg_ld + r] = df_split(v);
     else D.fg_V[(long)Y.fg_j * D.fg_ld + r] = v;
     if (mgmode == 1) bs::mg_put_input<double>(D, r, v);
     else if (mgmode == 2) bs::mg_put_input<float>(D, r, v);
+}
+
+// Column finisher (one block, the scene's last): the new column h[0..j] of
+// H, with h_{j+1,j} = hn below it, rotated by the cycle's earlier Givens
+// rotations (staged in shared memory; the sweep, a dependent chain, run by
+// one thread), a new rotation that zeroes hn, the residual estimate
+// |g_{j+1}| and the cycle's state.  est: hn was formed from the Gram
+// relation rather than summed, and was not trusted (cancellation), so the
+// cycle restarts from the true residual instead of going on.
+__device__ void fg_finish_column(const Dev& D, int s, const FgSmall& f, int j, double hn, bool est_bad, int* nconv) {
+    __shared__ double hcol[BS_FG_MAXM + 2], csh[BS_FG_MAXM], snh[BS_FG_MAXM];
+    const ScenePar& P = D.par[s];
+    const int m = D.fg_m;
+    double* h = f.H + (long)j * (m + 1);
+    for (int i = threadIdx.x; i <= j; i += BS_THREADS) hcol[i] = h[i];
+    for (int i = threadIdx.x; i < j; i += BS_THREADS) {
+        csh[i] = f.cs[i];
+        snh[i] = f.sn[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        SceneDyn& Y = D.dyn[s];
+        double hi = hcol[0];
+        for (int i = 0; i < j; ++i) {   // earlier rotations on the new column
+            const double b = hcol[i + 1];
+            hcol[i] = csh[i] * hi + snh[i] * b;
+            hi = -snh[i] * hi + csh[i] * b;
+        }
+        const double a = hi;
+        const double den = sqrt(a * a + hn * hn);
+        const double c = den > 0.0 ? a / den : 1.0, sn = den > 0.0 ? hn / den : 0.0;
+        f.cs[j] = c;
+        f.sn[j] = sn;
+        hcol[j] = den;
+        hcol[j + 1] = 0.0;
+        const double gj = f.g[j];
+        f.g[j] = c * gj;
+        f.g[j + 1] = -sn * gj;
+        const double res = fabs(f.g[j + 1]);
+        Y.rnorm2 = res * res;
+        Y.rho_old = hn;
+        Y.fg_rinv = hn > 0.0 ? 1.0 / hn : 0.0;
+        Y.iters += 1;
+        Y.fg_j = j + 1;
+        int st = 0;
+        if (!isfinite(res) || !isfinite(hn)) {
+            st = 3;
+            set_err(D, s, BS_ERR_NONFINITE);
+        } else if (est_bad) {
+            st = Y.iters >= P.maxit ? 3 : 1;
+        } else if (res <= Y.part_tmp || hn <= 1e-12) {
+            st = 2;
+        } else if (Y.iters >= P.maxit) {
+            st = 3;
+        } else if (j + 1 == m) {
+            st = 1;
+        }
+        Y.fg_state = st;
+        if (st) atomicAdd(nconv, 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j + 1; i += BS_THREADS) h[i] = hcol[i];
 }
 
 // Pass 1's dots with a double-float basis: the block's w and v_j split into
@@ -808,7 +873,7 @@ __device__ __forceinline__ void fg_arn1_dots_df(const Dev& D, float2 wd, float2 
 // (I - V V^T)^2 = I - V (2I - V^T V) V^T, with the second projection
 // taken from the Gram matrix instead of a second pass over V.
 template <int DF>
-__global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond) {
+__global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond, int* nconv) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (!fg_running(D, s)) return;
@@ -831,7 +896,16 @@ __global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond) {
         if (precond) D.fg_Z[col + r] = D.sp2[r];
     }
     if (DF) {
+        // u.u for the Gram relation of ||w|| (block partial at dsh[2 nv])
+        __shared__ double wwp[BS_THREADS / 32];
+        const double ww = warp_sum(w * w);
+        if ((threadIdx.x & 31) == 0) wwp[threadIdx.x >> 5] = ww;
         fg_arn1_dots_df(D, df_split(w), vjd, nv, r0, rend, dsh);
+        if (threadIdx.x == 0) {
+            double a = 0.0;
+            for (int k = 0; k < BS_THREADS / 32; ++k) a += wwp[k];
+            dsh[2 * nv] = a;
+        }
     } else {
         ws[threadIdx.x] = w;
         vs[threadIdx.x] = vj;
@@ -879,7 +953,7 @@ __global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond) {
     }
     }
     __syncthreads();
-    if (!fg_scene_sum(D, s, 2 * nv, dsh, tsh)) return;
+    if (!fg_scene_sum(D, s, DF ? 2 * nv + 1 : 2 * nv, dsh, tsh)) return;
     const FgSmall f = fg_small(D, s);
     const int ldg = D.fg_m + 1;
     for (int i = threadIdx.x; i < nv; i += BS_THREADS) {
@@ -887,25 +961,65 @@ __global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond) {
         f.Gm[j + (long)i * ldg] = tsh[nv + i];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nv; i += BS_THREADS) {
-        double acc = 2.0 * tsh[i];
-        for (int k = 0; k < nv; ++k) acc -= __ldcg(f.Gm + i + (long)k * ldg) * tsh[k];
-        f.hc[i] = acc;
-        f.H[i + (long)j * ldg] = acc;
+    // hc = (2I - Gm) h, a warp per row: Gm is symmetric, so row i is read as
+    // the contiguous column i (coalesced, a few loads per lane)
+    __shared__ double hcs[BS_FG_MAXM + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = wid; i < nv; i += BS_THREADS / 32) {
+        const double* gcol = f.Gm + (long)i * ldg;
+        double a = 0.0;
+        for (int k = lane; k < nv; k += 32) a += __ldcg(gcol + k) * tsh[k];
+        a = warp_sum(a);
+        if (lane == 0) {
+            const double acc = 2.0 * tsh[i] - a;
+            f.hc[i] = acc;
+            f.H[i + (long)j * ldg] = acc;
+            hcs[i] = acc;
+        }
     }
+    if (!DF) return;
+    // h_{j+1,j} = ||w|| for w = u - V c without a pass over w: ||w||^2 =
+    // u.u - 2 c.h + c^T Gm c (u = A z_j, h = V^T u, Gm = V^T V, c = hc), so
+    // pass 2 can write v_{j+1} and the V-cycle input directly.  When that
+    // difference falls below 1e-6 u.u the estimate is not trusted and the
+    // cycle restarts from the true residual.
+    __shared__ double eparts[BS_THREADS / 32];
+    __shared__ double eta2s;
+    __syncthreads();
+    double part = 0.0;
+    for (int i = wid; i < nv; i += BS_THREADS / 32) {
+        const double* gcol = f.Gm + (long)i * ldg;
+        double g = 0.0;
+        for (int k = lane; k < nv; k += 32) g += __ldcg(gcol + k) * hcs[k];
+        g = warp_sum(g);
+        part += hcs[i] * (g - 2.0 * tsh[i]);
+    }
+    if (lane == 0) eparts[wid] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double e = tsh[2 * nv];
+        for (int w = 0; w < BS_THREADS / 32; ++w) e += eparts[w];
+        eta2s = e;
+    }
+    __syncthreads();
+    const double uu = tsh[2 * nv], eta2 = eta2s;
+    fg_finish_column(D, s, f, j, sqrt(fmax(eta2, 0.0)), !(eta2 > 1e-6 * uu), nconv);
 }
 
 // Column j, pass 2: w -= V hc (the pending vector, into ss), h_{j+1,j} = ||w||;
 // finisher: rotations, residual estimate, cycle end
+// With the double-float basis (DF): column j = fg_j - 1 was finished by pass
+// 1, and this pass writes v_{j+1} = (w - V hc) / h_{j+1,j} into the basis
+// and the V-cycle input (mgmode as k_fg_put), with no reduction.
 template <int DF>
-__global__ void k_fg_arn2(Dev D, int* nconv) {
+__global__ void k_fg_arn2(Dev D, int* nconv, int mgmode) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
     if (!fg_running(D, s)) return;
     __shared__ double hs[BS_FG_MAXM + 1];
     __shared__ float2 hsd[BS_FG_MAXM + 1];
     const ScenePar& P = D.par[s];
-    const int j = D.dyn[s].fg_j;
+    const int j = DF ? D.dyn[s].fg_j - 1 : D.dyn[s].fg_j;
     const int rend = P.row0 + D.dyn[s].n;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const FgSmall f = fg_small(D, s);
@@ -915,7 +1029,8 @@ __global__ void k_fg_arn2(Dev D, int* nconv) {
     }
     __syncthreads();
     double q[1] = {0.0};
-    if (r < rend && DF) {   // w -= (V hc) summed in double-float
+    if (DF) {   // w -= (V hc) summed in double-float, then v_{j+1}
+        if (r >= rend) return;
         double w = D.sv[r];
         const float2* v = reinterpret_cast<const float2*>(D.fg_V) + r;
         const long ld = D.fg_ld;
@@ -930,8 +1045,11 @@ __global__ void k_fg_arn2(Dev D, int* nconv) {
         }
         for (; i <= j; ++i) df_fma(a0, hsd[i], v[i * ld]);
         w = __dsub_rn(w, df_to_double(df_add(df_add(a0, a1), df_add(a2, a3))));
-        D.ss[r] = w;
-        q[0] = w * w;
+        const double vn = w * D.dyn[s].fg_rinv;
+        reinterpret_cast<float2*>(D.fg_V)[(long)(j + 1) * ld + r] = df_split(vn);
+        if (mgmode == 1) bs::mg_put_input<double>(D, r, vn);
+        else if (mgmode == 2) bs::mg_put_input<float>(D, r, vn);
+        return;
     } else if (r < rend) {
         double w = D.sv[r];
         const double* v = D.fg_V + r;
@@ -950,57 +1068,7 @@ __global__ void k_fg_arn2(Dev D, int* nconv) {
     }
     double tot[1];
     if (!scene_sum<1>(D, s, q, tot)) return;
-    // finisher: the column and the rotations staged in shared memory, the
-    // rotation sweep (a dependent chain) run there by one thread
-    __shared__ double hcol[BS_FG_MAXM + 2], csh[BS_FG_MAXM], snh[BS_FG_MAXM];
-    const int m = D.fg_m;
-    double* h = f.H + (long)j * (m + 1);
-    for (int i = threadIdx.x; i <= j; i += BS_THREADS) hcol[i] = h[i];
-    for (int i = threadIdx.x; i < j; i += BS_THREADS) {
-        csh[i] = f.cs[i];
-        snh[i] = f.sn[i];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        SceneDyn& Y = D.dyn[s];
-        const double hn = sqrt(tot[0]);
-        double hi = hcol[0];
-        for (int i = 0; i < j; ++i) {   // earlier rotations on the new column
-            const double b = hcol[i + 1];
-            hcol[i] = csh[i] * hi + snh[i] * b;
-            hi = -snh[i] * hi + csh[i] * b;
-        }
-        const double a = hi;
-        const double den = sqrt(a * a + hn * hn);
-        const double c = den > 0.0 ? a / den : 1.0, sn = den > 0.0 ? hn / den : 0.0;
-        f.cs[j] = c;
-        f.sn[j] = sn;
-        hcol[j] = den;
-        hcol[j + 1] = 0.0;
-        const double gj = f.g[j];
-        f.g[j] = c * gj;
-        f.g[j + 1] = -sn * gj;
-        const double res = fabs(f.g[j + 1]);
-        Y.rnorm2 = res * res;
-        Y.rho_old = hn;
-        Y.iters += 1;
-        Y.fg_j = j + 1;
-        int st = 0;
-        if (!isfinite(res) || !isfinite(hn)) {
-            st = 3;
-            set_err(D, s, BS_ERR_NONFINITE);
-        } else if (res <= Y.part_tmp || hn <= 1e-12) {
-            st = 2;
-        } else if (Y.iters >= P.maxit) {
-            st = 3;
-        } else if (j + 1 == m) {
-            st = 1;
-        }
-        Y.fg_state = st;
-        if (st) atomicAdd(nconv, 1);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i <= j + 1; i += BS_THREADS) h[i] = hcol[i];
+    fg_finish_column(D, s, f, j, sqrt(tot[0]), false, nconv);
 }
 
 // One warp per scene: y = R^-1 g over the cycle's k columns; scenes that
@@ -1167,18 +1235,24 @@ void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int
         mg_setup(D, L, mg_prec);
     }
     const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
-    auto column = [&]() {
+    // a column: [v_j and the V-cycle input], the V-cycle, pass 1, pass 2.  With
+    // the double-float basis pass 2 writes v_{j+1} and the next input, so only
+    // a cycle's first vector needs k_fg_put (after k_fg_start).
+    auto put = [&]() {
         int q2 = tbegin(L, K_FG_PUT);
         launch_pdl(L, k_fg_put, L.nblk_rows, BS_THREADS, 0, D, mgmode);
         tend(L, q2);
+    };
+    auto column = [&]() {
+        if (!D.fg_df) put();
         if (precond) mg_apply(D, L, mg_prec, D.fg_V, D.sp2);
-        q2 = tbegin(L, K_FG_ARN);
-        if (D.fg_df) launch_pdl(L, k_fg_arn1<1>, L.nblk_rows, BS_THREADS, 0, D, precond);
-        else launch_pdl(L, k_fg_arn1<0>, L.nblk_rows, BS_THREADS, 0, D, precond);
+        int q2 = tbegin(L, K_FG_ARN);
+        if (D.fg_df) launch_pdl(L, k_fg_arn1<1>, L.nblk_rows, BS_THREADS, 0, D, precond, d_nconv);
+        else launch_pdl(L, k_fg_arn1<0>, L.nblk_rows, BS_THREADS, 0, D, precond, d_nconv);
         tend(L, q2);
         q2 = tbegin(L, K_FG_ORTH);
-        if (D.fg_df) launch_pdl(L, k_fg_arn2<1>, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
-        else launch_pdl(L, k_fg_arn2<0>, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
+        if (D.fg_df) launch_pdl(L, k_fg_arn2<1>, L.nblk_rows, BS_THREADS, 0, D, d_nconv, mgmode);
+        else launch_pdl(L, k_fg_arn2<0>, L.nblk_rows, BS_THREADS, 0, D, d_nconv, mgmode);
         tend(L, q2);
     };
     IterGraph* G = L.graph;
@@ -1220,6 +1294,7 @@ void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int
         cudaStreamSynchronize(L.stream);
         timer_collect(L.timer, false);
         if (h_nconv[1] >= D.nscene) break;
+        if (D.fg_df) put();
         int it = 0;
         while (it < D.fg_m) {
             cudaMemcpyAsync(h_nconv, d_nconv, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
