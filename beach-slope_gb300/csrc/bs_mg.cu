@@ -276,7 +276,11 @@ __device__ __forceinline__ LevelS view_of(const MgLevel& G, int k) {
 }
 
 // Levels l -> l+1 for coarse cell q of the scene: pre-smooth from zero,
-// residual, restriction (2x2 sum).
+// residual, restriction (2x2 sum).  The smoothed values w r D^-1 of the 4x4
+// fine cells around the box are loaded once and all loads are issued before
+// the sums (one round of memory latency instead of one per child: these
+// levels are bound by their chains of dependent loads); the sums run in the
+// same order as child by child.
 template <typename T>
 __device__ __forceinline__ void op_down(const MgDev& M, const LevelS& F, const LevelS& C, int q) {
     const int I = q % C.ny, J = q / C.ny;
@@ -285,25 +289,42 @@ __device__ __forceinline__ void op_down(const MgDev& M, const LevelS& F, const L
     const T* __restrict__ r = (const T*)M.r[F.l];
     const T w = (T)M.omega;
     T sum = 0;
+    if (!M.prec) {
+        for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {
+                const int fi = 2 * I + a, fj = 2 * J + b;
+                if (fi < F.ny && fj < F.nx) sum += r[F.off + fj * F.ny + fi];
+            }
+        ((T*)M.r[C.l])[C.off + q] = sum;
+        return;
+    }
+    const int fi0 = 2 * I - 1, fj0 = 2 * J - 1;   // the 4x4 neighbourhood's corner
+    T y[4][4], rc[2][2];
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int ni = fi0 + a, nj = fj0 + b;
+            const bool in = ni >= 0 && nj >= 0 && ni < F.ny && nj < F.nx;
+            const int nb = F.off + nj * F.ny + ni;
+            y[b][a] = in ? w * r[nb] * __ldg(dinv + nb) : (T)0;
+            if (a >= 1 && a <= 2 && b >= 1 && b <= 2) rc[b - 1][a - 1] = in ? r[nb] : (T)0;
+        }
+#pragma unroll
     for (int b = 0; b < 2; ++b)
+#pragma unroll
         for (int a = 0; a < 2; ++a) {
             const int fi = 2 * I + a, fj = 2 * J + b;
             if (fi >= F.ny || fj >= F.nx) continue;
             const int c = F.off + fj * F.ny + fi;
-            const T rc = r[c];
-            if (!M.prec) {
-                sum += rc;
-                continue;
-            }
             T ax = 0;
 #pragma unroll
             for (int t = 0; t < 9; ++t) {
                 const int ni = fi + (t % 3) - 1, nj = fj + (t / 3) - 1;
                 if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-                const int nb = F.off + nj * F.ny + ni;
-                ax += __ldg(A + (long)t * F.n + c) * (w * r[nb] * __ldg(dinv + nb));
+                ax += __ldg(A + (long)t * F.n + c) * y[b + t / 3][a + t % 3];
             }
-            sum += rc - ax;
+            sum += rc[b][a] - ax;
         }
     ((T*)M.r[C.l])[C.off + q] = sum;
 }
@@ -369,22 +390,56 @@ __device__ __forceinline__ void op_coarse(const MgDev& M, const LevelS& F, int a
     const T w = (T)M.omega;
     for (int q = threadIdx.x; q < m; q += blockDim.x) z[q] = 0;
     __syncthreads();
-    for (int it = 0; it < M.coarse_sweeps; ++it) {
-        for (int q = threadIdx.x; q < m; q += blockDim.x) {
-            const int i = q % F.ny, j = q / F.ny;
-            const int c = F.off + q;
-            T ax = 0;
+    if (m <= (int)blockDim.x) {
+        // one cell per thread: its stencil, D^-1 and r held in registers
+        // across the sweeps, which then touch shared memory only
+        const int q = threadIdx.x;
+        const bool act = q < m;
+        const int i = q % F.ny, j = q / F.ny;
+        const int c = F.off + q;
+        T a9[9], dc = 0, rcv = 0;
 #pragma unroll
-            for (int t = 0; t < 9; ++t) {
-                const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
-                if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-                ax += __ldg(A + (long)t * F.n + c) * z[nj * F.ny + ni];
-            }
-            z2[q] = z[q] + w * __ldg(dinv + c) * (r[c] - ax);
+        for (int t = 0; t < 9; ++t) {
+            const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+            a9[t] = (act && !(ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx)) ? __ldg(A + (long)t * F.n + c) : (T)0;
         }
-        __syncthreads();
-        for (int q = threadIdx.x; q < m; q += blockDim.x) z[q] = z2[q];
-        __syncthreads();
+        if (act) {
+            dc = __ldg(dinv + c);
+            rcv = r[c];
+        }
+        for (int it = 0; it < M.coarse_sweeps; ++it) {
+            if (act) {
+                T ax = 0;
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+                    if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+                    ax += a9[t] * z[nj * F.ny + ni];
+                }
+                z2[q] = z[q] + w * dc * (rcv - ax);
+            }
+            __syncthreads();
+            if (act) z[q] = z2[q];
+            __syncthreads();
+        }
+    } else {
+        for (int it = 0; it < M.coarse_sweeps; ++it) {
+            for (int q = threadIdx.x; q < m; q += blockDim.x) {
+                const int i = q % F.ny, j = q / F.ny;
+                const int c = F.off + q;
+                T ax = 0;
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+                    if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+                    ax += __ldg(A + (long)t * F.n + c) * z[nj * F.ny + ni];
+                }
+                z2[q] = z[q] + w * __ldg(dinv + c) * (r[c] - ax);
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < m; q += blockDim.x) z[q] = z2[q];
+            __syncthreads();
+        }
     }
     T* out = (T*)M.z[F.l];
     for (int q = threadIdx.x; q < m; q += blockDim.x) out[F.off + q] = acc ? out[F.off + q] + z[q] : z[q];
