@@ -360,17 +360,24 @@ __device__ __forceinline__ void op_up(const MgDev& M, const LevelS& F, const Lev
     const T* __restrict__ e = (const T*)M.z[C.l];
     const T w = (T)M.omega, cs = (T)M.cscale;
     const T wp = M.prec ? w : (T)0;
-    auto zval = [&](int ii, int jj) -> T {
-        const int nb = F.off + jj * F.ny + ii;
-        return wp * r[nb] * __ldg(dinv + nb) + cs * e[C.off + (jj / 2) * C.ny + (ii / 2)];
-    };
-    const T zc = zval(i, j);
+    // every load of the 3x3 neighbourhood issued before the sum (one round
+    // of latency), the sum in stencil order
+    T zv[9], av[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+        const bool in = !(ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx);
+        const int nb = F.off + nj * F.ny + ni;
+        zv[t] = in ? wp * r[nb] * __ldg(dinv + nb) + cs * e[C.off + (nj / 2) * C.ny + (ni / 2)] : (T)0;
+        av[t] = in ? __ldg(A + (long)t * F.n + c) : (T)0;
+    }
+    const T zc = zv[4];
     T ax = 0;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
         if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-        ax += __ldg(A + (long)t * F.n + c) * (t == 4 ? zc : zval(ni, nj));
+        ax += av[t] * zv[t];
     }
     const T v = zc + w * __ldg(dinv + c) * (r[c] - ax);
     T* zo = (T*)M.z[F.l];
