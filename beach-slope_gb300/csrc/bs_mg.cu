@@ -338,14 +338,23 @@ __device__ __forceinline__ void op_resid(const MgDev& M, const LevelS& F, int q)
     const T* __restrict__ A = (const T*)M.A[F.l];
     const T* z = (const T*)M.z[F.l];
     T* r = (T*)M.r[F.l];
+    T zv[9], av[9];   // loads first (one round of latency), then the sum in stencil order
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+        const bool in = !(ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx);
+        zv[t] = in ? z[F.off + nj * F.ny + ni] : (T)0;
+        av[t] = in ? __ldg(A + (long)t * F.n + c) : (T)0;
+    }
+    const T rc = r[c];
     T ax = 0;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
         const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
         if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
-        ax += __ldg(A + (long)t * F.n + c) * z[F.off + nj * F.ny + ni];
+        ax += av[t] * zv[t];
     }
-    r[c] = r[c] - ax;
+    r[c] = rc - ax;
 }
 
 // Levels l+1 -> l for cell q of the scene: prolongation (constant per box,
