@@ -133,37 +133,49 @@ __global__ void k_cell_prefix(Dev D) {
 }
 
 // one block per scene: exclusive scan of the scene's cell totals
+// One block per scene (1024 threads): each thread sums a contiguous run of
+// cells, the run totals are scanned across the block (warp shuffles, then
+// the 32 warp totals), and each thread writes its run's ranges -- two passes
+// over the cells instead of a barrier-bound scan per 1024 cells.
 __global__ void k_scan_cells(Dev D) {
     const int s = blockIdx.x;
     const ScenePar& P = D.par[s];
-    __shared__ int sh[1024];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const int nb = blockDim.x;
-    for (int base = 0; base < P.ncell; base += nb) {
-        const int q = base + threadIdx.x;
-        const int v = (q < P.ncell) ? D.cell_total[P.cell0 + q] : 0;
-        sh[threadIdx.x] = v;
-        __syncthreads();
-        for (int o = 1; o < nb; o <<= 1) {   // Hillis-Steele inclusive scan
-            const int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
-            __syncthreads();
-            sh[threadIdx.x] += t;
-            __syncthreads();
-        }
-        if (q < P.ncell) {
-            const int st = P.row0 + carry + sh[threadIdx.x] - v;
-            D.cell_start2[P.cell0 + q] = st;
-            D.cell_end2[P.cell0 + q] = st + v;
-        }
-        __syncthreads();
-        if (threadIdx.x == nb - 1) carry += sh[nb - 1];
-        __syncthreads();
+    __shared__ int wsum[32];
+    __shared__ int total;
+    const int nb = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = (P.ncell + nb - 1) / nb;
+    const int q0 = t * per, q1 = min(P.ncell, q0 + per);
+    const int* __restrict__ tot = D.cell_total + P.cell0;
+    int loc = 0;
+    for (int q = q0; q < q1; ++q) loc += tot[q];
+    int inc = loc;   // inclusive scan within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
     }
-    if (threadIdx.x == 0) {
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = nb >> 5;
+        int x = lane < nw ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += v;
+        }
+        if (lane < nw) wsum[lane] = x;   // inclusive warp prefix
+        if (lane == nw - 1) total = x;
+    }
+    __syncthreads();
+    int run = P.row0 + (w ? wsum[w - 1] : 0) + inc - loc;
+    for (int q = q0; q < q1; ++q) {
+        const int v = tot[q];
+        D.cell_start2[P.cell0 + q] = run;
+        D.cell_end2[P.cell0 + q] = run + v;
+        run += v;
+    }
+    if (t == 0) {
         D.dyn[s].n_prev = D.dyn[s].n;
-        D.dyn[s].n = carry;
+        D.dyn[s].n = total;
     }
 }
 

@@ -57,7 +57,9 @@ __global__ void k_mg_dinv0(Dev D) {
 // accumulating the row's 9 stencil entries, then one masked warp reduction
 // per (half-cell, entry); lane m keeps entry m and m+32 of the 36 results.
 // An offset beyond one half-cell (a pair split by rounding at a mid-line)
-// is clamped into the stencil.
+// is clamped into the stencil.  Sums in the level's type T (FP32 in the
+// mixed form, from the FP32 copy of the matrix); the neighbour's cell column
+// offset (-1, 0, 1) from two comparisons instead of an integer division.
 template <typename T>
 __global__ void k_mg_gal0(Dev D) {
     BS_PDL_ENTRY();
@@ -69,31 +71,32 @@ __global__ void k_mg_gal0(Dev D) {
     if (c - P.cell0 >= P.ncell) return;   // reserved cells beyond the scene's current grid
     const int celly = P.celly;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
-    const double* A = (const double*)D.aval;
+    const T* A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
     const uint8_t* sub = D.mg.sub;
-    double mine0 = 0.0, mine1 = 0.0;
+    T mine0 = 0, mine1 = 0;
     for (int base = r0; base < r1; base += 32) {
         const int r = base + lane;
-        double acc[9];
+        T acc[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+        for (int k = 0; k < 9; ++k) acc[k] = 0;
         int sb = -1;
         if (r < r1) {
             sb = sub[r];
             const int si = sb & 1, sj = sb >> 1;
-            acc[4] += D.adiag[r];
+            acc[4] += (T)D.adiag[r];
             const int n = D.ncount[r];
             for (int k = 0; k < n; ++k) {
                 const long e = ell(r, k, D.kmax);
                 const int col = D.nidx[e];
                 const int d = D.cell[col] - c;
-                const int dj = (d + celly + 1) / celly - 1;
+                const int u = d + celly + 1;   // in [0, 2 celly + 2] for the 3x3 neighbour cells
+                const int dj = (u >= 2 * celly) ? 1 : ((u >= celly) ? 0 : -1);
                 const int di = d - dj * celly;
                 const int s2 = sub[col];
                 const int dI = min(max(2 * di + (s2 & 1) - si, -1), 1);
                 const int dJ = min(max(2 * dj + (s2 >> 1) - sj, -1), 1);
                 const int q = (dJ + 1) * 3 + (dI + 1);
-                const double v = A[e];
+                const T v = A[e];
 #pragma unroll
                 for (int t = 0; t < 9; ++t)
                     if (t == q) acc[t] += v;
@@ -103,7 +106,7 @@ __global__ void k_mg_gal0(Dev D) {
         for (int t = 0; t < 4; ++t)
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                double v = (sb == t) ? acc[k] : 0.0;
+                T v = (sb == t) ? acc[k] : (T)0;
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                 const int m = t * 9 + k;
                 if (m < 32) { if (lane == m) mine0 += v; }
@@ -116,11 +119,11 @@ __global__ void k_mg_gal0(Dev D) {
     const int lc = c - P.cell0;
     const int i0 = lc % celly, j0 = lc / celly;
     const int o1 = D.mg.off[1][s], ny1 = 2 * celly;
-    auto put = [&](int m, double v) {
+    auto put = [&](int m, T v) {
         const int t = m / 9, k = m - 9 * (m / 9);
         const int Q = o1 + (2 * j0 + (t >> 1)) * ny1 + 2 * i0 + (t & 1);
-        Al[(long)k * n1 + Q] = (T)v;
-        if (k == 4) dl[Q] = (v != 0.0 && isfinite(v)) ? (T)(1.0 / v) : (T)0;
+        Al[(long)k * n1 + Q] = v;
+        if (k == 4) dl[Q] = (v != (T)0 && isfinite(v)) ? (T)1 / v : (T)0;
     };
     put(lane, mine0);
     if (lane < 4) put(lane + 32, mine1);
