@@ -332,6 +332,40 @@ __device__ __forceinline__ void op_down(const MgDev& M, const LevelS& F, const L
     ((T*)M.r[C.l])[C.off + q] = sum;
 }
 
+// One child (a, b) of coarse cell q's 2x2 box: r_c - (A (w D^-1 r))_c, the
+// value op_down adds for it (0 for a child beyond the fine grid); the
+// neighbourhood's loads issued before the sum.
+template <typename T>
+__device__ __forceinline__ T down_child(const MgDev& M, const LevelS& F, const LevelS& C, int q, int a, int b) {
+    const int I = q % C.ny, J = q / C.ny;
+    const int fi = 2 * I + a, fj = 2 * J + b;
+    if (fi >= F.ny || fj >= F.nx) return (T)0;
+    const T* __restrict__ A = (const T*)M.A[F.l];
+    const T* __restrict__ dinv = (const T*)M.dinv[F.l];
+    const T* __restrict__ r = (const T*)M.r[F.l];
+    const T w = (T)M.omega;
+    const int c = F.off + fj * F.ny + fi;
+    const T rc = r[c];
+    if (!M.prec) return rc;
+    T yv[9], av[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = fi + (t % 3) - 1, nj = fj + (t / 3) - 1;
+        const bool in = !(ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx);
+        const int nb = F.off + nj * F.ny + ni;
+        yv[t] = in ? w * r[nb] * __ldg(dinv + nb) : (T)0;
+        av[t] = in ? __ldg(A + (long)t * F.n + c) : (T)0;
+    }
+    T ax = 0;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int ni = fi + (t % 3) - 1, nj = fj + (t / 3) - 1;
+        if (ni < 0 || nj < 0 || ni >= F.ny || nj >= F.nx) continue;
+        ax += av[t] * yv[t];
+    }
+    return rc - ax;
+}
+
 // In-place residual on level l, cell q of the scene: r = r - A z (between
 // the two visits of a W-cycle level; reads its own r and the stencil's z).
 template <typename T>
@@ -465,16 +499,35 @@ __device__ __forceinline__ void op_coarse(const MgDev& M, const LevelS& F, int a
 }
 
 // ---- one launch per level operation
+// A quad of lanes per coarse cell: lane (a, b) smooths child (a, b), the
+// first lane adds the four values in op_down's order (b outer, a inner), so
+// the result is bit-identical to op_down with a quarter of its loads per
+// thread in flight at once.
 template <typename T>
 __global__ void k_mg_down(Dev D, __grid_constant__ const MgLevel F, __grid_constant__ const MgLevel C) {
     BS_PDL_ENTRY();
-    const int Q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (Q >= C.n) return;
-    const int k = scene_at(C, Q);
-    const LevelS c = view_of(C, k);
-    const int q = Q - c.off;
-    if (q >= c.nx * c.ny) return;   // reserved beyond the scene's current grid
-    op_down<T>(D.mg, view_of(F, k), c, q);
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Q = g >> 2, child = g & 3;
+    bool ok = false;
+    int q = 0, k = 0;
+    T val = 0;
+    if (Q < C.n) {
+        k = scene_at(C, Q);
+        q = Q - C.off[k];
+        ok = q < C.nx[k] * C.ny[k];   // not reserved beyond the scene's current grid
+        if (ok) val = down_child<T>(D.mg, view_of(F, k), view_of(C, k), q, child & 1, child >> 1);
+    }
+    const int base = (threadIdx.x & 31) & ~3;
+    const T v0 = __shfl_sync(0xffffffffu, val, base), v1 = __shfl_sync(0xffffffffu, val, base + 1);
+    const T v2 = __shfl_sync(0xffffffffu, val, base + 2), v3 = __shfl_sync(0xffffffffu, val, base + 3);
+    if (ok && child == 0) {
+        T sum = 0;
+        sum += v0;
+        sum += v1;
+        sum += v2;
+        sum += v3;
+        ((T*)D.mg.r[C.l])[C.off[k] + q] = sum;
+    }
 }
 
 template <typename T>
@@ -668,7 +721,7 @@ void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     }
     if (!(need & 2)) return;
     q = tbegin(L, K_MG_DOWN);
-    launch_pdl(L, k_mg_down<T>, gdiv(D.mg.n[l + 1], 128), 128, 0, D, G[l], G[l + 1]);
+    launch_pdl(L, k_mg_down<T>, gdiv(4L * D.mg.n[l + 1], 128), 128, 0, D, G[l], G[l + 1]);
     tend(L, q);
     cycle_t<T>(D, L, l + 1, 0);
     if (l <= D.mg.wlev) {
