@@ -313,11 +313,16 @@ int bs_buffer_exchange(struct bs_ctx* ctx, int32_t scene, int32_t zone);
 int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path, const char* buffer_path);
 
 /* Solver tunables, set by the project autotuner (beach-slope_gb300/autotune.py):
+ * "ppe_solver" (BS_SOLVER_*), "ppe_restart" (FGMRES restart, 1..150),
  * "mg_omega" (Jacobi damping), "mg_cscale" (coarse-correction scale),
  * "mg_pre0" / "mg_prec" (pre-smoothing at the particle / cell levels, 0 or 1),
- * "mg_coarse_sweeps", "mg_wlev" (coarse levels 1..mg_wlev visit the next
- * level twice: W-cycle on top, V-cycle below), "ppe_precond";
- * bs_get_option also reads "mg_levels". */
+ * "mg_post0" (1 or 2 particle-level post-sweeps), "mg_coarse_sweeps",
+ * "mg_wlev" (coarse levels 1..mg_wlev visit the next level twice: W-cycle on
+ * top, V-cycle below), "mg_sub" (0/1: the small levels of a visit as one
+ * clustered launch), "ppe_precond", "fg_df" (0/1, default 1: the FGMRES basis
+ * of the preconditioned mixed solve as double-float (hi, lo) FP32 pairs, its
+ * dots on the FP32 pipe, h_{j+1,j} from the Gram relation);
+ * bs_get_option also reads "mg_levels" and "mg_sub_level". */
 int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
 int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);
 
