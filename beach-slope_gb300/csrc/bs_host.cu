@@ -512,6 +512,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
         float* f;
         rc = dalloc(ctx, &f, E);
         D.aval32 = f;
+        if (!rc) rc = dalloc(ctx, &D.aval_lo, E);
+        if (!rc) rc = dalloc(ctx, &D.zf, R);
         float** fv[] = {&D.fr, &D.fp, &D.fp2, &D.fv, &D.fv2, &D.fs, &D.ft, &D.fd, &D.frhat};
         for (auto q : fv)
             if (!rc) rc = dalloc(ctx, q, R);
@@ -594,6 +596,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     }
     if (!rc && ctx->precision != BS_PREC_MIXED) {   // FP32 matrix copy for an FP32 V-cycle is mixed-only
         D.aval32 = nullptr;
+        D.aval_lo = nullptr;
+        D.zf = nullptr;
     }
     ScenePar* dpar = nullptr;
     SceneDyn* ddyn = nullptr;

@@ -144,6 +144,8 @@ struct Dev {
     // PPE
     void* aval;                     // ELL values (double or float hi)
     float* aval32;                  // mixed: FP32 copy of the values (inner operator)
+    float* aval_lo;                 // mixed: value - aval32 in FP32 (aval32 + aval_lo: 48 bits)
+    float* zf;                      // mixed: the V-cycle output in FP32 (it is FP32-exact)
     double *adiag, *rhs;
     double *sx, *sr, *srhat, *sp, *sp2, *sv, *sv2, *ss, *st, *sxd;  // solver vectors
     float *fr, *fp, *fp2, *fv, *fv2, *fs, *ft, *fd, *frhat;          // mixed inner vectors

@@ -636,8 +636,12 @@ __global__ void k_mg_l0_up(Dev D, double* __restrict__ out, int mode) {
     const T ax = ell_dot<T>(A, idx, zz, r, D.ncount[r], D.kmax, ((const T*)D.mg.adiagT)[r] * zr);
     const T x = ((const T*)D.mg.xin)[r];
     const T v = zr + (T)D.mg.omega * ((const T*)D.mg.dinv0)[r] * (x - ax);
-    if (mode == 1) ((T*)D.mg.u)[r] = v;
-    else out[r] = (double)v;
+    if (mode == 1) {
+        ((T*)D.mg.u)[r] = v;
+    } else {
+        out[r] = (double)v;
+        if (sizeof(T) == 4 && D.zf) D.zf[r] = (float)v;   // the FGMRES pass reads it in FP32
+    }
 }
 
 inline unsigned gdiv(long a, int b) { return (unsigned)((a + b - 1) / b); }

@@ -479,7 +479,9 @@ __global__ void k_mx_convert(Dev D) {
     const int n = D.ncount[r];
     for (int k = 0; k < n; ++k) {
         const long e = ell(r, k, D.kmax);
-        F[e] = (float)A[e];
+        const float h = (float)A[e];
+        F[e] = h;
+        D.aval_lo[e] = __double2float_rn(__dsub_rn(A[e], (double)h));
     }
 }
 
@@ -807,6 +809,46 @@ __device__ void fg_finish_column(const Dev& D, int s, const FgSmall& f, int j, d
     for (int i = threadIdx.x; i <= j + 1; i += BS_THREADS) h[i] = hcol[i];
 }
 
+// s += (a.x + a.y) z for an FP32 z: TwoProduct of the high part, the low
+// part's product into the error, TwoSum into the running sum
+__device__ __forceinline__ void df_fma1(float2& s, float2 a, float z) {
+    const float ph = __fmul_rn(a.x, z);
+    float pe = __fmaf_rn(a.x, z, -ph);
+    pe = __fmaf_rn(a.y, z, pe);
+    const float t = __fadd_rn(s.x, ph);
+    const float v = __fsub_rn(t, s.x);
+    const float e = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, v)), __fsub_rn(ph, v));
+    s.y = __fadd_rn(s.y, __fadd_rn(e, pe));
+    s.x = t;
+}
+
+// Row r of A z for an FP32-exact z (the mixed V-cycle output, zf): the
+// off-diagonal values as double-float pairs (aval32 + aval_lo, 48 bits) and
+// the products and sums on the FP32 pipe; the diagonal term in FP64.
+__device__ __forceinline__ double spmv_row_df(const Dev& D, const float* __restrict__ z, int r) {
+    const float* __restrict__ Ah = D.aval32;
+    const float* __restrict__ Al = D.aval_lo;
+    const int* __restrict__ idx = D.nidx;
+    const int n = D.ncount[r];
+    float2 acc = make_float2(0.f, 0.f);
+    long e = ell(r, 0, D.kmax);
+    int k = 0;
+    for (; k + 4 <= n; k += 4, e += 128) {   // four independent gathers in flight
+        const int j0 = __ldg(idx + e), j1 = __ldg(idx + e + 32), j2 = __ldg(idx + e + 64), j3 = __ldg(idx + e + 96);
+        const float2 a0 = make_float2(__ldg(Ah + e), __ldg(Al + e));
+        const float2 a1 = make_float2(__ldg(Ah + e + 32), __ldg(Al + e + 32));
+        const float2 a2 = make_float2(__ldg(Ah + e + 64), __ldg(Al + e + 64));
+        const float2 a3 = make_float2(__ldg(Ah + e + 96), __ldg(Al + e + 96));
+        const float z0 = z[j0], z1 = z[j1], z2 = z[j2], z3 = z[j3];
+        df_fma1(acc, a0, z0);
+        df_fma1(acc, a1, z1);
+        df_fma1(acc, a2, z2);
+        df_fma1(acc, a3, z3);
+    }
+    for (; k < n; ++k, e += 32) df_fma1(acc, make_float2(__ldg(Ah + e), __ldg(Al + e)), z[__ldg(idx + e)]);
+    return __dadd_rn(__dmul_rn(D.adiag[r], (double)z[r]), df_to_double(acc));
+}
+
 // Pass 1's dots with a double-float basis: the block's w and v_j split into
 // (hi, lo) pairs in shared memory, each lane keeps its 8 rows of both in
 // registers; warp `warp` takes basis vectors warp + 8 (4g + u) as in the FP64
@@ -889,7 +931,7 @@ __global__ void __launch_bounds__(BS_THREADS, 5) k_fg_arn1(Dev D, int precond, i
     double w = 0.0, vj = 0.0;
     float2 vjd = make_float2(0.f, 0.f);
     if (r < rend) {
-        w = spmv_row64(D, u, r);
+        w = DF ? spmv_row_df(D, D.zf, r) : spmv_row64(D, u, r);
         D.sv[r] = w;
         if (DF) vjd = reinterpret_cast<const float2*>(D.fg_V)[col + r];
         else vj = D.fg_V[col + r];
