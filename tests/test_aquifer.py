@@ -238,3 +238,17 @@ def test_reference_solver_gpu_matches_oracle(api, aq, oracle):
         _compare(g, r, name, tol_x=1e-9, tol_p=1e-6)
         assert abs(gi["ppe_iters"] - ri["ppe_iters"]) <= 1, name
         assert gi["err_bits"] == 0, name
+
+
+def test_reference_scene_size(aq):
+    """The scene the reference's defaults give (initialize.f90:21-60): a
+    46 x 14 cell grid, h1 = 18.6 mm, 1,233 wall and 12,448 fluid particles
+    (435 in the two buffers), 25,643 soil grains, 88 + 86 template particles."""
+    from beachslope_gb300 import abi
+    p, st, gr, zones, info = aq.aquifer_scene()
+    assert (p.cellx, p.celly) == (46, 14)
+    assert abs(p.h - 0.0185991365) < 1e-9
+    assert (st["tid"] <= 2).sum() == 1233 and (st["tid"] == abi.TID_FLUID).sum() == 12448
+    assert ((st["flags"] & abi.FLAG_BUFFER) > 0).sum() == 435
+    assert len(gr["x"]) == 25643
+    assert [len(z["x"]) for z in zones] == [88, 86]

@@ -100,3 +100,23 @@ def test_batch_scenes_uneven():
     assert len(set(sizes)) > 1
     slopes = [s[0].dl for s in out]
     assert all(0.02 <= d <= 0.04 for d in slopes)
+
+
+def test_download_into_buffers_host_logic():
+    """abi.state_out with caller buffers: views of their first n rows, and
+    a clear error for buffers that are too short or of the wrong type."""
+    import numpy as np
+    from beachslope_gb300 import abi
+    n = 10
+    into = {f: np.zeros(n + 5) for f in abi.STATE_FIELDS_F64}
+    into.update({f: np.zeros(n + 5, np.int32) for f in abi.STATE_FIELDS_I32})
+    into["flags"] = np.zeros(n + 5, np.uint8)
+    st, out = abi.state_out(n, False, into)
+    assert st.n == n and all(len(v) == n for v in out.values())
+    assert all(np.shares_memory(out[f], into[f]) for f in out)
+    short = dict(into, x=np.zeros(n - 1))
+    with pytest.raises(ValueError):
+        abi.state_out(n, False, short)
+    wrong = dict(into, pid=np.zeros(n + 5))
+    with pytest.raises(ValueError):
+        abi.state_out(n, False, wrong)
