@@ -307,6 +307,10 @@ def aquifer_scene(precision=abi.PREC_FP64, **overrides):
     return p, st, grains, zones, info
 
 
+# the largest step the reference's time-step rule takes (integrator.f90:927-936)
+DT_MAX = 0.005
+
+
 def salinity_setup(state, info):
     """main.f90:156-191: every fluid particle con = -0.5; fluid above the
     coast line denser by rel_den (mass, oden, density) and con = +0.5.
@@ -372,11 +376,23 @@ def run_schedule(ctx, zones, info, settle1=50, settle2=8000, production=None, ou
             zd["rho"] = zones[1]["rho"] * info["rel_den"]
         ctx.set_inflow(z, zd, s)
     phase("salted")
+    # steps run in chunks that cannot reach the next output time or the end:
+    # the time-step rule never takes dt above DT_MAX, so n steps with
+    # n DT_MAX <= (target - t) stay short of it, and the step that crosses a
+    # target is taken alone (the outputs fall on the same steps as one step
+    # at a time, with one host read of t per chunk)
     steps, k = 0, 1
-    while (ctx.info(s)["t"] < info["time"]) if production is None else (steps < production):
-        told = ctx.info(s)["t"]
-        ctx.step(1)
-        steps += 1
+    t = ctx.info(s)["t"]
+    while (t < info["time"]) if production is None else (steps < production):
+        target = k * info["displaytime"]
+        if production is None:
+            target = min(target, info["time"])
+        n = max(1, int((target - t) / DT_MAX))
+        if production is not None:
+            n = min(n, production - steps)
+        told = t
+        ctx.step(n)
+        steps += n
         t = ctx.info(s)["t"]
         if told < k * info["displaytime"] <= t:
             dump(k)

@@ -252,3 +252,39 @@ def test_reference_scene_size(aq):
     assert ((st["flags"] & abi.FLAG_BUFFER) > 0).sum() == 435
     assert len(gr["x"]) == 25643
     assert [len(z["x"]) for z in zones] == [88, 86]
+
+
+def test_production_chunks_keep_output_steps(aq, oracle, tmp_path):
+    """Production runs in chunks of steps that cannot reach the next output
+    time; the outputs land on the same steps as one step at a time (the same
+    files, byte for byte; the oracle on one thread, whose sums are then in a
+    fixed order)."""
+    import os
+    oracle.set_threads(1)
+    try:
+        _chunks_vs_single(aq, oracle, tmp_path)
+    finally:
+        oracle.set_threads(os.cpu_count() or 1)
+
+
+def _chunks_vs_single(aq, oracle, tmp_path):
+    p, st, gr, zones, info = _short(aq, periods=(1.0, 1.0))
+    info = dict(info, displaytime=0.012)
+    a = tmp_path / "chunked"
+    o = oracle.Oracle(p, st, gr)
+    aq.run_schedule(_OracleCtx(o), zones, info, settle1=1, settle2=1, production=30, out_dir=str(a))
+
+    class OneByOne(_OracleCtx):
+        def step(self, n=1):
+            for _ in range(n):
+                self.o.step(1)
+            self.calls = getattr(self, "calls", 0) + n
+
+    b = tmp_path / "single"
+    ob = OneByOne(oracle.Oracle(p, st, gr))
+    aq.run_schedule(ob, zones, info, settle1=1, settle2=1, production=30, out_dir=str(b))
+    names = sorted(f.name for f in (a / "fluid").iterdir())
+    assert names == sorted(f.name for f in (b / "fluid").iterdir())
+    assert names == ["fluid_1000.txt", "fluid_1001.txt", "fluid_1002.txt", "fluid_1003.txt"]
+    for n in names:
+        assert (a / "fluid" / n).read_bytes() == (b / "fluid" / n).read_bytes(), n
