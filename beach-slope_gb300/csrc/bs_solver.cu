@@ -528,6 +528,16 @@ __global__ void k_true_res64(Dev D) {
 // step; a scene whose cycle ended returns at the top of every column kernel,
 // and the column index lives in the scene's state, so one captured chunk of
 // columns serves every cycle.
+//
+// Two forms of a column.  FP64 basis (fg_df = 0): k_fg_put writes v_j and the
+// V-cycle input, pass 1 (k_fg_arn1<0>) the SpMV and the dots, pass 2
+// (k_fg_arn2<0>) the projection, the norm and, in its finisher, the
+// rotations.  Double-float basis (fg_df = 1, the preconditioned mixed solve):
+// the basis is stored as (hi, lo) FP32 pairs and its dots and projection run
+// on the FP32 pipe; pass 1 (k_fg_arn1<1>) also sums u.u and its finisher takes
+// h_{j+1,j} from the Gram relation and runs the rotations, so pass 2
+// (k_fg_arn2<1>) streams v_{j+1} and the next V-cycle input with no reduction
+// and k_fg_put runs once per cycle.
 
 // Per-scene small storage: H [(m+1) x m] column-major (R of the rotated
 // Hessenberg matrix), Gm [(m+1) x (m+1)] (the Gram matrix V^T V of the
