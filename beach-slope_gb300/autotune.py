@@ -94,7 +94,7 @@ def tune(ctx, grains, steps=2, verbose=True):
         [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
         [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
-        [{"mg_omega": w} for w in (0.8, 0.9, 1.0)],
+        [{"mg_omega": w} for w in (0.8, 0.9, 0.95, 1.0)],
         [{"mg_coarse_sweeps": c} for c in (5, 10, 20)],
         [{"mg_sub": 1}],
         [{"mg_post0": 2}],
