@@ -303,3 +303,28 @@ def test_fgmres_scene_solve(oracle):
     assert rc2 == 0
     pa, pb = a.get()["p"], b.get()["p"]
     assert np.linalg.norm(pa - pb) / np.linalg.norm(pb) < 0.05
+
+
+def test_step_runs_the_named_solver(oracle):
+    """The oracle's step solves the PPE with the solver the parameters name
+    (ppe_solver): FGMRES and BiCGStab steps to 1e-12 give the same state, and
+    FGMRES's column count is what the step reports."""
+    from beachslope_gb300 import abi, scene
+    p, st, gr = scene.beach_scene(dx=0.04)
+    p.ppe_tol = 1e-12
+    p.ppe_maxit = 20000
+    q = abi.Params.from_buffer_copy(p)
+    q.ppe_solver = abi.SOLVER_FGMRES
+    q.ppe_restart = 150
+    q.ppe_maxit = 600
+    a, b = oracle.Oracle(p, st, gr), oracle.Oracle(q, st, gr)
+    for o in (a, b):
+        o.stage("prime")
+        o.step(2)
+    ga, gb = a.get(), b.get()
+    np.testing.assert_array_equal(ga["pid"], gb["pid"])
+    assert np.linalg.norm(gb["p"] - ga["p"]) / np.linalg.norm(ga["p"]) < 1e-8
+    assert np.max(np.abs(gb["x"] - ga["x"])) < 1e-12
+    ia, ib = a.info(), b.info()
+    assert ib["ppe_relres"] <= 1e-12 and ib["err_bits"] == 0
+    assert ib["ppe_iters"] != ia["ppe_iters"]   # different methods, different counts
