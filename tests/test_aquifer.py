@@ -288,3 +288,26 @@ def _chunks_vs_single(aq, oracle, tmp_path):
     assert names == ["fluid_1000.txt", "fluid_1001.txt", "fluid_1002.txt", "fluid_1003.txt"]
     for n in names:
         assert (a / "fluid" / n).read_bytes() == (b / "fluid" / n).read_bytes(), n
+
+
+def test_reference_scene_bytes(aq):
+    """Regression pin of the generated scene: SHA-1 over the particles' x,
+    y, p, vx, mass, tid, pid, flags, the grains' x, y and both zones'
+    templates and entry cells (IEEE arithmetic in the reference's operation
+    order, so the bytes are the same on every platform)."""
+    import hashlib
+    p, st, gr, zones, info = aq.aquifer_scene()
+    h = hashlib.sha1()
+    for k in ("x", "y", "p", "vx", "mass"):
+        h.update(np.ascontiguousarray(st[k]).tobytes())
+    h.update(st["tid"].tobytes())
+    h.update(st["pid"].tobytes())
+    h.update(st["flags"].tobytes())
+    for k in ("x", "y"):
+        h.update(gr[k].tobytes())
+    for z in zones:
+        h.update(z["x"].tobytes())
+        h.update(z["y"].tobytes())
+        h.update(z["p"].tobytes())
+        h.update(np.asarray(z["cells"], np.int32).tobytes())
+    assert h.hexdigest() == "9a24ea2262d527380aa3a2fec5920ba942508ae3"
