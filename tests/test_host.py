@@ -120,3 +120,22 @@ def test_download_into_buffers_host_logic():
     wrong = dict(into, pid=np.zeros(n + 5))
     with pytest.raises(ValueError):
         abi.state_out(n, False, wrong)
+
+
+def test_inflow_and_field_structs():
+    """abi.inflow_in / fields_in: the C structs carry the dict's arrays and
+    scalars; None clears a zone; absent fields stay null pointers."""
+    import numpy as np
+    from beachslope_gb300 import abi
+    assert abi.inflow_in(None).n == 0 and abi.inflow_in(None).ncells == 0
+    z = {"x": [1.0, 2.0], "y": [3.0, 4.0], "vx": [0.1, 0.1], "vy": [0.0, 0.0], "p": [5.0, 6.0],
+         "pid": None, "mass": 0.08, "rho": 1000.0, "ovol": 8e-5, "con": -0.5, "period": 391.0,
+         "phase": 8.05, "remove_x": 3.18, "remove_side": 1, "cells": [(5, 44), (6, 44)]}
+    s = abi.inflow_in(z)
+    assert s.n == 2 and s.ncells == 2 and s.remove_side == 1 and not s.pid
+    assert [s.x[k] for k in range(2)] == [1.0, 2.0] and [s.p[k] for k in range(2)] == [5.0, 6.0]
+    assert [(s.cell_i[k], s.cell_j[k]) for k in range(2)] == [(5, 44), (6, 44)]
+    assert (s.mass, s.rho, s.con, s.period, s.phase, s.remove_x) == (0.08, 1000.0, -0.5, 391.0, 8.05, 3.18)
+    f = abi.fields_in({"vx": np.arange(3.0), "con": np.ones(3)})
+    assert f.n == 3 and f.vx[2] == 2.0 and f.con[0] == 1.0
+    assert not f.vy and not f.p and not f.mass
