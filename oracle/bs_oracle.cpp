@@ -736,11 +736,23 @@ void spmv2(const or_scene* s, const std::vector<double>& b, std::vector<double>&
     }
 }
 
-double vecvec(const std::vector<double>& a, const std::vector<double>& b) {   // solver.f90:8-25
-    double res = 0.0;
+// vecvec, solver.f90:8-25.  Each thread sums a fixed contiguous range and the
+// partial sums are added in thread order, so the result depends only on the
+// thread count (an OpenMP reduction clause combines in arrival order); on one
+// thread it is the sequential sum.
+double vecvec(const std::vector<double>& a, const std::vector<double>& b) {
     const long n = (long)a.size();
-#pragma omp parallel for reduction(+ : res) schedule(static)
-    for (long k = 0; k < n; ++k) res = res + a[k] * b[k];
+    std::vector<double> part(omp_get_max_threads(), 0.0);
+#pragma omp parallel
+    {
+        const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        const long lo = n * t / nt, hi = n * (t + 1) / nt;
+        double s = 0.0;
+        for (long k = lo; k < hi; ++k) s = s + a[k] * b[k];
+        part[t] = s;
+    }
+    double res = 0.0;
+    for (double v : part) res = res + v;
     return res;
 }
 
