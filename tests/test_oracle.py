@@ -328,3 +328,18 @@ def test_step_runs_the_named_solver(oracle):
     ia, ib = a.info(), b.info()
     assert ib["ppe_relres"] <= 1e-12 and ib["err_bits"] == 0
     assert ib["ppe_iters"] != ia["ppe_iters"]   # different methods, different counts
+
+
+def test_oracle_reproducible_on_many_threads(oracle):
+    """Two runs of the same steps on the default thread count give the same
+    bits (the dot products add per-thread partial sums in a fixed order)."""
+    from beachslope_gb300 import scene
+    out = []
+    for _ in range(2):
+        p, st, gr = scene.beach_scene(dx=0.03)
+        o = oracle.Oracle(p, st, gr)
+        o.stage("prime")
+        o.step(2)
+        out.append(o.get())
+    for f in ("p", "x", "y", "vx", "con"):
+        np.testing.assert_array_equal(out[0][f], out[1][f], err_msg=f)
