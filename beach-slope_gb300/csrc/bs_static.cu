@@ -22,6 +22,10 @@
 //  * The device address of the array is looked up with cudaGetSymbolAddress
 //    on the first call on each device (that device current) and cached; make
 //    that first call before any stream capture begins.
+//  * Convergence is judged on the recursive residual, as bs_bicgstab_csr
+//    judges it; *relres reports the true residual ||b - A x|| / ||b||
+//    computed after the last iteration.  The flag is read back to the host
+//    every four iterations (the call waits for its stream there).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -106,6 +110,11 @@ __global__ void ks_init(Csr A, const double* __restrict__ b, const double* __res
 // single block: sum the partials in block order and update the scalars
 __global__ void ks_reduce(int nblk, int phase, double tol, int maxit, double* base) {
     const Scr S = carve(base);
+    // the host launches iterations in groups: once a solve has converged the
+    // iteration phases of the rest of the group leave every scalar (and the
+    // iteration count) as they are; the flag is read by the whole block, so
+    // the early return is uniform
+    if (phase >= 1 && phase <= 3 && S.sc[S_CONV] != 0.0) return;
     __shared__ double sh[3 * 32];
     double a[3] = {0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nblk; b += blockDim.x)

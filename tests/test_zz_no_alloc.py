@@ -43,21 +43,50 @@ def test_noalloc_matches_allocating_entry_point(api):
     for rp, col, val, b in systems:   # two calls in a row on the shared scratch
         n = len(b)
         x0 = np.ones(n)
-        rc, xref, _, rr_ref = api.bicgstab_csr(rp, col, val, b, x0, tol=1e-12, maxit=5000)
+        rc, xref, it_ref, rr_ref = api.bicgstab_csr(rp, col, val, b, x0, tol=1e-12, maxit=5000)
         assert rc == 0
-        t_rp = torch.tensor(np.asarray(rp, np.int32), device=dev)
-        t_col = torch.tensor(np.asarray(col, np.int32), device=dev)
-        t_val = torch.tensor(np.asarray(val, np.float64), device=dev)
-        t_b = torch.tensor(np.asarray(b, np.float64), device=dev)
+        t = _device_system(torch, dev, rp, col, val, b)
         t_x = torch.tensor(x0, device=dev)
         torch.cuda.synchronize()
-        rc, it, rr = api.bicgstab_csr_noalloc(n, t_rp.data_ptr(), t_col.data_ptr(), t_val.data_ptr(),
-                                              t_b.data_ptr(), t_x.data_ptr(), tol=1e-12, maxit=5000)
+        rc, it, rr = api.bicgstab_csr_noalloc(n, *t, t_x.data_ptr(), tol=1e-12, maxit=5000)
         x = t_x.cpu().numpy()
         assert rc == 0, rc
         assert rr <= 1e-11
+        # the same recurrence: the same number of iterations
+        assert it == it_ref, (it, it_ref)
         # the tolerance the parity tests use for converged FP64 solves
         assert np.linalg.norm(x - xref) / np.linalg.norm(xref) < 1e-9
+
+
+def _device_system(torch, dev, rp, col, val, b):
+    ts = [torch.tensor(np.asarray(rp, np.int32), device=dev), torch.tensor(np.asarray(col, np.int32), device=dev),
+          torch.tensor(np.asarray(val, np.float64), device=dev), torch.tensor(np.asarray(b, np.float64), device=dev)]
+    _device_system.keep = ts   # the tensors must outlive the call
+    return [q.data_ptr() for q in ts]
+
+
+def test_noalloc_iteration_count(api):
+    """An exact initial guess takes no iteration; a capped solve stops at
+    maxit, reports maxit iterations and the not-converged status, as the
+    allocating entry point does."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    b = np.array([8.0, 6.0, 4.0, 9.0, 8.0])
+    t = _device_system(torch, dev, KAT_ROW, KAT_COL, np.ones(13), b)
+    t_x = torch.tensor(np.arange(1.0, 6.0), device=dev)   # solvertest.f90's solution
+    torch.cuda.synchronize()
+    rc, it, rr = api.bicgstab_csr_noalloc(5, *t, t_x.data_ptr(), tol=1e-12, maxit=5)
+    assert (rc, it) == (0, 0)
+    assert rr == 0.0
+    rp, col, val, b = _ppe_csr(api)
+    for maxit in (1, 3, 5, 6):
+        rc_ref, _, it_ref, _ = api.bicgstab_csr(rp, col, val, b, np.zeros(len(b)), tol=1e-14, maxit=maxit)
+        t = _device_system(torch, dev, rp, col, val, b)
+        t_x = torch.zeros(len(b), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        rc, it, rr = api.bicgstab_csr_noalloc(len(b), *t, t_x.data_ptr(), tol=1e-14, maxit=maxit)
+        assert rc == -5 and rc_ref == -5, (rc, rc_ref)   # BS_E_NOTCONV
+        assert it == maxit == it_ref, (it, maxit, it_ref)
 
 
 def test_noalloc_rejects_oversize(api):
