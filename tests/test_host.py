@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
-def test_struct_layouts_match_c():
+def test_struct_layouts_match_c(tmp_path):
     from beachslope_gb300 import abi
     src = r'''
     #include <stdio.h>
@@ -42,8 +42,7 @@ def test_struct_layouts_match_c():
              offsetof(bs_scene_info, err_bits));
       return 0; }
     '''
-    tmp = os.path.join(ROOT, "_work")
-    os.makedirs(tmp, exist_ok=True)
+    tmp = str(tmp_path)
     c_file = os.path.join(tmp, "layout_check.c")
     exe = os.path.join(tmp, "layout_check")
     with open(c_file, "w") as f:
