@@ -88,6 +88,9 @@ def _load():
         "bs_kernel_timing_get": (C.c_int, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(i32),
                                            C.POINTER(C.c_double)]),
         "bs_launch_count": (C.c_int64, [vp]),
+        "bs_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+        "bs_device_memory": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+        "bs_context_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -128,7 +131,7 @@ class Context:
         self.tuning = None
         if tuning == "auto":   # solver options picked by the autotuner for this size class
             from . import autotune
-            self.tuning = autotune.apply(self, params[0].precision, sum(caps))
+            self.tuning = autotune.apply(self, params[0].precision, sum(caps), n)
         elif isinstance(tuning, dict):
             for k, v in tuning.items():
                 self.set_option(k, v)
@@ -313,6 +316,12 @@ class Context:
     def launch_count(self):
         return int(lib.bs_launch_count(self.h))
 
+    def device_bytes(self):
+        """Device bytes the context holds."""
+        v = C.c_size_t()
+        self._check(lib.bs_context_bytes(self.h, C.byref(v)), "context_bytes")
+        return int(v.value)
+
 
 for _name in STAGE_FUNCS:
     def _mk(nm):
@@ -366,6 +375,24 @@ def set_device(device):
     rc = lib.bs_set_device(int(device))
     if rc != 0:
         raise BeachSlopeError(f"bs_set_device({device}) failed ({rc})")
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    f, t = C.c_size_t(), C.c_size_t()
+    rc = lib.bs_device_memory(C.byref(f), C.byref(t))
+    if rc != 0:
+        raise BeachSlopeError(f"bs_device_memory failed ({rc})")
+    return f.value, t.value
+
+
+def measure_fp64_peak():
+    """FP64 TFLOP/s of the current device (chains of dependent DFMAs on every SM)."""
+    v = C.c_double()
+    rc = lib.bs_measure_fp64_peak(C.byref(v))
+    if rc != 0:
+        raise BeachSlopeError(f"bs_measure_fp64_peak failed ({rc})")
+    return v.value
 
 
 def bicgstab_csr(row_ptr, col, val, b, x0, tol=1e-12, maxit=1000, rule=abi.STOP_RELRES):

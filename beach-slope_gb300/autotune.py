@@ -28,8 +28,10 @@ def bucket(n_particles):
     return str(int(round(math.log(max(n_particles, 1), 4))))
 
 
-def key(precision, n_particles):
-    return f"prec{precision}_n4^{bucket(n_particles)}"
+def key(precision, n_particles, scenes=1):
+    """Cache key: precision, size class and, for a batch, a scene-count class."""
+    k = f"prec{precision}_n4^{bucket(n_particles)}"
+    return k if scenes <= 1 else k + f"_s4^{bucket(scenes)}"
 
 
 def load():
@@ -40,8 +42,17 @@ def load():
         return {}
 
 
-def lookup(precision, n_particles):
-    return load().get(key(precision, n_particles))
+def lookup(precision, n_particles, scenes=1):
+    """The entry of this size class (and scene-count class); otherwise the
+    single-scene entry of the nearest size class of the same precision."""
+    d = load()
+    for k in (key(precision, n_particles, scenes), key(precision, n_particles)):
+        if k in d:
+            return d[k]
+    b = int(bucket(n_particles))
+    near = sorted((abs(int(k.split("^")[1]) - b), k) for k in d
+                  if k.startswith(f"prec{precision}_n4^") and "_s4^" not in k)
+    return d[near[0][1]] if near else None
 
 
 def _measure(ctx, steps):
@@ -118,15 +129,15 @@ def tune(ctx, grains, steps=2, verbose=True):
     return best, best_ms, table
 
 
-def save(precision, n_particles, best, best_ms, workload):
+def save(precision, n_particles, best, best_ms, workload, scenes=1):
     d = load()
-    d[key(precision, n_particles)] = {"options": best, "ms_per_step": best_ms, "workload": workload}
+    d[key(precision, n_particles, scenes)] = {"options": best, "ms_per_step": best_ms, "workload": workload}
     with open(CACHE, "w") as f:
         json.dump(d, f, indent=1, sort_keys=True)
 
 
-def apply(ctx, precision, n_particles):
-    t = lookup(precision, n_particles)
+def apply(ctx, precision, n_particles, scenes=1):
+    t = lookup(precision, n_particles, scenes)
     if t:
         # the restart length before the method, so FGMRES storage is sized once
         for k in sorted(t["options"], key=lambda k: OPTIONS.index(k) if k in OPTIONS else len(OPTIONS)):
@@ -140,9 +151,24 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--dx", type=float, nargs="+", default=[0.00125, 0.0025, 0.01])
     ap.add_argument("--precision", nargs="+", default=["mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=0,
+                    help="tune the batch of this many seeded beach scenes instead of single scenes")
     args = ap.parse_args()
     for prec_name in args.precision:
         prec = abi.PREC_MIXED if prec_name == "mixed" else abi.PREC_FP64
+        if args.batch:
+            scenes = scene.batch_scenes(args.batch, precision=prec)
+            P, S, G = [q[0] for q in scenes], [q[1] for q in scenes], [q[2] for q in scenes]
+            ctx = api.Context(P, S, G)
+            ctx.prime()
+            ctx.step(2)
+            n = sum(len(q["x"]) for q in S)
+            print(f"{prec_name} batch of {len(P)} scenes, n={n}", flush=True)
+            best, ms, _ = tune(ctx, G)
+            print(f"  best {best} {ms:.2f} ms/step", flush=True)
+            save(prec, n, best, ms, f"batch of {len(P)} beach scenes", scenes=len(P))
+            ctx.close()
+            continue
         for dx in args.dx:
             p, st, gr = scene.beach_scene(dx=dx, precision=prec)
             ctx = api.Context([p], [st], [gr])

@@ -16,7 +16,7 @@ INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
-SOURCES = ["bs_bin.cu", "bs_sweep.cu", "bs_solver.cu", "bs_mg.cu", "bs_static.cu", "bs_host.cu"]
+SOURCES = ["bs_bin.cu", "bs_sweep.cu", "bs_solver.cu", "bs_mg.cu", "bs_static.cu", "bs_probe.cu", "bs_host.cu"]
 
 
 def nvcc():

@@ -35,6 +35,7 @@ struct bs_ctx {
     int* h_pinned = nullptr;   // [0] converged counter, [1..] solsteps per scene
     int* d_nconv = nullptr;
     std::vector<void*> allocs;
+    std::vector<size_t> alloc_bytes;   // size of each entry of allocs
     bool assembled = false;
     bool disp_ready = false;
     int max_solsteps = 1;
@@ -85,6 +86,7 @@ int dalloc(bs_ctx* ctx, T** p, size_t n) {
     if (e != cudaSuccess) return fail(ctx, BS_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     cudaMemset(q, 0, n * sizeof(T));
     ctx->allocs.push_back(q);
+    ctx->alloc_bytes.push_back(n * sizeof(T));
     *p = (T*)q;
     return 0;
 }
@@ -95,6 +97,7 @@ void dfree(bs_ctx* ctx, T*& p) {
     for (size_t i = 0; i < ctx->allocs.size(); ++i)
         if (ctx->allocs[i] == (void*)p) {
             ctx->allocs.erase(ctx->allocs.begin() + i);
+            ctx->alloc_bytes.erase(ctx->alloc_bytes.begin() + i);
             break;
         }
     cudaFree(p);
@@ -1639,5 +1642,18 @@ int bs_kernel_timing_get(bs_ctx* ctx, int32_t idx, const char** name, int32_t* l
     return 0;
 }
 int64_t bs_launch_count(bs_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int bs_device_memory(size_t* free_bytes, size_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return BS_E_ARG;
+    return cudaMemGetInfo(free_bytes, total_bytes) == cudaSuccess ? BS_OK : BS_E_CUDA;
+}
+
+int bs_context_bytes(bs_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return BS_E_ARG;
+    size_t t = 0;
+    for (size_t b : ctx->alloc_bytes) t += b;
+    *bytes = t;
+    return BS_OK;
+}
 
 }  // extern "C"

@@ -29,7 +29,7 @@
 // constants with the reference's literal precision (default REAL = single)
 #define BS_C28 ((double)(28.0f * 3.14f))   // kernel.f90:61
 #define BS_C3 ((double)(3.0f * 3.14f))     // kernel.f90:62
-#define BS_SP1EM5 ((double)1e-5f)          // functions.f90:324
+#define BS_SP1EM5 ((double)1e-5f)          // functions.f90:75, solver.f90:235
 #define BS_SP1EM6 ((double)1e-6f)          // integrator.f90:581
 #define BS_SP1EM9 ((double)1e-9f)          // scalar.f90:246 (Dm)
 

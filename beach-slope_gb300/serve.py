@@ -15,6 +15,14 @@ as running it alone: the batch computes every scene's reductions, multigrid
 hierarchy and solver convergence on its own.
 
 Latency of a request = completion time - arrival time (queueing included).
+
+Admission by free device memory: `Server.for_memory` lays the slot table out
+at start within a budget taken from the device's free memory (cudaMemGetInfo
+through bs_device_memory): each size class gets its share of the budget, and
+as many slots as that share holds at the measured device bytes per row of a
+calibration context (capped by the class's concurrency limit).  A request
+waits in the queue until a free slot of a class that holds it exists; one
+larger than every slot is rejected at once.
 """
 import collections
 import time
@@ -43,11 +51,62 @@ class Server:
         self.ctx.prime()
 
     @staticmethod
-    def slots_for_memory(template, rows, grains, budget_bytes, bytes_per_row=2600.0, max_slots=64):
+    def slot_bytes(template, rows, grains, bytes_per_row):
+        """Device bytes one slot of `rows` rows reserves: the per-row arrays
+        (particles, neighbour list, matrix, multigrid, Krylov basis) at the
+        measured bytes per row, the grains and the per-cell arrays."""
+        return rows * bytes_per_row + grains * 40.0 + template.cellx * template.celly * 120.0
+
+    @staticmethod
+    def slots_for_memory(template, rows, grains, budget_bytes, bytes_per_row, max_slots=64):
         """How many slots of one template fit in `budget_bytes` of device
-        memory (admission by free HBM when the pool is laid out)."""
-        per = rows * bytes_per_row + grains * 40.0 + template.cellx * template.celly * 4 * 120.0
-        return int(max(1, min(max_slots, budget_bytes // per)))
+        memory (0 when not even one does)."""
+        per = Server.slot_bytes(template, rows, grains, bytes_per_row)
+        return int(max(0, min(max_slots, budget_bytes // per)))
+
+    @staticmethod
+    def plan(classes, budget_bytes, bytes_per_row):
+        """Slot table within a memory budget.  classes = [(template params,
+        rows, grains, share of the budget, concurrency limit)]; returns the
+        number of slots of each class and the bytes they reserve."""
+        counts, used = [], 0.0
+        for t, rows, grains, share, limit in classes:
+            k = Server.slots_for_memory(t, rows, grains, share * budget_bytes, bytes_per_row, limit)
+            counts.append(k)
+            used += k * Server.slot_bytes(t, rows, grains, bytes_per_row)
+        return counts, used
+
+    @staticmethod
+    def calibrate(params, state, grains, tuning=None):
+        """Measured device bytes per row of a one-scene context holding
+        `state` at 1.3x its rows, after prime and one production step (the
+        Krylov basis is allocated at the first solve)."""
+        rows = int(1.3 * len(state["x"]))
+        ng = int(1.3 * len(grains["x"])) + 64 if grains is not None else 64
+        c = api.Context([params], [state], [grains], capacity=[rows], grain_capacity=[ng], tuning=tuning)
+        c.prime()
+        c.step(1)
+        b = c.device_bytes()
+        c.close()
+        return b / rows
+
+    @classmethod
+    def for_memory(cls, classes, bytes_per_row, budget_bytes=None, fraction=0.5, tuning=None):
+        """A server whose slot table is laid out within `budget_bytes`
+        (default: `fraction` of the device's free memory now)."""
+        if budget_bytes is None:
+            free, _ = api.device_memory()
+            budget_bytes = fraction * free
+        counts, used = cls.plan(classes, budget_bytes, bytes_per_row)
+        if not any(counts):
+            raise MemoryError("no slot fits the device memory budget")
+        templates = []
+        for (t, rows, grains, _, _), k in zip(classes, counts):
+            templates += [(t, rows, grains)] * k
+        srv = cls(templates, tuning=tuning)
+        srv.budget_bytes, srv.planned_bytes, srv.bytes_per_row = budget_bytes, used, bytes_per_row
+        srv.class_counts = counts
+        return srv
 
     def fits(self, slot, req):
         t = self.templates[slot]
@@ -75,10 +134,15 @@ class Server:
         out = {}
         i = 0
         self.step_ms = []
+        self.rejected = []
         while i < len(reqs) or queue or active:
             tnow = now()
             while i < len(reqs) and reqs[i].arrival <= tnow:
-                queue.append(reqs[i])
+                if any(self.fits(k, reqs[i]) for k in range(self.nslots)):
+                    queue.append(reqs[i])
+                else:   # no slot of the table can ever hold it
+                    self.rejected.append(reqs[i].rid)
+                    out[reqs[i].rid] = {"error": "larger than every slot", "arrival": reqs[i].arrival}
                 i += 1
             # admission in arrival order; a request that fits no free slot
             # waits, and later requests that fit may pass it

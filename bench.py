@@ -142,13 +142,25 @@ def peaks():
         return 6800.0, "fallback"
 
 
+_FP64_PEAK = None
+
+
+def fp64_peak():
+    """FP64 TFLOP/s of this GPU, measured once by the library's DFMA-chain probe."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        from beachslope_gb300 import api
+        _FP64_PEAK = api.measure_fp64_peak()
+    return _FP64_PEAK
+
+
 # ------------------------------------------------------------- our arm
 # Kernels bracketed by CUDA events during the timed region (the candidates for
 # the dominant kernel).
 TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down", "mg_l0_up",
                  "fg_arnoldi_spmv", "fg_project")
 # DRAM bytes per launch measured by ncu over the algorithmic bytes of the same
-# launch (0.18 M-particle beach, mixed; profiles/*_beach_dx0.0025_mixed.md);
+# launch (ncu dram__bytes_read.sum + dram__bytes_write.sum on the 0.18 M-particle beach, mixed);
 # the traffic grows with the nonzeros and rows, so the ratio scales it to the
 # bench's workload.  k_it2_64 has k_it1_64's access pattern.
 TRAFFIC_RATIO = {"search_effpor": 0.46, "bicg_it1_spmv": 0.99, "bicg_it2_spmv": 0.99,
@@ -291,19 +303,102 @@ def run_ours(args, D):
               and int(ctx.get_option("fg_df")) == 1 and P[0].ppe_precond == 1)
         fl = fp64_flops(ctx, name, fg_reads / max(fg_launches, 1), df)
         if fl:
+            f64pk = fp64_peak()
             out["roofline"]["fp64"] = {"flops_per_launch": round(fl), "achieved_tflops": round(fl / avg_s / 1e12, 3),
-                                       "nominal_peak_tflops": 1.25,
-                                       "frac": round(fl / avg_s / 1e12 / 1.25, 3)}
+                                       "peak_tflops": round(f64pk, 3),
+                                       "peak_source": "measured (bs_measure_fp64_peak: dependent DFMA chains)",
+                                       "frac": round(fl / avg_s / 1e12 / f64pk, 3)}
             if df:
                 out["roofline"]["fp64"]["note"] = ("basis dots, projection and off-diagonal SpMV in "
                                                    "double-float on the FP32 pipe")
+        out["step_roofline"] = step_roofline(ctx, kt, fg_reads, fg_launches, args, ms_timed, pk, src)
     state = ctx.download(0)
     ctx.close()
     if not args.no_e2e:
         out["e2e"] = run_e2e(args, D, P, S, G)
     if args.precision == "mixed" and not args.no_fp64:
         out["fp64"] = run_fp64_and_accuracy(args, P, S, G, state)
+        out["fp64"]["trajectory_vs_fp64"] = trajectory_errors(args, P, S, G)
     return out
+
+
+# Per-particle algorithmic bytes of one production step outside the PPE solve,
+# stage by stage (own fields read + written once; neighbour index lists at 4 B
+# per entry for each sweep that reads them): pos words are 8 B, the other
+# words w (8 FP64, 4 mixed).  Stages: projection (isph.f90:17), two re-bins
+# (integrator.f90:33,251), two searches (search.f90:310), two effpor
+# (porous.f90:107), two eddyvis (turbulence.f90:12), int_vel
+# (integrator.f90:459), assembly (isph.f90:136), comp_vel (integrator.f90:705),
+# comp_pos (integrator.f90:845), freesurf (isph.f90:49), opt2_shift
+# (part_shift.f90:12), densityupdate (scalar.f90:399), timestep
+# (integrator.f90:885), one scalar sub-step (scalar.f90:242).
+SWEEP_POS_WORDS = 6 + 12 + 4 + 4 + 2 + 2 + 2 + 6 + 4 + 2           # 44
+SWEEP_W_WORDS = 3 + 32 + 16 + 14 + 18 + 16 + 12 + 13 + 3 + 1 + 10 + 6 + 2 + 11   # 157
+SWEEP_LIST_READS = 2 + 2 + 1 + 1 + 1 + 1 + 1 + 1                    # index lists read (4 B per entry)
+
+
+def sweep_bytes_per_particle(K, precision):
+    """Algorithmic bytes per particle of one step outside the PPE solve, plus
+    the assembled matrix written once ((K+1) values of 8 B and 4 B indices)."""
+    w = 4 if precision == "mixed" else 8
+    return SWEEP_POS_WORDS * 8 + SWEEP_W_WORDS * w + 16 + SWEEP_LIST_READS * 4 * K + K + (K + 1) * 12
+
+
+def step_roofline(ctx, kt, fg_reads, fg_launches, args, ms_timed, pk, src):
+    """Whole-step roofline: the algorithmic bytes of one step (the sweeps per
+    particle from sweep_bytes_per_particle, plus the solver kernels' launches
+    in the event-timed pass at their per-launch algorithmic bytes) over the
+    measured time of a step."""
+    n = sum(len(ctx.neighbour_counts(s)) for s in range(ctx.nscenes))
+    K = float(np.mean(np.concatenate([ctx.neighbour_counts(s) for s in range(ctx.nscenes)])))
+    sweeps = n * sweep_bytes_per_particle(K, args.precision)
+    solver = 0.0
+    for name in ("fg_arnoldi_spmv", "fg_project", "mg_l0_down", "mg_l0_up", "bicg_it1_spmv", "bicg_it2_spmv"):
+        cnt = kt.get(name, (0, 0.0))[0]
+        if cnt:
+            solver += cnt * algorithmic_bytes(ctx, name, args.precision,
+                                              basis_reads=fg_reads / max(fg_launches, 1))
+    per_step = sweeps + solver / args.steps
+    t = ms_timed / args.steps / 1e3
+    return {"bound": "hbm", "achieved": round(per_step / t / 1e9, 1), "peak": pk, "peak_source": src,
+            "unit": "GB/s", "frac": round(per_step / t / 1e9 / pk, 4),
+            "bytes_per_step": round(per_step), "sweep_bytes_per_step": round(sweeps),
+            "solver_bytes_per_step": round(solver / args.steps), "mean_neighbours": round(K, 2),
+            "ms_per_step": round(ms_timed / args.steps, 3),
+            "note": "time of the event-timed pass; coarse multigrid levels and scene sums counted as zero bytes"}
+
+
+def trajectory_errors(args, P, S, G):
+    """Mixed and FP64 from the same initial state, stepped side by side for
+    the timed number of steps (each with its own tuned solver, PPE to the
+    configured tolerance): rel-L2 of p, vx, vy and con between the two after
+    every step, paired by particle id; max over the steps and the last."""
+    from beachslope_gb300 import abi, api
+    ctxs = []
+    for prec in (abi.PREC_MIXED, abi.PREC_FP64):
+        Q = [abi.Params.from_buffer_copy(p) for p in P]
+        for q in Q:
+            q.precision = prec
+        c = api.Context(Q, S, G, tuning="auto")
+        c.prime()
+        ctxs.append(c)
+    fields = ("p", "vx", "vy", "con")
+    per = {f: [] for f in fields}
+    for _ in range(args.steps):
+        for c in ctxs:
+            c.step(1)
+        a, b = ctxs[0].download(0, full=False), ctxs[1].download(0, full=False)
+        oa, ob = np.argsort(a["pid"]), np.argsort(b["pid"])
+        if not np.array_equal(a["pid"][oa], b["pid"][ob]):
+            return {"error": "particle sets differ"}
+        for f in fields:
+            per[f].append(float(np.linalg.norm(a[f][oa] - b[f][ob]) / max(np.linalg.norm(b[f]), 1e-300)))
+    for c in ctxs:
+        c.close()
+    return {"steps": args.steps, "ppe_tol": P[0].ppe_tol,
+            "max": {f: max(v) for f, v in per.items()}, "last": {f: v[-1] for f, v in per.items()},
+            "per_step": {f: [float("%.3g" % e) for e in v] for f, v in per.items()},
+            "note": "mixed vs FP64 trajectories from one initial state, compared after every step"}
 
 
 def run_fp64_and_accuracy(args, P, S, G, state):
@@ -419,6 +514,9 @@ def run_reference(args, D, budget_s=150.0):
 
 
 def cpu_baseline(args):
+    """One production step of the oracle (all host threads) on the full
+    workload: the CPU baseline, and the checker of one GPU step from the same
+    initial state in both precision forms (returned as a second dict)."""
     from oracle import oracle
     from beachslope_gb300 import abi
     threads = os.cpu_count() or 1
@@ -429,8 +527,136 @@ def cpu_baseline(args):
     t0 = time.perf_counter()
     o.step(1)
     t = time.perf_counter() - t0
-    return {"value": o.n / t, "unit": UNIT, "cores": threads, "kind": "port",
+    base = {"value": o.n / t, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"1 production step of the full {args.workload} scene ({o.n} particles), {t:.1f} s"}
+    return base, oracle_parity(o, P, S, G)
+
+
+def oracle_parity(o, P, S, G):
+    """One production step of the GPU (FP64 drop-in and mixed form, each with
+    its tuned solver) from the oracle's initial state, against the oracle's
+    step: particle order and neighbour lists bit-exact (FP64), rel-L2 of p,
+    vx, vy, con and the largest position difference.  Both solve the PPE to
+    the workload's tolerance, so the pressure differs at the level of that
+    tolerance (different Krylov methods stop at different iterates)."""
+    from beachslope_gb300 import abi, api
+    r = o.get()
+    kmax = P[0].kmax
+    co, io, do, _, _ = o.neighbours(kmax)
+    out = {"steps": 1, "ppe_tol": P[0].ppe_tol, "oracle_solver": "BiCGStab (solver.f90:129-254), true-residual stop"}
+    for name, prec in (("fp64", abi.PREC_FP64), ("mixed", abi.PREC_MIXED)):
+        Q = abi.Params.from_buffer_copy(P[0])
+        Q.precision = prec
+        c = api.Context([Q], S, G, tuning="auto")
+        c.prime()
+        c.step(1)
+        g = c.download(0)
+        res = {"order_equal": bool(np.array_equal(g["pid"], r["pid"]))}
+        if prec == abi.PREC_FP64:
+            cg, ig, dg, _, _ = c.neighbours()
+            m = np.arange(kmax)[None, :] < co[:, None]
+            res["neighbour_sets_equal"] = bool(np.array_equal(cg, co) and np.array_equal(ig[m], io[m]))
+            if res["neighbour_sets_equal"]:   # positions differ in the last bits after the step
+                res["pair_dist_max_rel"] = float(np.max(np.abs(dg[m] - do[m]) / do[m]))
+            res["mean_neighbours"] = round(float(co.mean()), 3)
+            del cg, ig, dg
+        og, orr = np.argsort(g["pid"]), np.argsort(r["pid"])
+        if np.array_equal(g["pid"][og], r["pid"][orr]):
+            for f in ("p", "vx", "vy", "con"):
+                res[f"{f}_rel_l2"] = float(np.linalg.norm(g[f][og] - r[f][orr]) / max(np.linalg.norm(r[f]), 1e-300))
+            res["x_max_abs"] = float(max(np.max(np.abs(g["x"][og] - r["x"][orr])),
+                                         np.max(np.abs(g["y"][og] - r["y"][orr]))))
+        res["ppe_iters"] = c.info(0)["ppe_iters"]
+        c.close()
+        out[name] = res
+    out["oracle_ppe_iters"] = o.info()["ppe_iters"]
+    return out
+
+
+def run_config1(args):
+    """The 13 k-particle beach (dx = 10 mm) over 2000 production steps: the
+    FP64 drop-in and the mixed form on the GPU (CUDA events), and the oracle
+    on the host cores over a bounded sample of the same steps."""
+    from oracle import oracle
+    from beachslope_gb300 import abi, api, scene
+    steps = args.config1_steps
+    out = {"workload": "beach_dx0.01", "steps": steps}
+    for name, prec in (("fp64", abi.PREC_FP64), ("mixed", abi.PREC_MIXED)):
+        p, st, gr = scene.beach_scene(dx=0.01, precision=prec)
+        c = api.Context([p], [st], [gr], tuning="auto")
+        c.prime()
+        c.step(3)
+        c.sync()
+        c.record(0)
+        c.step(steps)
+        c.record(1)
+        ms = c.elapsed_ms(0, 1)
+        n = len(st["x"])
+        out["particles"] = n
+        out[name] = {"value": n * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                     "err_bits": c.info(0)["err_bits"]}
+        c.close()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    p, st, gr = scene.beach_scene(dx=0.01)
+    o = oracle.Oracle(p, st, gr)
+    o.stage("prime")
+    o.step(1)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps and time.perf_counter() - t0 < args.config1_cpu_s:
+        o.step(10)
+        done += 10
+    t = time.perf_counter() - t0
+    out["cpu_oracle"] = {"value": o.n * done / t, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{done} production steps after 1 warm-up step, {t:.1f} s"}
+    return out
+
+
+def run_config3(args):
+    """Standalone search + PPE on the 1000 x 1000 jittered lattice (1 M
+    particles, free surface on the top row, walls on three sides, N(0,1)
+    source): search, effpor + int_vel, assembly and the solve to 1e-8 timed
+    by CUDA events in both precision forms; neighbour sets compared, and the
+    mixed pressure against the FP64 one."""
+    from beachslope_gb300 import abi, api, scene
+    out = {"workload": "lattice_1000x1000", "ppe_tol": 1e-8}
+    sol, nb = {}, {}
+    for name, prec in (("fp64", abi.PREC_FP64), ("mixed", abi.PREC_MIXED)):
+        p, st, gr = scene.lattice_scene(n=1000, dx=1e-3)
+        p.precision = prec
+        p.ppe_tol = 1e-8
+        c = api.Context([p], [st], [None], tuning="auto")
+        out["particles"] = len(st["x"])
+        b = np.random.default_rng(20261203).standard_normal(len(st["x"]))
+        c.sync()
+        c.record(0)
+        c.search()
+        c.record(1)
+        c.porosity()
+        c.int_vel()
+        c.record(2)
+        c.ppe_assemble()
+        c.record(3)
+        c.sync()
+        c.set_rhs(b)
+        c.record(4)
+        c.ppe_solve()
+        c.record(5)
+        ms = [c.elapsed_ms(0, 1), c.elapsed_ms(1, 2), c.elapsed_ms(2, 3), c.elapsed_ms(4, 5)]
+        inf = c.info(0)
+        out[name] = {"search_ms": ms[0], "effpor_int_vel_ms": ms[1], "assemble_ms": ms[2], "solve_ms": ms[3],
+                     "total_ms": sum(ms), "ppe_iters": inf["ppe_iters"], "ppe_relres": inf["ppe_relres"],
+                     "err_bits": inf["err_bits"]}
+        sol[name] = c.download(0, full=False)["p"]
+        cnt, idx, *_ = c.neighbours()
+        nb[name] = (cnt, idx)
+        c.close()
+    m = np.arange(nb["fp64"][1].shape[1])[None, :] < nb["fp64"][0][:, None]
+    out["neighbour_sets_equal"] = bool(np.array_equal(nb["fp64"][0], nb["mixed"][0])
+                                       and np.array_equal(nb["fp64"][1][m], nb["mixed"][1][m]))
+    out["p_rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(sol["mixed"] - sol["fp64"]) / np.linalg.norm(sol["fp64"]))
+    return out
 
 
 def run_batched(args):
@@ -445,17 +671,23 @@ def run_batched(args):
     out = {"scenes": len(P), "particles": n, "particles_min": min(len(s["x"]) for s in S),
            "particles_max": max(len(s["x"]) for s in S), "steps": args.batch_steps,
            "description": "slope 1:5-1:20, A 0.02-0.10 m, porosity 0.3-0.5, dx 5-20 mm log-uniform (seeded)"}
-    for mode in ("isph", "wcsph"):
+    final = {}
+    for mode in ("isph", "isph_fp64", "wcsph"):
         if mode == "wcsph":
             conv = [scene.to_wcsph(p, s) for p, s in zip(P, S)]
             Pm, Sm = [c[0] for c in conv], [c[1] for c in conv]
+        elif mode == "isph_fp64":
+            Pm = [abi.Params.from_buffer_copy(p) for p in P]
+            for p in Pm:
+                p.precision = abi.PREC_FP64
+            Sm = S
         else:
             Pm, Sm = P, S
-        ctx = api.Context(Pm, Sm, G)
+        ctx = api.Context(Pm, Sm, G, tuning="auto")
         ctx.prime()
         if mode == "wcsph":
             ctx.stage("wcsph_pressure_to_density")
-        stepf = ctx.step if mode == "isph" else ctx.wcsph_step
+        stepf = ctx.wcsph_step if mode == "wcsph" else ctx.step
         stepf(2)
         ctx.sync()
         ctx.record(0)
@@ -464,9 +696,41 @@ def run_batched(args):
         ms = ctx.elapsed_ms(0, 1)
         err = [ctx.info(k)["err_bits"] for k in range(len(Pm))]
         out[mode] = {"value": n * args.batch_steps / (ms / 1e3), "unit": UNIT,
-                     "ms_per_step": ms / args.batch_steps, "scenes_with_errors": int(sum(e != 0 for e in err))}
+                     "ms_per_step": ms / args.batch_steps, "scenes_with_errors": int(sum(e != 0 for e in err)),
+                     "tuning": ctx.tuning["options"] if ctx.tuning else None}
+        if mode != "wcsph":
+            final[mode] = [ctx.download(k, full=False) for k in range(len(Pm))]
         ctx.close()
+    out["isph_mixed_over_fp64"] = out["isph"]["value"] / out["isph_fp64"]["value"]
+    out["isph_p_rel_l2_mixed_vs_fp64"] = batch_step_errors(P, G, final["isph"])
     return out
+
+
+def batch_step_errors(P, G, states):
+    """Per-step pressure error of the mixed batch against the FP64 batch: both
+    restart from the same state (the mixed batch's state at the end of its
+    timed steps) and take one step; per-scene rel-L2 of p by particle id."""
+    from beachslope_gb300 import abi, api
+    keys = ["x", "y", "vx", "vy", "p", "mass", "rho", "oden", "ovol", "con", "tid", "pid", "flags"]
+    S = [{k: st[k] for k in keys} for st in states]
+    got = {}
+    for prec in (abi.PREC_MIXED, abi.PREC_FP64):
+        Q = [abi.Params.from_buffer_copy(p) for p in P]
+        for q in Q:
+            q.precision = prec
+        c = api.Context(Q, S, G, tuning="auto")
+        c.prime()
+        c.step(1)
+        got[prec] = [c.download(k, full=False) for k in range(len(Q))]
+        c.close()
+    errs = []
+    for a, b in zip(got[abi.PREC_MIXED], got[abi.PREC_FP64]):
+        oa, ob = np.argsort(a["pid"]), np.argsort(b["pid"])
+        if np.array_equal(a["pid"][oa], b["pid"][ob]):
+            errs.append(float(np.linalg.norm(a["p"][oa] - b["p"][ob]) / max(np.linalg.norm(b["p"]), 1e-300)))
+    return {"scenes_compared": len(errs), "max": max(errs) if errs else None,
+            "median": float(np.median(errs)) if errs else None,
+            "note": "one step of both forms from the mixed batch's state after its timed steps"}
 
 
 def run_serving(args):
@@ -476,32 +740,51 @@ def run_serving(args):
     from beachslope_gb300 import abi, api, scene, serve
     reqs = serve.poisson_requests(args.serve_requests, args.serve_rate, precision=abi.PREC_MIXED)
     steps = args.serve_steps
-    classes = [(500_000, 3), (64_000, 5)]   # (largest request, slots)
-    templates = []
-    for cap, k in classes:
+    # size classes (largest request of the class, share of the memory budget,
+    # concurrency limit): the slot table is laid out within half of the free
+    # device memory at the device bytes per row measured on a calibration context
+    spec = [(500_000, 0.85, args.serve_large_slots), (64_000, 0.15, args.serve_small_slots)]
+    classes = []
+    for cap, share, limit in spec:
         tp, tst, tgr = scene.beach_scene(dx=scene.dx_for_particles(cap), precision=abi.PREC_MIXED)
-        templates += [(tp, int(1.3 * len(tst["x"])), int(1.3 * len(tgr["x"])) + 64)] * k
-    srv = serve.Server(templates)
+        classes.append((tp, int(1.3 * len(tst["x"])), int(1.3 * len(tgr["x"])) + 64, share, limit))
+        if cap == spec[0][0]:
+            bpr = serve.Server.calibrate(tp, tst, tgr, tuning="auto")
+    free0, total = api.device_memory()
+    srv = serve.Server.for_memory(classes, bpr, budget_bytes=0.5 * free0, tuning="auto")
     t0 = time.perf_counter()
     res = srv.run(reqs, steps)
     wall = time.perf_counter() - t0
+    held = srv.ctx.device_bytes()
     srv.close()
-    lat = np.array([res[r.rid]["latency"] for r in reqs])
-    psteps = sum(len(r.state["x"]) for r in reqs) * steps
+    done = [r for r in reqs if "latency" in res[r.rid]]
+    lat = np.array([res[r.rid]["latency"] for r in done])
+    psteps = sum(len(r.state["x"]) for r in done) * steps
     out = {"requests": len(reqs), "rate_per_s": args.serve_rate, "steps_per_request": steps,
            "particles_min": min(len(r.state["x"]) for r in reqs),
            "particles_max": max(len(r.state["x"]) for r in reqs),
-           "slots": {str(c): k for c, k in classes},
+           "slots": {str(c[0]): k for c, k in zip(spec, srv.class_counts)},
+           "memory": {"device_free_bytes": int(free0), "device_total_bytes": int(total),
+                      "budget_bytes": int(srv.budget_bytes), "planned_bytes": int(srv.planned_bytes),
+                      "context_bytes": int(held), "bytes_per_row": round(bpr, 1),
+                      "limits": {str(c[0]): c[2] for c in spec},
+                      "binding": {str(c[0]): ("memory" if k < c[2] else "concurrency limit")
+                                  for c, k in zip(spec, srv.class_counts)}},
+           "rejected": len(srv.rejected),
            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                          "mean": float(lat.mean())},
            "value": psteps / wall, "unit": UNIT, "wall_s": wall,
-           "errors": int(sum(res[r.rid]["info"]["err_bits"] != 0 for r in reqs)),
+           "errors": int(sum(res[r.rid]["info"]["err_bits"] != 0 for r in done)),
+           "error_bits": sorted({int(res[r.rid]["info"]["err_bits"]) for r in done} - {0}),
+           "error_requests": [{"n": len(r.state["x"]), "bits": int(res[r.rid]["info"]["err_bits"]),
+                               "iters": int(res[r.rid]["info"]["ppe_iters"])}
+                              for r in done if res[r.rid]["info"]["err_bits"]][:8],
            "note": "each request %d production steps (the configuration's 0.5 s of physical time is %d steps)"
                    % (steps, 5000)}
     # serial FP64 baseline: the same requests one after another
     t0 = time.perf_counter()
     lat_s = []
-    for r in reqs:
+    for r in done:
         p = abi.Params.from_buffer_copy(r.params)
         p.precision = abi.PREC_FP64
         c = api.Context([p], [r.state], [r.grains], tuning="auto")
@@ -535,9 +818,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched workload")
     ap.add_argument("--batch-scenes", type=int, default=64)
-    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-steps", type=int, default=200)
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop workload")
-    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-large-slots", type=int, default=6)
+    ap.add_argument("--serve-small-slots", type=int, default=12)
+    ap.add_argument("--no-config1", action="store_true", help="skip the 13 k-particle 2000-step leg")
+    ap.add_argument("--config1-steps", type=int, default=2000)
+    ap.add_argument("--config1-cpu-s", type=float, default=10.0)
+    ap.add_argument("--no-config3", action="store_true", help="skip the standalone 1 M search + PPE leg")
+    ap.add_argument("--no-oracle-parity", action="store_true")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-steps", type=int, default=40)
     args = ap.parse_args()
@@ -564,7 +854,7 @@ def main():
     if D.rank == 0:
         line = dict(base)
         line.update({"value": out["value"], "ms_per_step": out["ms_per_step"], "dtype": dtype_of(args.precision)})
-        for k in ("roofline", "e2e", "gpu_launches", "clocks", "fp64"):
+        for k in ("roofline", "step_roofline", "e2e", "gpu_launches", "clocks", "fp64"):
             if k in out:
                 line[k] = out[k]
         line["config"]["particles_per_gpu"] = out["particles"]
@@ -577,7 +867,13 @@ def main():
             f"FGMRES({int(tun.get('ppe_restart', 150))}), multigrid right preconditioner"
             if int(tun.get("ppe_solver", 0)) == 1 else "BiCGStab, multigrid right preconditioner")
         if D.world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(args)
+            line["cpu_baseline"], par = cpu_baseline(args)
+            if not args.no_oracle_parity:
+                line["oracle_parity"] = par
+        if not args.no_config1:
+            line["config1"] = run_config1(args)
+        if not args.no_config3:
+            line["config3"] = run_config3(args)
         if not args.no_batch:
             line["batched"] = run_batched(args)
         if not args.no_serve:

@@ -90,23 +90,23 @@ typedef struct bs_params {
     int32_t adaptive_dt; /* 1: timestep() rule integrator.f90:927-937 sets dt          */
     int32_t scalar_on;   /* 1: salinity sub-steps run at the start of each step        */
     /* fluid */
-    double rho;        /* reference density (initialize.f90:247)                      */
-    double rhomin;     /* scalar.f90:414                                              */
+    double rho;        /* reference density (initialize.f90:23)                       */
+    double rhomin;     /* initialize.f90:24, used at scalar.f90:414                   */
     double rhomax;     /* rho*rel_den (setup.f90:19)                                  */
-    double rel_den;    /* initialize.f90:251                                          */
+    double rel_den;    /* initialize.f90:27                                           */
     double g;          /* gravity along y (negative)                                  */
-    double mu;         /* viscosity in the timestep rule (initialize.f90:263)         */
-    double tschmidt;   /* turbulent Schmidt number (initialize.f90:249)               */
+    double mu;         /* viscosity in the timestep rule (initialize.f90:39)          */
+    double tschmidt;   /* turbulent Schmidt number (initialize.f90:25)                */
     /* porous medium (porous.f90:111) */
     double por;        /* grain-bed porosity                                          */
     double lamk;       /* Ergun constant                                              */
     double d50;        /* grain diameter                                              */
     /* free surface and shifting */
-    double lamfs;      /* 0.8  (initialize.f90:270)                                   */
-    double maxdivr;    /* 2.0  (initialize.f90:269)                                   */
-    double csh;        /* 0.5  (initialize.f90:248)                                   */
-    double maxshift;   /* 0.1  (initialize.f90:264)                                   */
-    double sig1;       /* 0.2  CFL factor (initialize.f90:263)                        */
+    double lamfs;      /* 0.8  (initialize.f90:46)                                    */
+    double maxdivr;    /* 2.0  (initialize.f90:45)                                    */
+    double csh;        /* 0.5  (initialize.f90:24)                                    */
+    double maxshift;   /* 0.1  (initialize.f90:40)                                    */
+    double sig1;       /* 0.2  CFL factor (initialize.f90:39)                         */
     /* outflow cut-offs used by the second re-bin (integrator.f90:61-62) */
     double xlcutoff;
     double ytcutoff;
@@ -412,8 +412,11 @@ int bs_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const d
  * 65,536 rows (larger n returns BS_E_CAPACITY).  The array is shared by all
  * calls: calls whose GPU work overlaps race, so serialise them.  The first call
  * on each device looks up the array's address (cudaGetSymbolAddress, that
- * device current); make it before any stream capture.  `stream` is a
- * cudaStream_t (NULL: the default stream). */
+ * device current); make it before any stream capture.  Convergence is judged
+ * on the recursive residual, as in bs_bicgstab_csr; *relres is the true
+ * residual ||b - A x|| / ||b|| after the last iteration; the convergence flag
+ * is read back every four iterations (the call waits for `stream` there).
+ * `stream` is a cudaStream_t (NULL: the default stream). */
 int bs_bicgstab_csr_noalloc(int32_t n, const int32_t* d_row_ptr, const int32_t* d_col, const double* d_val,
                             const double* d_b, double* d_x, double tol, int32_t maxit, void* stream,
                             int32_t* iters, double* relres);
@@ -428,6 +431,19 @@ int bs_kernel_timing_get(struct bs_ctx* ctx, int32_t idx, const char** name, int
                          double* total_ms);
 /* count of kernels launched by the library since context creation */
 int64_t bs_launch_count(struct bs_ctx* ctx);
+
+/* No counterpart in the reference (admission of requests by free device
+ * memory): free and total bytes of the current device (cudaMemGetInfo), and
+ * the device bytes a context holds (its particle, neighbour, matrix,
+ * multigrid and Krylov arrays; the FGMRES basis is allocated at the first
+ * FGMRES solve and counted from then on). */
+int bs_device_memory(size_t* free_bytes, size_t* total_bytes);
+int bs_context_bytes(struct bs_ctx* ctx, size_t* bytes);
+
+/* No counterpart in the reference: a measurement helper for the roofline.
+ * FP64 rate of the current device in TFLOP/s, from chains of dependent
+ * fused multiply-adds on every SM (best of five timed launches, ~0.5 s). */
+int bs_measure_fp64_peak(double* tflops);
 
 #ifdef __cplusplus
 }

@@ -74,8 +74,18 @@ def test_cache_round_trip(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "tuning.json"))
     autotune.save(1, 700_000, {"mg_wlev": 2, "ppe_restart": 120, "ppe_solver": 1}, 21.0, "w")
     assert autotune.lookup(1, 712_460)["options"]["mg_wlev"] == 2   # same size class
-    assert autotune.lookup(1, 180_000) is None
+    assert autotune.lookup(0, 712_460) is None                      # no entry of that precision
     assert autotune.key(1, 712_460) == "prec1_n4^10"
+    # a size class without an entry falls back to the nearest single-scene class
+    autotune.save(1, 180_000, {"mg_wlev": 1}, 7.0, "small")
+    assert autotune.lookup(1, 3_000_000)["options"]["mg_wlev"] == 2
+    assert autotune.lookup(1, 100_000)["options"]["mg_wlev"] == 1
+    # a batch uses its own entry (size and scene-count class) when there is one
+    assert autotune.key(1, 1_000_000, 64) == "prec1_n4^10_s4^3"
+    assert autotune.lookup(1, 1_000_000, 64)["options"]["mg_wlev"] == 2
+    autotune.save(1, 1_000_000, {"mg_wlev": 0}, 20.0, "batch", scenes=64)
+    assert autotune.lookup(1, 1_000_000, 64)["options"]["mg_wlev"] == 0
+    assert autotune.lookup(1, 712_460)["options"]["mg_wlev"] == 2
     ctx = _FakeCtx(lambda o: 1.0)
     autotune.apply(ctx, 1, 712_460)
     assert list(ctx.opts) == ["ppe_restart", "ppe_solver", "mg_wlev"]   # restart before the method

@@ -84,5 +84,53 @@ def test_fits_checks_rows_grains_and_the_cell_grid():
     assert not srv.fits(0, _req(0, 0, 10, cell=(60, 10)))   # grid wider than the slot's
     from beachslope_gb300 import serve
     t = srv.templates[0]
-    assert serve.Server.slots_for_memory(t, 1000, 0, 1e12) == 64
-    assert serve.Server.slots_for_memory(t, 1000, 0, 1.0) == 1
+    assert serve.Server.slots_for_memory(t, 1000, 0, 1e12, 4000.0) == 64
+    assert serve.Server.slots_for_memory(t, 1000, 0, 1.0, 4000.0) == 0
+
+
+def _memory_server(budget, bytes_per_row=4000.0):
+    """A server laid out by serve.Server.plan within `budget` bytes (two size
+    classes, half of the budget each), on the fake context."""
+    from beachslope_gb300 import abi, serve
+    t = abi.default_params()
+    t.cellx, t.celly = 50, 20
+    classes = [(t, 1000, 0, 0.5, 8), (t, 100, 0, 0.5, 8)]
+    counts, used = serve.Server.plan(classes, budget, bytes_per_row)
+    caps = [1000] * counts[0] + [100] * counts[1]
+    return _server(caps), counts, used
+
+
+def test_slot_table_from_a_memory_budget():
+    from beachslope_gb300 import abi, serve
+    t = abi.default_params()
+    t.cellx, t.celly = 50, 20
+    per_big = serve.Server.slot_bytes(t, 1000, 0, 4000.0)
+    per_small = serve.Server.slot_bytes(t, 100, 0, 4000.0)
+    # room for one slot of each class: the budget binds
+    srv, counts, used = _memory_server(2 * per_big + 0.5)
+    assert counts == [1, int(per_big // per_small)] and used <= 2 * per_big + 0.5
+    # a large budget: the concurrency limit binds
+    _, counts, _ = _memory_server(1e15)
+    assert counts == [8, 8]
+    # a budget below one large slot leaves that class out
+    _, counts, _ = _memory_server(1.5 * per_small / 0.5)
+    assert counts[0] == 0 and counts[1] == 1
+
+
+def test_a_small_memory_budget_forces_queueing_and_rejects_what_never_fits():
+    """One slot per class fits the budget: requests of the large class queue
+    behind each other; a request larger than every slot is rejected at once
+    instead of waiting forever."""
+    from beachslope_gb300 import abi, serve
+    t = abi.default_params()
+    t.cellx, t.celly = 50, 20
+    budget = serve.Server.slot_bytes(t, 1000, 0, 4000.0) * 2 + 1.0
+    classes = [(t, 1000, 0, 0.5, 8), (t, 100, 0, 0.5, 1)]
+    counts, _ = serve.Server.plan(classes, budget, 4000.0)
+    assert counts == [1, 1]
+    srv = _server([1000, 100])
+    reqs = [_req(0, 0, 800), _req(1, 0, 700), _req(2, 1, 900), _req(3, 1, 5000)]
+    out = srv.run(reqs, steps=3, clock="steps")
+    assert out[0]["admit"] == 0 and out[1]["admit"] == 3 and out[2]["admit"] == 6
+    assert out[2]["latency"] == 9 - 1
+    assert out[3]["error"] == "larger than every slot" and srv.rejected == [3]
