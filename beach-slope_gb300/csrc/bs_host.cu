@@ -63,9 +63,34 @@ struct bs_ctx {
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
     // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
     int fg_df_on = 1;
+    // captured production steps (one CUDA graph per step, loops on the device):
+    // cache keyed by the bytes the capture depends on; the pointer pairs the
+    // stages swap cycle with a period of a few steps, so a few entries serve
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<unsigned char> key;
+        Dev after{};            // the device tables after the step (the swaps the capture made)
+        bool disp_after = false;
+        int64_t kernels = 0;    // kernels outside the device loops
+        uint64_t used = 0;
+    };
+    std::vector<StepGraph> sgraphs;
+    int step_graph_on = 1;      // option "step_graph"
+    bool step_graph_broken = false;   // a capture failed: eager steps from then on
+    uint64_t sg_clock = 0;
+    int64_t graph_steps = 0;
+    bool solsteps_stale = false;      // solsteps not read back since the last captured step
+    cudaStream_t side[3] = {};        // streams that capture the loop bodies
 };
 
 namespace {
+
+// drop the captured steps (their kernels hold the old tables and sizes)
+void sg_clear(bs_ctx* ctx) {
+    for (auto& g : ctx->sgraphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    ctx->sgraphs.clear();
+}
 
 int fail(bs_ctx* c, int code, const std::string& m) {
     if (c) c->err = m;
@@ -611,6 +636,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     if (!rc) rc = dalloc(ctx, &dcs, cell);
     if (!rc) rc = dalloc(ctx, &dbd, nscenes);
     if (!rc) rc = dalloc(ctx, &ctx->d_nconv, 4);   // [0] inner, [1] outer converged-scene counters
+    if (!rc) rc = dalloc(ctx, &D.loop, 1);
     if (rc) {
         int r2 = rc;
         bs_destroy(ctx);
@@ -642,6 +668,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     D.fg_gdone = nullptr;
     D.fg_m = D.fg_small_n = D.fg_ld = 0;
     cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (auto& q : ctx->side) cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking);
     for (auto& e : ctx->ev) cudaEventCreate(&e);
     cudaEventCreateWithFlags(&ctx->evsync, cudaEventDisableTiming);
     cudaMallocHost(&ctx->h_pinned, sizeof(int) * (nscenes + 4));
@@ -671,6 +698,10 @@ int bs_destroy(bs_ctx* ctx) {
     if (ctx->timer.ready)
         for (auto& e : ctx->timer.ev) cudaEventDestroy(e);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
+    for (auto& g : ctx->sgraphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (auto& q : ctx->side)
+        if (q) cudaStreamDestroy(q);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BS_OK;
@@ -680,6 +711,7 @@ const char* bs_last_error(bs_ctx* ctx) { return ctx ? ctx->err.c_str() : "null c
 
 int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     if (!ctx || s < 0 || s >= ctx->nscene || !st) return BS_E_ARG;
+    sg_clear(ctx);
     const bs_params& p = ctx->prm[s];
     const ScenePar& P = ctx->hpar[s];
     const int n = st->n;
@@ -991,7 +1023,11 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
         for (auto& p : ctx->prm) p.ppe_restart = (int32_t)value;
-    else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
+    else if (k == "step_graph" && (value == 0 || value == 1)) {
+        ctx->step_graph_on = (int)value;
+        ctx->step_graph_broken = false;
+    } else return fail(ctx, BS_E_ARG, "unknown option or value out of range: " + k);
+    sg_clear(ctx);
     if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
         if (int rc = fg_ensure(ctx)) return rc;
     mg_sub_choose(ctx);   // the W depth changes the visits' op lists
@@ -1017,6 +1053,9 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "fg_df") *value = ctx->fg_df_on;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
+    else if (k == "step_graph") *value = ctx->step_graph_on && !ctx->step_graph_broken;
+    else if (k == "step_graph_steps") *value = (double)ctx->graph_steps;
+    else if (k == "step_graph_cached") *value = (double)ctx->sgraphs.size();
     else return BS_E_ARG;
     return 0;
 }
@@ -1038,6 +1077,7 @@ int bs_set_rhs(bs_ctx* ctx, int32_t s, const double* b) {
 int bs_set_inflow(bs_ctx* ctx, int32_t s, int32_t zone, const bs_inflow* z) {
     if (!ctx || s < 0 || s >= ctx->nscene || zone < 0 || zone > 1 || !z || z->n < 0 || z->ncells < 0)
         return BS_E_ARG;
+    sg_clear(ctx);
     const bool clear = (z->n == 0 && z->ncells == 0);
     if (!clear && ((z->n && (!z->x || !z->y || !z->vx || !z->vy || !z->p)) || (z->ncells && (!z->cell_i || !z->cell_j)) ||
                    (z->remove_side != 1 && z->remove_side != -1) || !(z->rho > 0)))
@@ -1445,12 +1485,206 @@ int bs_wcsph_step(bs_ctx* ctx, int32_t nsteps) {
 // Full production step, main.f90:199-272 (open-boundary buffers excluded).
 int bs_step(bs_ctx* ctx, int32_t nsteps) { return bs_step_flags(ctx, nsteps, BS_STEP_ALL); }
 
+}  // extern "C"
+
+// ------------------------------------------------------------ captured step
+// A production step as one CUDA graph: the stages as stream capture on the
+// context's stream, the salinity sub-steps and the Krylov loops as
+// conditional while/if nodes whose condition kernels read the device's own
+// counters (solsteps, converged scenes), so K steps are K graph launches
+// with no host round trip.  The results are those of the eager step: the
+// same kernels in the same order; the sub-steps run in pairs (the second of
+// a pair beyond a scene's solsteps copies through, as the eager loop's
+// surplus sub-steps do), which keeps the salinity buffers in place.
+namespace {
+
+bool any_scalar_on(const bs_ctx* ctx) {
+    for (auto& p : ctx->prm)
+        if (p.scalar_on) return true;
+    return false;
+}
+
+int max_ppe_maxit(const bs_ctx* c) {
+    int maxit = 0;
+    for (auto& p : c->prm) maxit = std::max(maxit, (int)p.ppe_maxit);
+    return maxit;
+}
+
+template <class T>
+void key_put(std::vector<unsigned char>& k, const T& v) {
+    const unsigned char* b = (const unsigned char*)&v;
+    k.insert(k.end(), b, b + sizeof(T));
+}
+
+// everything the captured kernels and their launch shapes depend on
+std::vector<unsigned char> step_key(const bs_ctx* c, int flags) {
+    std::vector<unsigned char> k;
+    key_put(k, c->D);
+    const int v[] = {flags, c->precision, c->prm[0].ppe_solver, c->prm[0].ppe_restart, c->prm[0].ppe_precond,
+                     c->prm[0].mixed_max_outer, max_ppe_maxit(c), c->mgsub_on, c->mgsub_level, c->mgsub_cs,
+                     c->fg_df_on, c->disp_ready ? 1 : 0, any_scalar_on(c) ? 1 : 0, c->nblk_total};
+    key_put(k, v);
+    for (const auto& m : c->mglev) key_put(k, m);
+    k.insert(k.end(), c->mgneed.begin(), c->mgneed.end());
+    return k;
+}
+
+// can this step be captured?  (buffer zones need the host's schedule, the
+// per-kernel timer needs events between launches, and the FP32-inner
+// refinement solver keeps its host loop)
+bool step_graph_ok(const bs_ctx* c) {
+    if (!c->step_graph_on || c->step_graph_broken || c->any_zone) return false;
+    if (c->timer.mask) return false;
+    const bool fg = c->prm[0].ppe_solver == BS_SOLVER_FGMRES;
+    if (!fg && c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0) return false;
+    return true;
+}
+
+// the stages of bs_step_flags, recorded into the capture of ctx->stream
+bool record_step(bs_ctx* ctx, int flags) {
+    Dev& D = ctx->D;
+    bs::Launch L = launch_of(ctx);
+    L.graph = nullptr;
+    bs::advance_time(D, L);
+    if (any_scalar_on(ctx) && (flags & BS_STEP_SCALAR)) {
+        if (!ctx->disp_ready) {
+            bs::disp(D, L);
+            ctx->disp_ready = true;
+        }
+        cudaMemsetAsync(&D.loop->j, 0, sizeof(int), ctx->stream);
+        cudaGraphConditionalHandle hs;
+        if (!bs::cond_handle(ctx->stream, 1, &hs)) return false;
+        const bool ok = bs::cond_node(ctx->stream, ctx->side[0], cudaGraphCondTypeWhile, hs, [&]() {
+            bs::Launch B = L;
+            B.stream = ctx->side[0];
+            const int64_t b0 = ctx->launches;
+            bs::scalar(D, B, ctx->precision, 0, &D.loop->j);   // sub-step j: con -> con_new
+            std::swap(D.con, D.con_new);
+            bs::scalar(D, B, ctx->precision, 1, &D.loop->j);   // sub-step j + 1: back into con
+            std::swap(D.con, D.con_new);
+            const int nk = (int)(ctx->launches - b0) + 1;
+            bs::cond_scalar(D, ctx->side[0], hs, nk);
+            ctx->launches = b0;
+            return cudaGetLastError() == cudaSuccess;
+        });
+        if (!ok) return false;
+    }
+    if (flags & BS_STEP_BUFFERS)
+        if (st_buffers(ctx)) return false;   // no zones here: nothing to do
+    st_rebin(ctx, 1, 0);
+    st_search(ctx, 1, 1);
+    bs::eddy(D, L, ctx->precision, 1, 1, 0);
+    bs::int_vel(D, L, ctx->precision);
+    bs::assemble(D, L, ctx->precision);
+    ctx->assembled = true;
+    const int maxit = max_ppe_maxit(ctx);
+    const int precond = ctx->prm[0].ppe_precond;
+    bool ok;
+    if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
+        ok = bs::capture_fgmres(D, L, ctx->side, maxit, precond ? 2 : 8, precond, ctx->precision, ctx->d_nconv);
+    else
+        ok = bs::capture_fp64(D, L, ctx->side, maxit, precond ? 4 : 8, precond, ctx->precision, ctx->d_nconv);
+    if (!ok) return false;
+    bs::comp_vel(D, L, ctx->precision, 1, 1);
+    bs::cell_max_timestep(D, L, 1, 0);
+    st_rebin(ctx, 0, 1);
+    st_search(ctx, 1, 1);
+    bs::freesurf(D, L);
+    bs::shift(D, L, ctx->precision);
+    bs::apply_density(D, L, 1, (flags & BS_STEP_DENSITY) ? 1 : 0);
+    bs::cell_max_timestep(D, L, 0, 1);
+    if (flags & BS_STEP_EDDY_END) {
+        bs::eddy(D, L, ctx->precision, 1, 0, 1);
+        ctx->disp_ready = true;
+    } else {
+        ctx->disp_ready = false;
+    }
+    return cudaGetLastError() == cudaSuccess;
+}
+
+// one step through the graph cache: 0 done, 1 not capturable (run eagerly),
+// < 0 error
+int step_graphed(bs_ctx* ctx, int flags) {
+    if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES) {
+        if (int rc = fg_ensure(ctx)) return rc;   // allocations cannot happen inside a capture
+        ctx->D.fg_df = (ctx->fg_df_on && ctx->precision == BS_PREC_MIXED && ctx->prm[0].ppe_precond) ? 1 : 0;
+    }
+    const std::vector<unsigned char> key = step_key(ctx, flags);
+    bs_ctx::StepGraph* G = nullptr;
+    for (auto& g : ctx->sgraphs)
+        if (g.key == key) G = &g;
+    if (!G) {
+        const Dev D0 = ctx->D;
+        const bool disp0 = ctx->disp_ready, asm0 = ctx->assembled;
+        const int64_t l0 = ctx->launches;
+        cudaGetLastError();
+        cudaGraph_t gr = nullptr;
+        cudaGraphExec_t ex = nullptr;
+        bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            ok = record_step(ctx, flags);
+            ok = (cudaStreamEndCapture(ctx->stream, &gr) == cudaSuccess) && ok && gr;
+        }
+        if (ok) ok = cudaGraphInstantiate(&ex, gr, 0) == cudaSuccess;
+        if (gr) cudaGraphDestroy(gr);
+        if (!ok) {   // put the host state back and step eagerly from now on
+            if (ex) cudaGraphExecDestroy(ex);
+            ctx->D = D0;
+            ctx->disp_ready = disp0;
+            ctx->assembled = asm0;
+            ctx->launches = l0;
+            ctx->step_graph_broken = true;
+            cudaGetLastError();
+            return 1;
+        }
+        if (ctx->sgraphs.size() >= 8) {   // drop the least recently used
+            size_t o = 0;
+            for (size_t i = 1; i < ctx->sgraphs.size(); ++i)
+                if (ctx->sgraphs[i].used < ctx->sgraphs[o].used) o = i;
+            cudaGraphExecDestroy(ctx->sgraphs[o].exec);
+            ctx->sgraphs.erase(ctx->sgraphs.begin() + o);
+        }
+        bs_ctx::StepGraph g;
+        g.exec = ex;
+        g.key = key;
+        g.after = ctx->D;
+        g.disp_after = ctx->disp_ready;
+        g.kernels = ctx->launches - l0;
+        ctx->launches = l0;
+        ctx->D = D0;
+        ctx->sgraphs.push_back(std::move(g));
+        G = &ctx->sgraphs.back();
+    }
+    G->used = ++ctx->sg_clock;
+    CK(cudaGraphLaunch(G->exec, ctx->stream));
+    ctx->D = G->after;
+    ctx->disp_ready = G->disp_after;
+    ctx->assembled = true;
+    ctx->launches += G->kernels;
+    ctx->graph_steps += 1;
+    ctx->solsteps_stale = true;
+    return check_launch(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
 // The production step of main.f90:199-272; the flags drop the parts the
 // reference's settling phases (main.f90:39-67, 95-155) do not run.
 int bs_step_flags(bs_ctx* ctx, int32_t nsteps, int32_t flags) {
     if (!ctx || nsteps < 0 || (flags & ~BS_STEP_ALL)) return BS_E_ARG;
     Dev& D = ctx->D;
     for (int it = 0; it < nsteps; ++it) {
+        if (step_graph_ok(ctx)) {
+            const int rc = step_graphed(ctx, flags);
+            if (rc < 0) return rc;
+            if (rc == 0) continue;
+        }
+        if (ctx->solsteps_stale) {   // the sub-step count of the last captured step
+            if (int rc = read_solsteps(ctx)) return rc;
+            ctx->solsteps_stale = false;
+        }
         bs::Launch L = launch_of(ctx);
         if (ctx->any_zone)
             if (int rc = read_dyn(ctx)) return rc;
@@ -1641,7 +1875,18 @@ int bs_kernel_timing_get(bs_ctx* ctx, int32_t idx, const char** name, int32_t* l
     if (total_ms) *total_ms = ctx->timer.total_ms[idx];
     return 0;
 }
-int64_t bs_launch_count(bs_ctx* ctx) { return ctx ? ctx->launches : -1; }
+int64_t bs_launch_count(bs_ctx* ctx) {
+    if (!ctx) return -1;
+    int64_t n = ctx->launches;
+    if (ctx->graph_steps) {   // kernels of the captured steps' device loops, counted on the device
+        unsigned long long k = 0;
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+            cudaMemcpy(&k, &ctx->D.loop->kernels, sizeof(k), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return -1;
+        n += (int64_t)k;
+    }
+    return n;
+}
 
 int bs_device_memory(size_t* free_bytes, size_t* total_bytes) {
     if (!free_bytes || !total_bytes) return BS_E_ARG;

@@ -182,6 +182,15 @@ struct Dev {
     int kmax;
     unsigned* err_word;
     MgDev mg;
+    struct LoopCtl* loop;           // device-side loop counters of the captured step (bs_graph)
+};
+
+// Counters of the device-side loops of a captured step: the scalar sub-step
+// pairs, BiCGStab iterations, FGMRES restart cycles and columns, and the
+// kernels the loop bodies launched (for the launch count).
+struct LoopCtl {
+    int j, it, cycle, col;
+    unsigned long long kernels;
 };
 
 // ------------------------------------------------------------ helpers
@@ -438,7 +447,8 @@ void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_p
 void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_timestep);
 void shift(const Dev& D, const Launch& L, int precision);
 void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density);
-void scalar(const Dev& D, const Launch& L, int precision, int substep);
+// one salinity sub-step; with jdev the sub-step index is substep + *jdev
+void scalar(const Dev& D, const Launch& L, int precision, int substep, const int* jdev = nullptr);
 // WCSPH (wcsph.f90): continuity, row updates (bit0 updateden, bit1
 // dentopress, bit2 presstoden), wall pressure of the WCSPH step
 void wc_continuity(const Dev& D, const Launch& L, int precision);
@@ -472,6 +482,46 @@ void buffer_exchange(const Dev& D, const Launch& L, int s, const ScenePar& P, co
 int mg_sub_max_clusters(int mg_precision, int cs, size_t smem);
 void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
                   int* d_nconv, int* h_nconv, cudaEvent_t ev);
+// The same solves recorded into the stream capture of L.stream with their
+// loops on the device (conditional while/if nodes whose condition kernels
+// read the converged-scene counters); side[0..2] are streams that capture the
+// loop bodies.  Return false when a CUDA call failed (the capture is unusable).
+bool capture_fp64(const Dev& D, const Launch& L, const cudaStream_t* side, int maxit, int check_every, int precond,
+                  int mg_prec, int* d_nconv);
+bool capture_fgmres(const Dev& D, const Launch& L, const cudaStream_t* side, int maxit, int check_every,
+                    int precond, int mg_prec, int* d_nconv);
+// conditional-node helpers for a capture in progress on `st`
+bool cond_handle(cudaStream_t st, unsigned init, cudaGraphConditionalHandle* h);
+template <class F>
+bool cond_node(cudaStream_t st, cudaStream_t side, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle h,
+               F&& body) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return false;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &np) != cudaSuccess) return false;
+    if (cudaStreamBeginCaptureToGraph(side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        return false;
+    const bool ok = body();
+    cudaGraph_t out = nullptr;
+    const bool ended = cudaStreamEndCapture(side, &out) == cudaSuccess;
+    if (!ok || !ended) return false;
+    return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+           cudaSuccess;
+}
+// condition kernel of the captured step's scalar sub-step pairs (two more
+// sub-steps done; go on while a scene has sub-steps left), launched on st
+void cond_scalar(const Dev& D, cudaStream_t st, cudaGraphConditionalHandle h, int body_kernels);
 // per-scene small FGMRES storage for restart length m (doubles)
 inline int fg_small_size(int m) { return (m + 1) * m + (m + 1) * (m + 1) + 2 * m + (m + 1) + m + (m + 1) + 8; }
 __host__ __device__ inline int fg_part_ld(int m) { return 2 * m + 4; }

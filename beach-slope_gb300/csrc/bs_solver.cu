@@ -691,8 +691,9 @@ __device__ __forceinline__ bool fg_scene_sum(const Dev& D, int s, int nv, const 
 
 // Cycle start: r = b - A x (into ss), ||r||, g = ||r|| e1.  first: every
 // scene, sets the stopping threshold (tol ||r0|| or tol ||b||).
-__global__ void k_fg_start(Dev D, int first, int* nconv) {
+__global__ void k_fg_start(Dev D, int first, int* nconv, const int* cycle) {
     BS_PDL_ENTRY();
+    if (cycle) first = (*cycle == 0);   // the captured solve counts its cycles on the device
     const int s = D.blk_scene[blockIdx.x];
     if (!first && D.dyn[s].converged) return;
     const ScenePar& P = D.par[s];
@@ -1340,7 +1341,7 @@ void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int
     for (int cycle = 0; cycle <= maxit; ++cycle) {
         cudaMemcpyAsync(d_nconv, d_nconv + 1, sizeof(int), cudaMemcpyDeviceToDevice, L.stream);
         q = tbegin(L, K_FG_START);
-        launch_pdl(L, k_fg_start, L.nblk_rows, BS_THREADS, 0, D, cycle == 0 ? 1 : 0, d_nconv);
+        launch_pdl(L, k_fg_start, L.nblk_rows, BS_THREADS, 0, D, cycle == 0 ? 1 : 0, d_nconv, (const int*)nullptr);
         tend(L, q);
         cudaMemcpyAsync(h_nconv, d_nconv, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
         cudaStreamSynchronize(L.stream);
@@ -1425,6 +1426,217 @@ void solve_mixed(const Dev& D, const Launch& L, int maxit, int check_every, int*
         launch_pdl(L, k_mx_update, L.nblk_rows, BS_THREADS, 0, D);
         tend(L, q);
     }
+}
+
+
+// ---------------------------------------------------------------- captured solves
+// The solves above check convergence on the host between chunks of
+// iterations.  Inside a captured step the loops run on the device instead:
+// a conditional while node repeats a chunk of iterations (or columns, or
+// restart cycles) for as long as its condition kernel -- one thread, after
+// the chunk -- finds a scene that has not converged and the iteration budget
+// not spent.  Every loop is bounded by the same maxit / restart length as the
+// host loops, so it ends even if no scene converges.
+
+bool cond_handle(cudaStream_t st, unsigned init, cudaGraphConditionalHandle* h) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive || !g)
+        return false;
+    return cudaGraphConditionalHandleCreate(h, g, init, cudaGraphCondAssignDefault) == cudaSuccess;
+}
+
+// BiCGStab chunk done: go on while a scene is not converged and it < maxit
+__global__ void k_cond_iter(Dev D, const int* nconv, cudaGraphConditionalHandle h, int chunk, int maxit,
+                            int body_kernels) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    LoopCtl* C = D.loop;
+    C->kernels += (unsigned long long)body_kernels;
+    C->it += chunk;
+    cudaGraphSetConditional(h, (*nconv < D.nscene && C->it < maxit) ? 1u : 0u);
+}
+
+// FGMRES cycle started (k_fg_start ran): the cycle's columns run if a scene
+// is not converged; another cycle follows while cycle <= maxit
+__global__ void k_cond_cycle(Dev D, const int* nconv, cudaGraphConditionalHandle hloop,
+                             cudaGraphConditionalHandle hbody, int maxit, int body_kernels) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    LoopCtl* C = D.loop;
+    C->kernels += (unsigned long long)body_kernels;
+    const bool go = nconv[1] < D.nscene;
+    C->cycle += 1;
+    cudaGraphSetConditional(hbody, go ? 1u : 0u);
+    cudaGraphSetConditional(hloop, (go && C->cycle <= maxit) ? 1u : 0u);
+}
+
+// start of a cycle's columns: column counter 0, the column loop armed
+__global__ void k_col_init(Dev D, cudaGraphConditionalHandle h, int body_kernels) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    LoopCtl* C = D.loop;
+    C->kernels += (unsigned long long)body_kernels;
+    C->col = 0;
+    cudaGraphSetConditional(h, 1u);
+}
+
+// a chunk of columns done: go on while col < restart length and a scene's cycle is open
+__global__ void k_cond_col(Dev D, const int* nconv, cudaGraphConditionalHandle h, int chunk, int body_kernels) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    LoopCtl* C = D.loop;
+    C->kernels += (unsigned long long)body_kernels;
+    C->col += chunk;
+    cudaGraphSetConditional(h, (C->col < D.fg_m && nconv[0] < D.nscene) ? 1u : 0u);
+}
+
+namespace {
+
+void bicg_iteration(const Dev& D, const Launch& L, int precond, int mg_prec, int* d_nconv) {
+    const double* pu = precond ? D.sp2 : D.sp;
+    const double* su = precond ? D.sv2 : D.ss;
+    const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
+    int q = tbegin(L, K_BICG_PUPD);
+    launch_pdl(L, k_pupd64, L.nblk_rows, BS_THREADS, 0, D, mgmode);
+    tend(L, q);
+    if (precond) mg_apply(D, L, mg_prec, D.sp, D.sp2);
+    q = tbegin(L, K_BICG_IT1);
+    launch_pdl(L, k_it1_64, L.nblk_rows, BS_THREADS, 0, D, pu);
+    tend(L, q);
+    q = tbegin(L, K_BICG_SUPD);
+    launch_pdl(L, k_supd64, L.nblk_rows, BS_THREADS, 0, D, mgmode);
+    tend(L, q);
+    if (precond) mg_apply(D, L, mg_prec, D.ss, D.sv2);
+    q = tbegin(L, K_BICG_IT2);
+    launch_pdl(L, k_it2_64, L.nblk_rows, BS_THREADS, 0, D, su);
+    tend(L, q);
+    q = tbegin(L, K_BICG_IT3);
+    launch_pdl(L, k_it3_64, L.nblk_rows, BS_THREADS, 0, D, pu, su, d_nconv);
+    tend(L, q);
+}
+
+void fg_put(const Dev& D, const Launch& L, int mgmode) {
+    int q = tbegin(L, K_FG_PUT);
+    launch_pdl(L, k_fg_put, L.nblk_rows, BS_THREADS, 0, D, mgmode);
+    tend(L, q);
+}
+
+void fg_column(const Dev& D, const Launch& L, int precond, int mg_prec, int mgmode, int* d_nconv) {
+    if (!D.fg_df) fg_put(D, L, mgmode);
+    if (precond) mg_apply(D, L, mg_prec, D.fg_V, D.sp2);
+    int q = tbegin(L, K_FG_ARN);
+    if (D.fg_df) launch_pdl(L, k_fg_arn1<1>, L.nblk_rows, BS_THREADS, 0, D, precond, d_nconv);
+    else launch_pdl(L, k_fg_arn1<0>, L.nblk_rows, BS_THREADS, 0, D, precond, d_nconv);
+    tend(L, q);
+    q = tbegin(L, K_FG_ORTH);
+    if (D.fg_df) launch_pdl(L, k_fg_arn2<1>, L.nblk_rows, BS_THREADS, 0, D, d_nconv, mgmode);
+    else launch_pdl(L, k_fg_arn2<0>, L.nblk_rows, BS_THREADS, 0, D, d_nconv, mgmode);
+    tend(L, q);
+}
+
+void precond_setup(const Dev& D, const Launch& L, int precond, int mg_prec) {
+    if (!precond) return;
+    if (mg_prec == BS_PREC_MIXED) {
+        const int q = tbegin(L, K_MX_CONV);
+        launch_pdl(L, k_mx_convert, L.nblk_rows, BS_THREADS, 0, D);
+        tend(L, q);
+    }
+    mg_setup(D, L, mg_prec);
+}
+
+Launch on_stream(const Launch& L, cudaStream_t st) {
+    Launch B = L;
+    B.stream = st;
+    return B;
+}
+
+}  // namespace
+
+bool capture_fp64(const Dev& D, const Launch& L, const cudaStream_t* side, int maxit, int check_every, int precond,
+                  int mg_prec, int* d_nconv) {
+    precond_setup(D, L, precond, mg_prec);
+    cudaMemsetAsync(d_nconv, 0, sizeof(int), L.stream);
+    int q = tbegin(L, K_BICG_INIT);
+    launch_pdl(L, k_init64, L.nblk_rows, BS_THREADS, 0, D, d_nconv);
+    tend(L, q);
+    cudaMemsetAsync(&D.loop->it, 0, sizeof(int), L.stream);
+    cudaGraphConditionalHandle h;
+    if (!cond_handle(L.stream, 1, &h)) return false;
+    const bool ok = cond_node(L.stream, side[0], cudaGraphCondTypeWhile, h, [&]() {
+        const Launch B = on_stream(L, side[0]);
+        const int64_t b0 = *L.launches;
+        for (int c = 0; c < check_every; ++c) bicg_iteration(D, B, precond, mg_prec, d_nconv);
+        const int nk = (int)(*L.launches - b0) + 1;
+        k_cond_iter<<<1, 32, 0, side[0]>>>(D, d_nconv, h, check_every, maxit, nk);
+        *L.launches = b0;   // counted on the device per iteration of the loop
+        return cudaGetLastError() == cudaSuccess;
+    });
+    q = tbegin(L, K_TRUERES);
+    launch_pdl(L, k_true_res64, L.nblk_rows, BS_THREADS, 0, D);
+    tend(L, q);
+    return ok;
+}
+
+bool capture_fgmres(const Dev& D, const Launch& L, const cudaStream_t* side, int maxit, int check_every,
+                    int precond, int mg_prec, int* d_nconv) {
+    precond_setup(D, L, precond, mg_prec);
+    const int mgmode = precond ? (mg_prec == BS_PREC_MIXED ? 2 : 1) : 0;
+    cudaMemsetAsync(d_nconv, 0, 2 * sizeof(int), L.stream);
+    cudaMemsetAsync(&D.loop->cycle, 0, sizeof(int), L.stream);
+    cudaGraphConditionalHandle hc, hif, hcol;
+    if (!cond_handle(L.stream, 1, &hc)) return false;
+    const bool ok = cond_node(L.stream, side[0], cudaGraphCondTypeWhile, hc, [&]() {
+        // one restart cycle: start (true residual, norms), then its columns
+        const Launch B0 = on_stream(L, side[0]);
+        const int64_t b0 = *L.launches;
+        cudaMemcpyAsync(d_nconv, d_nconv + 1, sizeof(int), cudaMemcpyDeviceToDevice, side[0]);
+        int q0 = tbegin(B0, K_FG_START);
+        launch_pdl(B0, k_fg_start, L.nblk_rows, BS_THREADS, 0, D, 0, d_nconv, (const int*)&D.loop->cycle);
+        tend(B0, q0);
+        if (!cond_handle(side[0], 0, &hif)) return false;
+        k_cond_cycle<<<1, 32, 0, side[0]>>>(D, d_nconv, hc, hif, maxit, 2);
+        const bool ok1 = cond_node(side[0], side[1], cudaGraphCondTypeIf, hif, [&]() {
+            const Launch B1 = on_stream(L, side[1]);
+            if (D.fg_df) fg_put(D, B1, mgmode);
+            if (!cond_handle(side[1], 1, &hcol)) return false;
+            // the cycle's own kernels: put (double-float basis), this one, the solve and the update
+            k_col_init<<<1, 32, 0, side[1]>>>(D, hcol, (D.fg_df ? 1 : 0) + 3);
+            const bool ok2 = cond_node(side[1], side[2], cudaGraphCondTypeWhile, hcol, [&]() {
+                const Launch B2 = on_stream(L, side[2]);
+                const int64_t b2 = *L.launches;
+                for (int c = 0; c < check_every; ++c) fg_column(D, B2, precond, mg_prec, mgmode, d_nconv);
+                const int nk = (int)(*L.launches - b2) + 1;
+                k_cond_col<<<1, 32, 0, side[2]>>>(D, d_nconv, hcol, check_every, nk);
+                *L.launches = b2;
+                return cudaGetLastError() == cudaSuccess;
+            });
+            int q1 = tbegin(B1, K_FG_UPD);
+            launch_pdl(B1, k_fg_solve, D.nscene, 32, 0, D, d_nconv);
+            launch_pdl(B1, k_fg_update, L.nblk_rows, BS_THREADS, 0, D, precond);
+            tend(B1, q1);
+            return ok2 && cudaGetLastError() == cudaSuccess;
+        });
+        *L.launches = b0;
+        return ok1 && cudaGetLastError() == cudaSuccess;
+    });
+    int q = tbegin(L, K_TRUERES);
+    launch_pdl(L, k_true_res64, L.nblk_rows, BS_THREADS, 0, D);
+    tend(L, q);
+    return ok;
+}
+
+// scalar sub-step pairs of the captured step
+__global__ void k_cond_scalar(Dev D, cudaGraphConditionalHandle h, int body_kernels) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    LoopCtl* C = D.loop;
+    C->kernels += (unsigned long long)body_kernels;
+    C->j += 2;
+    int mx = 1;
+    for (int s = 0; s < D.nscene; ++s) mx = max(mx, D.dyn[s].solsteps);
+    // the same sub-step count as the host loop (bounded: solsteps is finite)
+    cudaGraphSetConditional(h, C->j < mx ? 1u : 0u);
+}
+
+void cond_scalar(const Dev& D, cudaStream_t st, cudaGraphConditionalHandle h, int body_kernels) {
+    k_cond_scalar<<<1, 32, 0, st>>>(D, h, body_kernels);
 }
 
 }  // namespace bs

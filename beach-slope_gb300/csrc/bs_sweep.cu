@@ -767,9 +767,10 @@ __global__ void k_disp(Dev D) {
 // con, writes con_new (swapped by the host).  Uses the stored pair distance
 // with the current positions, as the reference does.
 template <typename T>
-__global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep) {
+__global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep, const int* jdev) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
+    if (jdev) substep += *jdev;   // the captured step counts its sub-step pairs on the device
     const ScenePar& P = D.par[R.s];
     const int r = R.r;
     const double coni = D.con[r];
@@ -1211,8 +1212,8 @@ void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density) 
 }
 void disp(const Dev& D, const Launch& L) { BS_PLAIN(K_DISP, k_disp, D); }
 void velmag(const Dev& D, const Launch& L) { BS_PLAIN(K_VELMAG, k_velmag, D); }
-void scalar(const Dev& D, const Launch& L, int precision, int substep) {
-    BS_DISPATCH(K_SCALAR, precision, k_scalar, D, substep);
+void scalar(const Dev& D, const Launch& L, int precision, int substep, const int* jdev) {
+    BS_DISPATCH(K_SCALAR, precision, k_scalar, D, substep, jdev);
 }
 void wc_continuity(const Dev& D, const Launch& L, int precision) {
     BS_PLAIN(K_WC_CONT, k_wc_hyd, D);
