@@ -50,6 +50,7 @@ def _load():
         "bs_set_option": (C.c_int, [vp, C.c_char_p, C.c_double]),
         "bs_get_option": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
         "bs_prime": (C.c_int, [vp]),
+        "bs_prime_setup": (C.c_int, [vp]),
         "bs_scalar_substep": (C.c_int, [vp]),
         "bs_projection": (C.c_int, [vp]),
         "bs_cellshift": (C.c_int, [vp, i32]),
@@ -168,6 +169,10 @@ class Context:
         """The reference's combined text output (output.f90:188-222) for scene s."""
         self._check(lib.bs_write_combined(self.h, s, fluid_path.encode(),
                                           buffer_path.encode() if buffer_path else None), "write_combined")
+
+    def prime_setup(self):
+        """Prime without the time-step rule (the reference's own set-up)."""
+        self._check(lib.bs_prime_setup(self.h), "prime_setup")
 
     def prime_scene(self, s):
         """Prime slot s alone (the other slots are left exactly as they are)."""

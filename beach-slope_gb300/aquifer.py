@@ -34,7 +34,8 @@ DEFAULTS = dict(
     wc=0.650, L=3.11, H=0.80, pr=0.0050 * 0.90, br=0.00490 * 0.90, wl=3.10, rho=1000.0, g=-9.810,
     csh=0.50, rhomin=1000.0, tschmidt=1.0, soill=3.230, soilh=0.80, set_ht=0.20, coastal_ht=0.450,
     por=0.380, bulkden=1800.0, entry_vel=-2.5 / (3600 * 24), lhs_btm=0.20, rel_den=1.0250,
-    dt=0.001, time=7320.0, displaytime=100.0, mu=0.0010, sig1=0.20, maxshift=0.1,
+    dt=float(np.float32(0.001)),   # initialize.f90:32 writes 0.001 as a default (single precision) REAL
+    time=7320.0, displaytime=100.0, mu=0.0010, sig1=0.20, maxshift=0.1,
     line_grad=16.690, lamfs=0.80, maxdivr=2.0, hfac=5.080, bl=3, open_lhs=43, incr=4,
 )
 
@@ -348,7 +349,7 @@ def run_schedule(ctx, zones, info, settle1=50, settle2=8000, production=None, ou
             on_phase(name)
 
     dump(0)
-    ctx.prime()
+    ctx.prime_setup()   # main.f90:23-37: no time-step rule before the first step
     # settling without buffers, scalar transport, density update or the
     # closing eddyvis (main.f90:39-67); then the fluid at rest
     ctx.step_flags(settle1, 0)

@@ -1274,19 +1274,25 @@ int bs_write_combined(bs_ctx* ctx, int32_t s, const char* fluid_path, const char
 }
 
 // ------------------------------------------------------------------ stages
-int bs_prime(bs_ctx* ctx) {
+static int prime_impl(bs_ctx* ctx, int rule) {
     if (!ctx) return BS_E_ARG;
     bs::Launch L = launch_of(ctx);
     st_search(ctx, 1, 1);
     bs::eddy(ctx->D, L, ctx->precision, 1, 0, 0);
     bs::velmag(ctx->D, L);
-    bs::cell_max_timestep(ctx->D, L, 1, 1);
+    bs::cell_max_timestep(ctx->D, L, 1, rule);
     bs::disp(ctx->D, L);
     ctx->disp_ready = true;
     int rc = check_launch(ctx);
     if (rc) return rc;
     return read_solsteps(ctx);
 }
+
+int bs_prime(bs_ctx* ctx) { return prime_impl(ctx, 1); }
+
+// The reference's set-up (main.f90:23-37) leaves dt at its initial value and
+// umax at 0 for the first step: prime without the time-step rule.
+int bs_prime_setup(bs_ctx* ctx) { return prime_impl(ctx, 0); }
 
 // Prime one scene only: the others are held (their rows, cells and
 // timestep untouched), so scenes already stepping carry on exactly as if no

@@ -334,6 +334,11 @@ int bs_set_rhs(struct bs_ctx* ctx, int32_t scene, const double* b);
 /* Warm-up: neighbour lists, porosity, eddy viscosity and timestep maxima for
  * the uploaded state (what the reference's spin-up leaves behind, main.f90:35-67). */
 int bs_prime(struct bs_ctx* ctx);
+/* The same without the time-step rule (integrator.f90:885-953): dt keeps the
+ * parameters' value and umax stays 0 for the first step, as the reference's
+ * own set-up leaves them (main.f90:23-37 calls no timestep before its loop;
+ * initialize.f90:32,46). */
+int bs_prime_setup(struct bs_ctx* ctx);
 int bs_scalar_substep(struct bs_ctx* ctx);  /* scalart_anisotropic+scalarupdate, scalar.f90:242,364 */
 int bs_projection(struct bs_ctx* ctx);      /* isph.f90:17                                   */
 int bs_cellshift(struct bs_ctx* ctx, int32_t alt); /* integrator.f90:251 (alt=0) / 33 (alt=1); resetid isph.f90:88 */

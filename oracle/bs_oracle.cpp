@@ -1539,7 +1539,7 @@ void ghost(or_scene* s, bool use_mls) {
     });
 }
 
-void prime(or_scene* s) {
+void prime(or_scene* s, bool rule = true) {
     resetid(s);
     neighbour(s);
     effpor(s);
@@ -1557,7 +1557,7 @@ void prime(or_scene* s) {
         c.maxvel = mv;
         c.maxeddy = me;
     });
-    timestep(s);
+    if (rule) timestep(s);
 }
 
 // one production step, main.f90:199-272 (buffers excluded)
@@ -1889,6 +1889,7 @@ int or_stage(or_scene* s, int32_t stage) {
         case OR_TIMESTEP: timestep(s); break;
         case OR_SCALAR_SUBSTEP: scalar_substep(s); break;
         case OR_PRIME: prime(s); break;
+        case OR_PRIME_SETUP: prime(s, false); break;
         case OR_CALMASSCONS: calmasscons(s); break;
         case OR_UPDATEDEN: updateden(s); break;
         case OR_DENTOPRESS: dentopress(s); break;

@@ -34,7 +34,9 @@ enum {
     OR_EFFPOR_KEEP,     /* effpor without its density write (WCSPH step)        */
     OR_BOUN_VEL,        /* boun_vel, integrator.f90:394-457 (never called)      */
     OR_GHOST,           /* comp_ghost + ghost_en, mls.f90:114-263 (Shepard)     */
-    OR_GHOST_MLS        /* the same with the MLS branch for the velocity        */
+    OR_GHOST_MLS,       /* the same with the MLS branch for the velocity        */
+    OR_PRIME_SETUP      /* prime without the time-step rule: dt and umax keep
+                           their initial values, as after main.f90:23-37        */
 };
 
 or_scene* or_create(const bs_params* p, const bs_state* st, const bs_grains* gr);

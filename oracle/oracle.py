@@ -23,7 +23,7 @@ STAGES = dict(projection=1, cellshift=2, cellshiftalt=3, resetid=4, neighbour=5,
               eddyvis=7, int_vel=8, ppe_assemble=9, ppe_solve=10, comp_vel=11, comp_pos=12,
               freesurf=13, opt2_shift=14, densityupdate=15, timestep=16, scalar_substep=17,
               prime=18, calmasscons=19, updateden=20, dentopress=21, presstoden=22,
-              wall_pressure=23, effpor_keep=24, boun_vel=25, ghost=26, ghost_mls=27)
+              wall_pressure=23, effpor_keep=24, boun_vel=25, ghost=26, ghost_mls=27, prime_setup=28)
 
 
 def build(force=False):

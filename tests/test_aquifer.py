@@ -39,6 +39,9 @@ class _OracleCtx:
     def prime(self):
         self.o.stage("prime")
 
+    def prime_setup(self):
+        self.o.stage("prime_setup")
+
     def step_flags(self, n, f):
         self.o.step_flags(n, f)
 
