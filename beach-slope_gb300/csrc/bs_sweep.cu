@@ -696,9 +696,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
     const double cfac = -P.csh * (P.h * P.h) * frac;
     const double xs = cfac * (double)sxs, ys = cfac * (double)sys;
     const double cap = P.maxshift * P.dl;
-    if (xs == 0.0 || ys == 0.0) set_err(D, R.s, BS_ERR_ZERO_SHIFT);
-    D.xs[r] = fmin(fabs(xs), cap) * xs / fabs(xs);
-    D.ys[r] = fmin(fabs(ys), cap) * ys / fabs(ys);
+    if (sizeof(T) == 4) {
+        // mixed form: a component of the FP32 sum that cancels to exactly 0
+        // (a neighbourhood symmetric along that axis) is no shift along it;
+        // the FP64 drop-in keeps the reference's 0 * 0 / 0 below
+        D.xs[r] = xs == 0.0 ? 0.0 : fmin(fabs(xs), cap) * xs / fabs(xs);
+        D.ys[r] = ys == 0.0 ? 0.0 : fmin(fabs(ys), cap) * ys / fabs(ys);
+    } else {
+        if (xs == 0.0 || ys == 0.0) set_err(D, R.s, BS_ERR_ZERO_SHIFT);
+        D.xs[r] = fmin(fabs(xs), cap) * xs / fabs(xs);
+        D.ys[r] = fmin(fabs(ys), cap) * ys / fabs(ys);
+    }
     D.vxs[r] = (double)a1 * xs + (double)a2 * ys;
     D.vys[r] = (double)b1 * xs + (double)b2 * ys;
 }

@@ -122,17 +122,21 @@ def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.0
 
     parts = []
     fmass = rho * dx * dx
+    # the right wall stands one spacing beyond the last fluid column (at
+    # X0 + nx dx, which is L when L/dx is an integer): a wall closer than
+    # dx to the fluid lattice, or further, makes the wall pressure blow up
+    Lw = nx * dx
     # --- walls: bottom (full width incl. corners), left, right
     wx, wy, wt = [], [], []
     for lay in range(layers):
         tid = abi.TID_WALL if lay == 0 else abi.TID_GHOST
         xb = X0 + (np.arange(-layers, nx + layers) + 0.5) * dx
         yb = np.full_like(xb, Y0 - (lay + 0.5) * dx)
-        tb = np.where((xb > X0) & (xb < X0 + L), tid, abi.TID_GHOST)
+        tb = np.where((xb > X0) & (xb < X0 + Lw), tid, abi.TID_GHOST)
         wx.append(xb); wy.append(yb); wt.append(tb)
         yl = Y0 + (np.arange(ny) + 0.5) * dx
         wx.append(np.full_like(yl, X0 - (lay + 0.5) * dx)); wy.append(yl); wt.append(np.full(ny, tid))
-        wx.append(np.full_like(yl, X0 + L + (lay + 0.5) * dx)); wy.append(yl); wt.append(np.full(ny, tid))
+        wx.append(np.full_like(yl, X0 + Lw + (lay + 0.5) * dx)); wy.append(yl); wt.append(np.full(ny, tid))
     # --- slope wall: lattice points within `layers` spacings below the slope surface
     gx, gy = np.meshgrid(xs, Y0 + (np.arange(ny) + 0.5) * dx, indexing="ij")
     gx = gx.ravel(); gy = gy.ravel()
@@ -172,7 +176,7 @@ def beach_scene(dx=0.01, L=4.0, H=0.6, depth=0.30, slope=0.1, toe=2.0, thick=0.0
     st = _cat(parts)
     p.wc_c0 = 10.0 * math.sqrt(-g * d)
     p.wc_ysurf = Y0 + d
-    _grid_for(p, X0 + L + (layers + 1) * dx, Y0 + H + 0.3)
+    _grid_for(p, X0 + max(L, Lw) + (layers + 1) * dx, Y0 + H + 0.3)
     if wcsph:
         p, st = to_wcsph(p, st)
     return p, st, grains
