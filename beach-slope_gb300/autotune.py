@@ -1,12 +1,14 @@
-"""Autotuner for the PPE solver: Krylov method and multigrid cycle shape.
+"""Autotuner for the PPE solver (Krylov method, multigrid cycle shape) and
+the launch shapes of the row kernels.
 
 Measures ms/step of the real workload (CUDA events on the context's stream)
 for a small staged grid -- the Krylov method (BiCGStab, or FGMRES with a
 restart length), then the multigrid cycle shape (W-cycle depth,
 pre-smoothing on the particle and cell levels, Jacobi damping,
 coarse-correction scale, coarsest sweeps, the clustered subtree, the
-second particle-level post-sweep, the double-float FGMRES basis), then the
-restart length again --
+second particle-level post-sweep, the double-float FGMRES basis), the
+threads per block of the neighbour sweeps and of the particle-level
+multigrid kernels, then the restart length again --
 and keeps the fastest configuration whose solves converged without error
 bits.  The result is written to tuning.json next to this file, keyed by
 precision and a particle-count bucket; Context(..., tuning="auto") applies it.
@@ -20,7 +22,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
 OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_post0", "mg_omega", "mg_cscale",
-           "mg_coarse_sweeps", "mg_sub", "fg_df")
+           "mg_coarse_sweeps", "mg_sub", "fg_df", "sweep_tpb", "mg0_tpb")
 
 
 def bucket(n_particles):
@@ -97,7 +99,8 @@ def tune(ctx, grains, steps=2, verbose=True):
         return ms if ok else math.inf
 
     base = {"ppe_restart": 30, "ppe_solver": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9,
-            "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0, "mg_post0": 1, "fg_df": 1}
+            "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0, "mg_post0": 1, "fg_df": 1,
+            "sweep_tpb": 256, "mg0_tpb": 256}
     best, best_ms = dict(base), run(base)
     solver_stage = [{"ppe_solver": 0}] + [{"ppe_solver": 1, "ppe_restart": r} for r in (20, 30, 50, 80, 120)]
     stages = [
@@ -110,6 +113,10 @@ def tune(ctx, grains, steps=2, verbose=True):
         [{"mg_sub": 1}],
         [{"mg_post0": 2}],
         [{"fg_df": 0}],
+        # launch shapes: threads per block of the neighbour sweeps and of the
+        # particle-level multigrid kernels (same results, different occupancy)
+        [{"sweep_tpb": t} for t in (64, 128, 256)],
+        [{"mg0_tpb": t} for t in (64, 128, 256)],
         solver_stage,
     ]
     for stage in stages:

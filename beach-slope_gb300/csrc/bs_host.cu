@@ -63,6 +63,9 @@ struct bs_ctx {
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
     // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
     int fg_df_on = 1;
+    // threads per block of the neighbour sweeps and of the particle-level
+    // multigrid kernels (options "sweep_tpb", "mg0_tpb"; the autotuner picks them)
+    int sweep_tpb = BS_THREADS, mg0_tpb = BS_THREADS;
     // captured production steps (one CUDA graph per step, loops on the device):
     // cache keyed by the bytes the capture depends on; the pointer pairs the
     // stages swap cycle with a period of a few steps, so a few entries serve
@@ -180,6 +183,8 @@ bs::Launch launch_of(bs_ctx* c) {
     L.mgneed = c->mgneed.empty() ? nullptr : c->mgneed.data();
     L.mgsub_level = c->mgsub_level;
     L.mgsub_cs = c->mgsub_cs;
+    L.sweep_tpb = c->sweep_tpb;
+    L.mg0_tpb = c->mg0_tpb;
     return L;
 }
 
@@ -1023,6 +1028,8 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
         for (auto& p : ctx->prm) p.ppe_restart = (int32_t)value;
+    else if ((k == "sweep_tpb" || k == "mg0_tpb") && (value == 64 || value == 128 || value == 256))
+        (k == "sweep_tpb" ? ctx->sweep_tpb : ctx->mg0_tpb) = (int)value;
     else if (k == "step_graph" && (value == 0 || value == 1)) {
         ctx->step_graph_on = (int)value;
         ctx->step_graph_broken = false;
@@ -1053,6 +1060,8 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "fg_df") *value = ctx->fg_df_on;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
+    else if (k == "sweep_tpb") *value = ctx->sweep_tpb;
+    else if (k == "mg0_tpb") *value = ctx->mg0_tpb;
     else if (k == "step_graph") *value = ctx->step_graph_on && !ctx->step_graph_broken;
     else if (k == "step_graph_steps") *value = (double)ctx->graph_steps;
     else if (k == "step_graph_cached") *value = (double)ctx->sgraphs.size();
@@ -1528,7 +1537,8 @@ std::vector<unsigned char> step_key(const bs_ctx* c, int flags) {
     key_put(k, c->D);
     const int v[] = {flags, c->precision, c->prm[0].ppe_solver, c->prm[0].ppe_restart, c->prm[0].ppe_precond,
                      c->prm[0].mixed_max_outer, max_ppe_maxit(c), c->mgsub_on, c->mgsub_level, c->mgsub_cs,
-                     c->fg_df_on, c->disp_ready ? 1 : 0, any_scalar_on(c) ? 1 : 0, c->nblk_total};
+                     c->fg_df_on, c->disp_ready ? 1 : 0, any_scalar_on(c) ? 1 : 0, c->nblk_total,
+                     c->sweep_tpb, c->mg0_tpb};
     key_put(k, v);
     for (const auto& m : c->mglev) key_put(k, m);
     k.insert(k.end(), c->mgneed.begin(), c->mgneed.end());

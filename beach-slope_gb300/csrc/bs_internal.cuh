@@ -391,7 +391,12 @@ struct Launch {
     const unsigned char* mgneed;   // per level: bit0 some scene visits it, bit1 restriction and
                                    // prolongation to the next level, bit2 coarsest-level solve
     int mgsub_level, mgsub_cs;     // first level of the clustered subtree (0: per-level launches), CTAs per cluster
+    int sweep_tpb;                 // threads per block of the neighbour sweeps (64, 128 or 256)
+    int mg0_tpb;                   // threads per block of the particle-level multigrid kernels
 };
+// blocks of `tpb` threads over the rows of a batch (scenes own multiples of
+// BS_ALIGN rows, so a block never straddles two scenes for tpb | BS_ALIGN)
+inline unsigned row_blocks(const Launch& L, int tpb) { return (unsigned)(L.nblk_rows * (BS_THREADS / tpb)); }
 // Programmatic dependent launch: a kernel launched by launch_pdl may be
 // scheduled while its predecessor in the stream still runs.  Its first
 // statement must be BS_PDL_ENTRY(): wait for the predecessor grid to finish

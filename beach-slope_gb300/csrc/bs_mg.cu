@@ -240,9 +240,9 @@ __global__ void k_mg_l0_down(Dev D) {
 template <typename T>
 __global__ void k_mg_l0_prolong(Dev D) {
     BS_PDL_ENTRY();
-    const int s = D.blk_scene[blockIdx.x];
-    if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[r / BS_ALIGN];
+    if (mg_skip(D, s)) return;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
     const T pre = D.mg.pre0 ? ((const T*)D.mg.u)[r] : (T)0;
     ((T*)D.mg.zz)[r] = pre + (T)D.mg.cscale * ((const T*)D.mg.z[1])[D.mg.agg1[r]];
@@ -625,9 +625,9 @@ __global__ void __launch_bounds__(1024) k_mg_sub(Dev D, __grid_constant__ const 
 template <typename T>
 __global__ void k_mg_l0_up(Dev D, double* __restrict__ out, int mode) {
     BS_PDL_ENTRY();
-    const int s = D.blk_scene[blockIdx.x];
-    if (mg_skip(D, s)) return;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[r / BS_ALIGN];
+    if (mg_skip(D, s)) return;
     if (r >= D.par[s].row0 + D.dyn[s].n) return;
     const T* __restrict__ zz = (const T*)(mode == 2 ? D.mg.u : D.mg.zz);
     const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
@@ -743,18 +743,18 @@ template <typename T>
 void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
     (void)in;   // the Krylov stream already wrote the input (mg_put_input)
     int q = tbegin(L, K_MG_L0DOWN);
-    launch_pdl(L, k_mg_l0_down<T>, gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, D);
+    launch_pdl(L, k_mg_l0_down<T>, gdiv((long)D.ncell_total * 32, L.mg0_tpb), L.mg0_tpb, 0, D);
     tend(L, q);
     cycle_t<T>(D, L, 1, 0);
     q = tbegin(L, K_MG_PROLONG);
-    launch_pdl(L, k_mg_l0_prolong<T>, L.nblk_rows, BS_THREADS, 0, D);
+    launch_pdl(L, k_mg_l0_prolong<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D);
     tend(L, q);
     q = tbegin(L, K_MG_L0UP);
     if (D.mg.post0 == 2) {
-        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 1);
-        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 2);
+        launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 1);
+        launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 2);
     } else {
-        launch_pdl(L, k_mg_l0_up<T>, L.nblk_rows, BS_THREADS, 0, D, out, 0);
+        launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 0);
     }
     tend(L, q);
 }

@@ -18,7 +18,7 @@ struct RowCtx {
 __device__ __forceinline__ RowCtx row_ctx(const Dev& D) {
     RowCtx c;
     c.r = blockIdx.x * blockDim.x + threadIdx.x;
-    c.s = D.blk_scene[blockIdx.x];
+    c.s = D.blk_scene[c.r / BS_ALIGN];   // the block's scene, whatever the block size
     const bool row = c.r < D.par[c.s].row0 + D.dyn[c.s].n;
     c.held = row && D.dyn[c.s].hold;
     c.active = row && !c.held;
@@ -1185,14 +1185,15 @@ __global__ void __launch_bounds__(BS_THREADS) k_ghost(Dev D, int use_mls) {
 #define BS_DISPATCH(id, prec, kern, ...)                                                          \
     do {                                                                                          \
         const int q_ = tbegin(L, id);                                                             \
-        if ((prec) == BS_PREC_MIXED) kern<float><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__); \
-        else kern<double><<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__);                  \
+        if ((prec) == BS_PREC_MIXED)                                                              \
+            kern<float><<<row_blocks(L, L.sweep_tpb), L.sweep_tpb, 0, L.stream>>>(__VA_ARGS__);   \
+        else kern<double><<<row_blocks(L, L.sweep_tpb), L.sweep_tpb, 0, L.stream>>>(__VA_ARGS__); \
         tend(L, q_);                                                                              \
     } while (0)
 #define BS_PLAIN(id, kern, ...)                                                                   \
     do {                                                                                          \
         const int q_ = tbegin(L, id);                                                             \
-        kern<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(__VA_ARGS__);                              \
+        kern<<<row_blocks(L, L.sweep_tpb), L.sweep_tpb, 0, L.stream>>>(__VA_ARGS__);              \
         tend(L, q_);                                                                              \
     } while (0)
 

@@ -321,8 +321,13 @@ int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path,
  * top, V-cycle below), "mg_sub" (0/1: the small levels of a visit as one
  * clustered launch), "ppe_precond", "fg_df" (0/1, default 1: the FGMRES basis
  * of the preconditioned mixed solve as double-float (hi, lo) FP32 pairs, its
- * dots on the FP32 pipe, h_{j+1,j} from the Gram relation);
- * bs_get_option also reads "mg_levels" and "mg_sub_level". */
+ * dots on the FP32 pipe, h_{j+1,j} from the Gram relation), "sweep_tpb" /
+ * "mg0_tpb" (64, 128 or 256 threads per block of the neighbour sweeps / of
+ * the particle-level multigrid kernels; every row is computed the same way
+ * whatever the block size), "step_graph" (0/1, default 1: each bs_step is
+ * one captured CUDA graph with the loops on the device);
+ * bs_get_option also reads "mg_levels", "mg_sub_level", "step_graph_steps"
+ * and "step_graph_cached". */
 int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
 int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);
 

@@ -66,3 +66,29 @@ def test_captured_step_batch_and_several_salinity_substeps(api):
     subs = [a.info(s)["solsteps"] for s in range(3)]
     assert max(subs) > 1, subs
     assert a.get_option("step_graph_steps") == 4
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_block_sizes_give_identical_steps(api, precision):
+    """The autotuner's launch shapes (threads per block of the neighbour
+    sweeps and of the particle-level multigrid kernels) change no result:
+    every row is computed by the same code whatever block it falls in."""
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.02, precision=precision)
+    ref = api.Context([p], [st], [gr], tuning="auto")
+    ref.set_option("sweep_tpb", 256)
+    ref.set_option("mg0_tpb", 256)
+    ref.prime()
+    ref.step(3)
+    want = ref.download()
+    for sw, mg in ((64, 128), (128, 64)):
+        c = api.Context([p], [st], [gr], tuning="auto")
+        c.set_option("sweep_tpb", sw)
+        c.set_option("mg0_tpb", mg)
+        assert c.get_option("sweep_tpb") == sw and c.get_option("mg0_tpb") == mg
+        c.prime()
+        c.step(3)
+        got = c.download()
+        for f in FIELDS:
+            assert np.array_equal(got[f], want[f]), (sw, mg, f)
+        assert c.info()["ppe_iters"] == ref.info()["ppe_iters"]
