@@ -6,7 +6,8 @@ for a small staged grid -- the Krylov method (BiCGStab, or FGMRES with a
 restart length), then the multigrid cycle shape (W-cycle depth,
 pre-smoothing on the particle and cell levels, Jacobi damping,
 coarse-correction scale, coarsest sweeps, the clustered subtree, the
-second particle-level post-sweep, the double-float FGMRES basis), the
+second particle-level post-sweep, the exact coarse solve, the double-float
+FGMRES basis), the
 threads per block of the neighbour sweeps and of the particle-level
 multigrid kernels, then the restart length again --
 and keeps the fastest configuration whose solves converged without error
@@ -22,7 +23,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
 OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_post0", "mg_omega", "mg_cscale",
-           "mg_coarse_sweeps", "mg_sub", "fg_df", "sweep_tpb", "mg0_tpb")
+           "mg_coarse_sweeps", "mg_sub", "mg_exact", "fg_df", "sweep_tpb", "mg0_tpb")
 
 
 def bucket(n_particles):
@@ -100,12 +101,13 @@ def tune(ctx, grains, steps=2, verbose=True):
 
     base = {"ppe_restart": 30, "ppe_solver": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9,
             "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0, "mg_post0": 1, "fg_df": 1,
-            "sweep_tpb": 256, "mg0_tpb": 256}
+            "sweep_tpb": 256, "mg0_tpb": 256, "mg_exact": 0}
     best, best_ms = dict(base), run(base)
     solver_stage = [{"ppe_solver": 0}] + [{"ppe_solver": 1, "ppe_restart": r} for r in (20, 30, 50, 80, 120)]
     stages = [
         solver_stage,
         [{"mg_wlev": w} for w in (0, 1, 2, 3, 4)],
+        [{"mg_exact": 1}],
         [{"mg_pre0": a, "mg_prec": b} for a in (0, 1) for b in (0, 1)],
         [{"mg_cscale": c} for c in (1.3, 1.5, 1.7)],
         [{"mg_omega": w} for w in (0.8, 0.9, 0.95, 1.0)],

@@ -66,6 +66,8 @@ struct bs_ctx {
     // threads per block of the neighbour sweeps and of the particle-level
     // multigrid kernels (options "sweep_tpb", "mg0_tpb"; the autotuner picks them)
     int sweep_tpb = BS_THREADS, mg0_tpb = BS_THREADS;
+    // exact coarse solve (option "mg_exact"): the scenes' exactly solved levels
+    MgExact mgexact{};
     // captured production steps (one CUDA graph per step, loops on the device):
     // cache keyed by the bytes the capture depends on; the pointer pairs the
     // stages swap cycle with a period of a few steps, so a few entries serve
@@ -185,6 +187,7 @@ bs::Launch launch_of(bs_ctx* c) {
     L.mgsub_cs = c->mgsub_cs;
     L.sweep_tpb = c->sweep_tpb;
     L.mg0_tpb = c->mg0_tpb;
+    L.exact = &c->mgexact;
     return L;
 }
 
@@ -223,7 +226,7 @@ void mg_sub_choose(bs_ctx* c) {
     c->mgsub_level = 0;
     c->mgsub_cs = 1;
     const MgDev& M = c->D.mg;
-    if (!c->mgsub_on || c->mglev.empty() || M.nlev < 1) return;
+    if (!c->mgsub_on || M.exact || c->mglev.empty() || M.nlev < 1) return;
     for (int l = 1; l <= M.nlev; ++l) {
         if (!(c->mgneed[l] & 1)) break;
         int mx = 0;
@@ -237,6 +240,19 @@ void mg_sub_choose(bs_ctx* c) {
         c->mgsub_cs = cs;
         return;
     }
+}
+
+// A scene's coarsest level: where its hierarchy ends (at most 256 cells), or
+// with the exact coarse solve its first level of at most BS_MG_EXACT_MAX
+// cells whose band LU factors fit the factorisation's shared memory.
+int coarsest_level(const bs_ctx* c, int s) {
+    const auto& d = c->mgdims[s];
+    if (c->D.mg.exact)
+        for (int l = 1; l <= (int)d.size(); ++l) {
+            const long m = (long)d[l - 1].first * d[l - 1].second;
+            if (m <= BS_MG_EXACT_MAX && m * (2L * (d[l - 1].second + 1) + 1) <= BS_MG_EXACT_BAND) return l;
+        }
+    return (int)d.size();
 }
 
 // Level tables (kernel arguments), the launches each level needs, and the
@@ -256,7 +272,7 @@ void mg_tables(bs_ctx* c) {
         std::vector<int> nxv(ns, 0), nyv(ns, 0);
         for (int s = 0; s < ns; ++s) {
             G.off[s] = o;
-            const int Lc = (int)c->mgdims[s].size();
+            const int Lc = coarsest_level(c, s);
             const bool has = Lc >= l;
             G.nx[s] = nxv[s] = has ? c->mgdims[s][l - 1].first : 0;
             G.ny[s] = nyv[s] = has ? c->mgdims[s][l - 1].second : 0;
@@ -270,7 +286,18 @@ void mg_tables(bs_ctx* c) {
         cudaMemcpy((void*)M.nx[l], nxv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
         cudaMemcpy((void*)M.ny[l], nyv.data(), sizeof(int) * ns, cudaMemcpyHostToDevice);
     }
-    for (int s = 0; s < ns; ++s) c->hpar[s].mg_lev = (int)c->mgdims[s].size();
+    c->mgexact = MgExact{};
+    c->mgexact.ns = ns;
+    for (int s = 0; s < ns; ++s) {
+        const int Lc = coarsest_level(c, s);
+        c->hpar[s].mg_lev = Lc;
+        if (M.exact && Lc >= 1) {
+            c->mgexact.l[s] = Lc;
+            c->mgexact.off[s] = c->mglev[Lc].off[s];
+            c->mgexact.nx[s] = c->mglev[Lc].nx[s];
+            c->mgexact.ny[s] = c->mglev[Lc].ny[s];
+        }
+    }
     mg_sub_choose(c);
 }
 
@@ -1028,6 +1055,20 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
         for (auto& p : ctx->prm) p.ppe_restart = (int32_t)value;
+    else if (k == "mg_exact" && (value == 0 || value == 1)) {
+        if (value == 1 && !M.ainv) {
+            const size_t per = (size_t)BS_MG_EXACT_MAX * BS_MG_EXACT_MAX * ctx->nscene;
+            int rc = bs::mg_exact_prepare();
+            if (rc) return fail(ctx, rc, "exact coarse solve: shared memory attribute");
+            char* a = nullptr;
+            rc = dalloc(ctx, &a, per * (ctx->precision == BS_PREC_MIXED ? sizeof(float) : sizeof(double)));
+            if (!rc) rc = dalloc(ctx, &M.xinv, per);
+            if (rc) return rc;
+            M.ainv = a;
+        }
+        M.exact = (int)value;
+        if (!ctx->mglev.empty()) mg_tables(ctx);
+    }
     else if ((k == "sweep_tpb" || k == "mg0_tpb") && (value == 64 || value == 128 || value == 256))
         (k == "sweep_tpb" ? ctx->sweep_tpb : ctx->mg0_tpb) = (int)value;
     else if (k == "step_graph" && (value == 0 || value == 1)) {
@@ -1060,6 +1101,7 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "fg_df") *value = ctx->fg_df_on;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
+    else if (k == "mg_exact") *value = M.exact;
     else if (k == "sweep_tpb") *value = ctx->sweep_tpb;
     else if (k == "mg0_tpb") *value = ctx->mg0_tpb;
     else if (k == "step_graph") *value = ctx->step_graph_on && !ctx->step_graph_broken;

@@ -99,7 +99,15 @@ struct MgDev {
     int post0;                        // level-0 post-sweeps (1 or 2)
     uint8_t* sub;                     // level 0: quadrant of the row in its cell (bit0 lower, bit1 right)
     int* agg1;                        // level 0: global level-1 index of the row's half-cell
+    // exact coarse solve (option mg_exact): each scene's hierarchy ends at
+    // its first level of at most BS_MG_EXACT_MAX cells, whose operator is
+    // inverted once per step; the visits apply the inverse
+    int exact;
+    void* ainv;                       // per scene: BS_MG_EXACT_MAX^2 values (the level's precision), row-major
+    double* xinv;                     // per scene: BS_MG_EXACT_MAX^2 doubles (the factorisation's work space)
 };
+#define BS_MG_EXACT_MAX 1024          // cells of an exactly solved level
+#define BS_MG_EXACT_BAND 20480        // band entries (doubles, shared memory) of its LU factors
 
 // One cell level's per-scene tables, passed to the level kernels by value
 // (__grid_constant__): scene k owns cells [off[k], off[k+1]) of the level, a
@@ -110,6 +118,11 @@ struct MgLevel {
     int off[BS_MG_MAXS + 1];
     int nx[BS_MG_MAXS], ny[BS_MG_MAXS];
     int lev[BS_MG_MAXS];       // the scene's coarsest level
+};
+// Per scene, the level solved exactly (0: none) and its grid and offset
+struct MgExact {
+    int ns;
+    int l[BS_MG_MAXS], off[BS_MG_MAXS], nx[BS_MG_MAXS], ny[BS_MG_MAXS];
 };
 
 // device pointers of one context (passed by value to kernels)
@@ -393,6 +406,7 @@ struct Launch {
     int mgsub_level, mgsub_cs;     // first level of the clustered subtree (0: per-level launches), CTAs per cluster
     int sweep_tpb;                 // threads per block of the neighbour sweeps (64, 128 or 256)
     int mg0_tpb;                   // threads per block of the particle-level multigrid kernels
+    const MgExact* exact;          // the scenes' exactly solved levels (when D.mg.exact)
 };
 // blocks of `tpb` threads over the rows of a batch (scenes own multiples of
 // BS_ALIGN rows, so a block never straddles two scenes for tpb | BS_ALIGN)
@@ -412,6 +426,22 @@ inline void launch_pdl(const Launch& L, void (*kernel)(KArgs...), unsigned grid,
                        Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = L.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+// the same with a 2-D grid
+template <typename... KArgs, typename... Args>
+inline void launch_pdl_2d(const Launch& L, void (*kernel)(KArgs...), dim3 grid, unsigned block, size_t smem,
+                          Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = L.stream;
@@ -485,6 +515,8 @@ struct ZoneDev {
 };
 void buffer_exchange(const Dev& D, const Launch& L, int s, const ScenePar& P, const ZoneDev& Z);
 int mg_sub_max_clusters(int mg_precision, int cs, size_t smem);
+// allow the exact coarse factorisation its shared memory (once per process)
+int mg_exact_prepare();
 void solve_fgmres(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_prec,
                   int* d_nconv, int* h_nconv, cudaEvent_t ev);
 // The same solves recorded into the stream capture of L.stream with their

@@ -564,6 +564,112 @@ __global__ void k_mg_coarse(Dev D, __grid_constant__ const MgLevel F, int acc) {
     op_coarse<T>(D.mg, view_of(F, k), acc, (T*)smem);
 }
 
+// ---- exact coarse solve (option mg_exact).  A scene's level of at most
+// BS_MG_EXACT_MAX cells (a 9-point Galerkin stencil on an nx x ny grid,
+// cells numbered q = j ny + i) is a band matrix of half-bandwidth b = ny + 1.
+// Once per step one block per scene factors it in FP64 (LU without pivoting,
+// in shared memory: the Jacobi-scaled PPE and its Galerkin products are
+// diagonally dominant M-matrices, whose pivots stay positive) and forms the
+// inverse by m forward/back substitutions in parallel, one right-hand side
+// per thread (the solution columns in global memory, coalesced across the
+// threads).  Each visit of the level then is one mat-vec z = A^-1 r, a warp
+// per row, in place of the Jacobi sweeps and the levels below.  Cells with
+// no particle (zero diagonal) are decoupled rows whose z stays 0; if a
+// pivot is not positive and finite the scene falls back to z = D^-1 r.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_exact_factor(Dev D, __grid_constant__ const MgExact E) {
+    BS_PDL_ENTRY();
+    const int k = blockIdx.x;
+    const int l = E.l[k];
+    if (l <= 0) return;
+    const int nx = E.nx[k], ny = E.ny[k], m = nx * ny;
+    if (m <= 0 || m > BS_MG_EXACT_MAX) return;
+    const int b = ny + 1, W = 2 * b + 1;
+    extern __shared__ double band[];   // row i: columns i-b .. i+b
+    __shared__ int bad;
+    const MgDev& M = D.mg;
+    const T* __restrict__ A = (const T*)M.A[l];
+    const long n = M.n[l];
+    const int off = E.off[k];
+    for (int e = threadIdx.x; e < m * W; e += blockDim.x) band[e] = 0.0;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        const int i = q % ny, j = q / ny;
+        const double dq = (double)A[4 * n + off + q];
+        if (dq == 0.0) {   // no particle in the cell: an identity row (its r is 0)
+            band[q * W + b] = 1.0;
+            continue;
+        }
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const int ni = i + (t % 3) - 1, nj = j + (t / 3) - 1;
+            if (ni < 0 || nj < 0 || ni >= ny || nj >= nx) continue;
+            band[q * W + (nj * ny + ni - q + b)] = (double)A[t * n + off + q];
+        }
+    }
+    __syncthreads();
+    for (int kk = 0; kk < m; ++kk) {
+        const double piv = band[kk * W + b];
+        const int nr = min(m - 1, kk + b) - kk;
+        if (threadIdx.x < nr) {
+            const int i = kk + 1 + threadIdx.x;
+            band[i * W + (kk - i + b)] /= piv;
+        }
+        if (threadIdx.x == 0 && !(piv > 0.0 && isfinite(piv))) bad = 1;
+        __syncthreads();
+        for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
+            const int i = kk + 1 + e / nr, jc = kk + 1 + e % nr;
+            band[i * W + (jc - i + b)] -= band[i * W + (kk - i + b)] * band[kk * W + (jc - kk + b)];
+        }
+        __syncthreads();
+    }
+    double* X = M.xinv + (long)k * BS_MG_EXACT_MAX * BS_MG_EXACT_MAX;
+    T* Ai = (T*)M.ainv + (long)k * BS_MG_EXACT_MAX * BS_MG_EXACT_MAX;
+    if (bad) {
+        const T* dinv = (const T*)M.dinv[l] + off;
+        for (long e = threadIdx.x; e < (long)m * m; e += blockDim.x) Ai[e] = (e / m == e % m) ? dinv[e / m] : (T)0;
+        return;
+    }
+    // column t of the inverse: L y = e_t (unit lower), then U x = y; X[i m + t]
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        for (int i = 0; i < m; ++i) {
+            double y = (i == t) ? 1.0 : 0.0;
+            for (int c = max(0, i - b); c < i; ++c) y -= band[i * W + (c - i + b)] * X[(long)c * m + t];
+            X[(long)i * m + t] = y;
+        }
+        for (int i = m - 1; i >= 0; --i) {
+            double x = X[(long)i * m + t];
+            for (int c = i + 1; c <= min(m - 1, i + b); ++c) x -= band[i * W + (c - i + b)] * X[(long)c * m + t];
+            X[(long)i * m + t] = x / band[i * W + b];
+        }
+    }
+    __syncthreads();
+    for (long e = threadIdx.x; e < (long)m * m; e += blockDim.x) Ai[e] = (T)X[e];
+}
+
+// z = A^-1 r on a scene's exactly solved level (added to z with acc): a warp
+// per row, lanes over the row, a fixed-order sum
+template <typename T>
+__global__ void k_mg_exact_apply(Dev D, __grid_constant__ const MgLevel F, int acc) {
+    BS_PDL_ENTRY();
+    const int k = blockIdx.y;
+    if (F.lev[k] != F.l) return;
+    const int m = F.nx[k] * F.ny[k];
+    const int lane = threadIdx.x & 31;
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= m) return;
+    const T* __restrict__ Ai = (const T*)D.mg.ainv + (long)k * BS_MG_EXACT_MAX * BS_MG_EXACT_MAX + (long)q * m;
+    const T* __restrict__ r = (const T*)D.mg.r[F.l] + F.off[k];
+    T a = 0;
+    for (int p = lane; p < m; p += 32) a += Ai[p] * r[p];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+        T* z = (T*)D.mg.z[F.l] + F.off[k];
+        z[q] = acc ? z[q] + a : a;
+    }
+}
+
 // ---- the levels from l0 down in one launch: one thread-block cluster per
 // scene (cluster rank r, nt threads over the cluster, one cell per thread
 // on the first level), the visit's level operations in order, a cluster
@@ -654,8 +760,14 @@ void setup_t(const Dev& D, const Launch& L) {
     tend(L, q);
     *L.launches += 1;
     for (int l = 1; l < D.mg.nlev; ++l) {
+        if (D.mg.exact && !(L.mgneed[l + 1] & 1)) break;   // below every scene's exact level
         q = tbegin(L, K_MG_GALC);
         launch_pdl(L, k_mg_galc<T>, gdiv(D.mg.n[l + 1], 128), 128, 0, D, l);
+        tend(L, q);
+    }
+    if (D.mg.exact && L.exact) {
+        q = tbegin(L, K_MG_GALC);
+        launch_pdl(L, k_mg_exact_factor<T>, D.nscene, 1024, BS_MG_EXACT_BAND * sizeof(double), D, *L.exact);
         tend(L, q);
     }
 }
@@ -720,7 +832,10 @@ void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     }
     if (need & 4) {
         q = tbegin(L, K_MG_COARSE);
-        launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
+        if (D.mg.exact)
+            launch_pdl_2d(L, k_mg_exact_apply<T>, dim3(BS_MG_EXACT_MAX / 8, D.nscene), 256, 0, D, G[l], acc);
+        else
+            launch_pdl(L, k_mg_coarse<T>, D.nscene, 256, 2 * D.mg.coarse_max * sizeof(T), D, G[l], acc);
         tend(L, q);
     }
     if (!(need & 2)) return;
@@ -791,6 +906,16 @@ int mg_sub_max_clusters(int mg_precision, int cs, size_t smem) {
         return 0;
     }
     return n;
+}
+
+int mg_exact_prepare() {
+    const int bytes = BS_MG_EXACT_BAND * (int)sizeof(double);
+    if (cudaFuncSetAttribute(k_mg_exact_factor<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_mg_exact_factor<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+            cudaSuccess)
+        return BS_E_CUDA;
+    return BS_OK;
 }
 
 void mg_setup(const Dev& D, const Launch& L, int mg_precision) {

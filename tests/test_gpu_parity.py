@@ -386,3 +386,46 @@ def test_pinned_upload_and_download_into_buffers(api):
     assert np.shares_memory(got["x"], buf["x"]) and len(got["x"]) == len(st["x"])
     with pytest.raises(ValueError):
         b.download(out=api.pinned_state(10))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_exact_coarse_solve(api, precision):
+    """The multigrid cycle with its coarsest levels replaced by an exact
+    solve of the first level of at most 1024 cells (option mg_exact):
+    the same converged pressure as the Jacobi-swept coarse levels when both
+    solve to 1e-12 (rel-L2 within 1e-7: two preconditioners, one system),
+    no more Krylov columns, and a batch gives each scene what it gives alone."""
+    from beachslope_gb300 import scene
+    p, st, gr = scene.beach_scene(dx=0.01, precision=precision)
+    p.ppe_tol = 1e-12
+    p.ppe_maxit = 20000
+    out = {}
+    for ex in (0, 1):
+        c = api.Context([p], [st], [gr], tuning="auto")
+        c.set_option("mg_exact", ex)
+        assert c.get_option("mg_exact") == ex
+        c.prime()
+        c.step(2)
+        out[ex] = (c.download(), c.info())
+        assert out[ex][1]["err_bits"] == 0 and out[ex][1]["ppe_relres"] <= 1e-11
+    g0, g1 = out[0][0], out[1][0]
+    o0, o1 = np.argsort(g0["pid"]), np.argsort(g1["pid"])
+    assert np.array_equal(g0["pid"][o0], g1["pid"][o1])
+    e = relL2(g1["p"][o1], g0["p"][o0])
+    print(f"exact vs swept coarse levels: p rel-L2 {e:.2e}, columns {out[1][1]['ppe_iters']} vs {out[0][1]['ppe_iters']}")
+    assert e <= 1e-7
+    assert out[1][1]["ppe_iters"] <= out[0][1]["ppe_iters"] + 1
+    scenes = [scene.beach_scene(dx=d, A=a, precision=precision) for d, a in ((0.03, 0.05), (0.02, 0.08))]
+    P, S, G = [q[0] for q in scenes], [q[1] for q in scenes], [q[2] for q in scenes]
+    batch = api.Context(P, S, G)
+    batch.set_option("mg_exact", 1)
+    batch.prime()
+    batch.step(2)
+    for k in range(2):
+        alone = api.Context([P[k]], [S[k]], [G[k]])
+        alone.set_option("mg_exact", 1)
+        alone.prime()
+        alone.step(2)
+        a, b = alone.download(), batch.download(k)
+        for f in ("x", "y", "vx", "vy", "p"):
+            assert np.array_equal(a[f], b[f]), f
