@@ -555,7 +555,8 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(bucket, C * BS_NCAT); A(cell_total, C); A(coderank, R);
     A(cell_maxvel, C); A(cell_maxeddy, C);
     A(gx, (size_t)gr); A(gy, (size_t)gr); A(gv, (size_t)gr); A(gcell_start, C); A(gcell_end, C);
-    A(gxr, (size_t)gr); A(gyr, (size_t)gr); A(xr, R); A(yr, R);
+    A(gxr, (size_t)gr); A(gyr, (size_t)gr); A(gpos4, (size_t)gr); A(xr, R); A(yr, R);
+    if (ctx->precision == BS_PREC_MIXED) A(pos4, R);
     A(part, (size_t)blk * BS_MAXDOT);
     A(err_word, 1);
 #undef A
@@ -827,6 +828,7 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
         const int m = (int)gk.size();
         std::vector<double> gx(m), gy(m), gv(m);
         std::vector<float> gxr(m), gyr(m);
+        std::vector<float4> gp4(m);
         std::vector<int> gs(P.ncell, 0), ge(P.ncell, 0), cnt(P.ncell, 0);
         for (int q = 0; q < m; ++q) {
             const int k = gk[q].second;
@@ -836,6 +838,8 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
             const int cj = gk[q].first / p.celly + 1, ci = gk[q].first % p.celly + 1;
             gxr[q] = (float)(gx[q] - xleft_of(p, cj));
             gyr[q] = (float)(gy[q] - ybot_of(p, ci));
+            const float xh = (float)gx[q], yh = (float)gy[q];
+            gp4[q] = make_float4(xh, (float)(gx[q] - (double)xh), yh, (float)(gy[q] - (double)yh));
             cnt[gk[q].first]++;
         }
         int acc = ctx->grain0[s];
@@ -851,6 +855,7 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
             CK(cudaMemcpy(D.gv + g0, gv.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
             CK(cudaMemcpy(D.gxr + g0, gxr.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
             CK(cudaMemcpy(D.gyr + g0, gyr.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(D.gpos4 + g0, gp4.data(), sizeof(float4) * m, cudaMemcpyHostToDevice));
         }
         CK(cudaMemcpy(D.gcell_start + P.cell0, gs.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(D.gcell_end + P.cell0, ge.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));

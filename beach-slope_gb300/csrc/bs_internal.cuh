@@ -130,6 +130,7 @@ struct Dev {
     // particle fields (current buffer)
     double *x, *y, *xs, *ys, *vx, *vy, *vxs, *vys, *p, *mass, *rho, *oden, *ovol, *con;
     float *xr, *yr;                 // position relative to the row's cell corner (xleft, ybot), FP32
+    float4* pos4;                   // mixed: position as (x hi, x lo, y hi, y lo) FP32 pairs (pos_split)
     double *vol, *nu;               // derived: m/rho, vis(oden)/oden
     int8_t* tid;
     uint8_t* flags;
@@ -190,6 +191,7 @@ struct Dev {
     // grains (static, sorted by cell)
     double *gx, *gy, *gv;           // gv = mass/density
     float *gxr, *gyr;               // grain position relative to its cell corner, FP32
+    float4* gpos4;                  // grain position as (x hi, x lo, y hi, y lo) FP32 pairs
     int *gcell_start, *gcell_end;
     int ncell_total, nrow_total, nblk_total, nscene;
     int kmax;
@@ -273,6 +275,86 @@ __device__ __forceinline__ double fast_rcp64(double d) {
     double y = (double)__frcp_rn((float)d);
     y = y * (2.0 - d * y);
     return y;
+}
+
+// ---------------------------------------------------- pair offsets on the FP32 pipe
+// The mixed form's neighbour sweeps take the pair offset x_j - x_i and the
+// pair distance from double-float positions (a value as hi + lo, two FP32
+// numbers; Dekker 1971, Knuth's TwoSum) instead of FP64 arithmetic: on this
+// part the FP64 pipe issues 2 lanes per clock per SM against 128 for FP32, and
+// one FP64 instruction per pair costs as much as ~60 FP32 ones.  Every
+// rounding is explicit (no contraction).
+
+// a + b = s + e exactly
+__device__ __forceinline__ float2 f2_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return make_float2(s, e);
+}
+// a + b = s + e exactly, for |a| >= |b|
+__device__ __forceinline__ float2 f2_fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+// (hi, lo) of a double: hi = fl32(v), lo = fl32(v - hi); |v - hi - lo| <= 2^-48 |v|
+__device__ __forceinline__ float2 f2_split(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+}
+// a position row as (x hi, x lo, y hi, y lo)
+__device__ __forceinline__ float4 pos_split(double x, double y) {
+    const float2 a = f2_split(x), b = f2_split(y);
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+// b - a of two double-float coordinates, renormalised (.x = fl32 of the
+// difference): the hi parts subtracted exactly, the lo parts added; absolute
+// error within ~2^-46 max(|a|, |b|) (1e-13 m on a 4 m domain)
+__device__ __forceinline__ float2 pos_diff(float bh, float bl, float ah, float al) {
+    const float2 s = f2_two_sum(bh, -ah);
+    return f2_two_sum(s.x, __fadd_rn(s.y, __fsub_rn(bl, al)));
+}
+// Pair distance from a double-float offset (dx, dy): s = dx^2 + dy^2 as
+// double-float (TwoProduct by FMA), r = sqrt(s) as (rh, rl) by one Newton
+// step from the FP32 reciprocal square root y (r = r0 + (s - r0^2) y / 2,
+// r0 = fl(s y); the residual s - r0^2 exact by Sterbenz and FMA), and 1/r
+// by one Newton step y (1 + (1 - r y)).  rh = fl32(r) and ir = fl32(1/r)
+// up to ties (relative error of r before rounding ~2^-44); sh = fl32(s).
+struct PairR {
+    float rh, rl, ir, sh;
+};
+__device__ __forceinline__ PairR pair_r(float2 dx, float2 dy) {
+    const float p1 = __fmul_rn(dx.x, dx.x);
+    const float e1 = __fmaf_rn(__fmul_rn(2.0f, dx.x), dx.y, __fmaf_rn(dx.x, dx.x, -p1));
+    const float p2 = __fmul_rn(dy.x, dy.x);
+    const float e2 = __fmaf_rn(__fmul_rn(2.0f, dy.x), dy.y, __fmaf_rn(dy.x, dy.x, -p2));
+    const float2 s0 = f2_two_sum(p1, p2);
+    const float2 s = f2_fast_two_sum(s0.x, __fadd_rn(s0.y, __fadd_rn(e1, e2)));
+    const float y = rsqrtf(s.x);
+    const float r0 = __fmul_rn(s.x, y);
+    const float q = __fmul_rn(r0, r0);
+    const float d = __fadd_rn(__fsub_rn(__fsub_rn(s.x, q), __fmaf_rn(r0, r0, -q)), s.y);
+    const float2 r = f2_fast_two_sum(r0, __fmul_rn(d, __fmul_rn(0.5f, y)));
+    const float t = __fmaf_rn(-r.y, y, __fmaf_rn(-r.x, y, 1.0f));
+    PairR o;
+    o.rh = r.x;
+    o.rl = r.y;
+    o.ir = __fmaf_rn(y, t, y);
+    o.sh = s.x;
+    return o;
+}
+// r < c for a double-float r and a double c given as (ch, cl)
+__device__ __forceinline__ bool f2_less(float rh, float rl, float ch, float cl) {
+    return rh < ch || (rh == ch && rl < cl);
+}
+// fl32(2 - r * ih) for a double-float r and ih = (ihh, ihl), r ih in [1, 2]
+// (2 - p exact by Sterbenz)
+__device__ __forceinline__ float f2_two_minus_prod(float rh, float rl, float ihh, float ihl) {
+    const float p = __fmul_rn(rh, ihh);
+    float pe = __fmaf_rn(rh, ihh, -p);
+    pe = __fmaf_rn(rh, ihl, pe);
+    pe = __fmaf_rn(rl, ihh, pe);
+    return __fsub_rn(__fsub_rn(2.0f, p), pe);
 }
 
 // Radial factor F(r) of the hybrid-kernel gradient: grad_i W_ij = F(r) (r_i - r_j)

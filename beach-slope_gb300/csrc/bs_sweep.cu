@@ -26,47 +26,44 @@ __device__ __forceinline__ RowCtx row_ctx(const Dev& D) {
 }
 
 // The four cells of the quadrant stencil in the reference's order
-// (search.f90:328-388); false for a non-finite position.
-__device__ __forceinline__ bool quad_cells(const ScenePar& P, int c, double xi, double yi, int cc[4], int& own_q) {
+// (search.f90:328-388): cell q lies (di0 + (q & 1), dj0 + (q >> 1)) rows and
+// columns from the row's cell c, i.e. at c + dj celly + di.  ordp packs
+// effpor's order of the same four (porous.f90:125-176: the row's own cell,
+// then the other three of the quadrant as listed), two bits per entry.
+// False for a non-finite position.
+__device__ __forceinline__ bool quad_cells(const ScenePar& P, int c, double xi, double yi, int& di0, int& dj0,
+                                          int& ordp) {
     const int lc = c - P.cell0;
     const int i = lc % P.celly + 1, j = lc / P.celly + 1;
     const double xl = cell_xleft(P, j), xr = cell_xright(P, j);
     const double yb = cell_ybot(P, i), yt = cell_ytop(P, i);
     const double mx = xl + fabs((xl - xr) / 2.0);
     const double my = yb + fabs((yt - yb) / 2.0);
-    int ci[4], cj[4];
     if (xi <= mx && yi <= my) {
-        ci[0] = i; cj[0] = j - 1; ci[1] = i + 1; cj[1] = j - 1; ci[2] = i; cj[2] = j; ci[3] = i + 1; cj[3] = j;
-        own_q = 2;
+        di0 = 0; dj0 = -1; ordp = 2 | 0 << 2 | 3 << 4 | 1 << 6;
     } else if (xi > mx && yi <= my) {
-        ci[0] = i; cj[0] = j; ci[1] = i + 1; cj[1] = j; ci[2] = i; cj[2] = j + 1; ci[3] = i + 1; cj[3] = j + 1;
-        own_q = 0;
+        di0 = 0; dj0 = 0; ordp = 0 | 2 << 2 | 1 << 4 | 3 << 6;
     } else if (xi > mx && yi > my) {
-        ci[0] = i - 1; cj[0] = j; ci[1] = i; cj[1] = j; ci[2] = i - 1; cj[2] = j + 1; ci[3] = i; cj[3] = j + 1;
-        own_q = 1;
+        di0 = -1; dj0 = 0; ordp = 1 | 2 << 2 | 0 << 4 | 3 << 6;
     } else if (xi <= mx && yi > my) {
-        ci[0] = i - 1; cj[0] = j - 1; ci[1] = i; cj[1] = j - 1; ci[2] = i - 1; cj[2] = j; ci[3] = i; cj[3] = j;
-        own_q = 3;
+        di0 = -1; dj0 = -1; ordp = 3 | 2 << 2 | 0 << 4 | 1 << 6;
     } else {
         return false;
     }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) cc[q] = P.cell0 + (cj[q] - 1) * P.celly + (ci[q] - 1);
     return true;
 }
 
-// corner of cell cq relative to the corner of cell c (both global indices),
-// rounded to FP32 once
-__device__ __forceinline__ void cell_offset(const ScenePar& P, int c, int cq, float& ox, float& oy) {
-    const int l = c - P.cell0, lq = cq - P.cell0;
-    const int i = l % P.celly + 1, j = l / P.celly + 1;
-    const int iq = lq % P.celly + 1, jq = lq / P.celly + 1;
-    ox = (float)(cell_xleft(P, jq) - cell_xleft(P, j));
-    oy = (float)(cell_ybot(P, iq) - cell_ybot(P, i));
+// Corner of the cell (dj, di) steps away relative to the row's own cell
+// corner, in FP32: cell_xleft advances by the cell width 4h per column and
+// cell_ybot falls by 4h per row (setup.f90:120-123).
+__device__ __forceinline__ void cell_offset(float cwf, int dj, int di, float& ox, float& oy) {
+    ox = (float)dj * cwf;
+    oy = (float)(-di) * cwf;
 }
 
 // FP32 position of every row relative to its cell's corner (the search's
-// candidate prefilter reads 8 bytes per candidate and no FP64)
+// candidate prefilter reads 8 bytes per candidate and no FP64) and, in the
+// mixed form, the double-float position the pair offsets are taken from
 __global__ void k_relpos(Dev D) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
@@ -74,8 +71,10 @@ __global__ void k_relpos(Dev D) {
     const int r = R.r;
     const int lc = D.cell[r] - P.cell0;
     const int i = lc % P.celly + 1, j = lc / P.celly + 1;
-    D.xr[r] = (float)(D.x[r] - cell_xleft(P, j));
-    D.yr[r] = (float)(D.y[r] - cell_ybot(P, i));
+    const double x = D.x[r], y = D.y[r];
+    D.xr[r] = (float)(x - cell_xleft(P, j));
+    D.yr[r] = (float)(y - cell_ybot(P, i));
+    if (P.precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
 }
 
 template <typename T>
@@ -99,8 +98,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
     const int r = R.r;
     const int tid = D.tid[r];
     const double xi = D.x[r], yi = D.y[r];
-    int cc[4], own_q;
-    const bool ok = quad_cells(P, D.cell[r], xi, yi, cc, own_q);
+    const int c = D.cell[r];
+    int di0, dj0, ordp;
+    const bool ok = quad_cells(P, c, xi, yi, di0, dj0, ordp);
+    const float cwf = (float)P.cw;
     uint8_t fl = D.flags[r];
     if (do_search) {
         const int kmax = D.kmax;
@@ -129,10 +130,12 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         if (ok) {
             const float xri = D.xr[r], yri = D.yr[r];
             for (int q = 0; q < 4; ++q) {
+                const int di = di0 + (q & 1), dj = dj0 + (q >> 1);
+                const int cq = c + dj * P.celly + di;
                 float ox, oy;
-                cell_offset(P, D.cell[r], cc[q], ox, oy);
-                const int r1 = D.cell_end[cc[q]];
-                int rj = D.cell_start[cc[q]];
+                cell_offset(cwf, dj, di, ox, oy);
+                const int r1 = D.cell_end[cq];
+                int rj = D.cell_start[cq];
                 for (; rj + 1 < r1; rj += 2) {   // two independent candidate loads in flight
                     const float x0 = __ldg(D.xr + rj) + ox, y0 = __ldg(D.yr + rj) + oy;
                     const float x1 = __ldg(D.xr + rj + 1) + ox, y1 = __ldg(D.yr + rj + 1) + oy;
@@ -149,30 +152,35 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         // the gradient-correction sums (search.f90:61-85).
         double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
         if (sizeof(T) == 4) {
-            // mixed: the pair quantities are stored in FP32.  r, 1/r and
-            // 2 - r/h come from FP64 (offsets exact, Newton square root): near
-            // the cut-off the kernel gradient goes as (2 - r/h)^2 and an FP32
-            // r would put errors of 1e-4 relative into it; the rest of the
-            // pair math is FP32 (the FP64 pipe of this part is the search's
-            // bound).  The correction sums are compensated FP32 sums.
+            // mixed: the pair quantities are stored in FP32 and computed on
+            // the FP32 pipe from double-float positions: the offset x_j - x_i
+            // (pos_diff, ~1e-13 m), r and 1/r (pair_r, r to ~2^-44 before
+            // rounding) and 2 - r/h (near the cut-off the kernel gradient
+            // goes as (2 - r/h)^2, so an FP32 r would put errors of 1e-4
+            // relative into it); each stored value is the FP32 rounding of
+            // the FP64 one up to ties.  The correction sums are compensated
+            // FP32 sums.
             Kahan32 f00, f01, f10, f11;
             const float ihf = (float)P.inv_h, ih2f = (float)P.inv_h2, ih3f = (float)P.inv_h3;
             const float c1f = (float)P.cn1, c2f = (float)P.cn2;
+            const float2 hf = f2_split(P.h), ihd = f2_split(P.inv_h);
+            const float lamf = (float)P.lam;
+            const float4 pi4 = D.pos4[r];
             for (int k = 0; k < n; ++k) {
                 const long e = ell(r, k, kmax);
                 const int rj = D.nidx[e];
-                const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
-                const double s2d = dx * dx + dy * dy;
-                double radd, ird;
-                fast_r64(s2d, radd, ird);
-                const float fx = (float)dx, fy = (float)dy;
-                const float rad = (float)radd, ir = (float)ird;
-                const float rinv = __frcp_rn((float)s2d + (float)P.lam);
+                const float4 pj4 = __ldg(D.pos4 + rj);
+                const float2 dx = pos_diff(pj4.x, pj4.y, pi4.x, pi4.y);
+                const float2 dy = pos_diff(pj4.z, pj4.w, pi4.z, pi4.w);
+                const PairR pr = pair_r(dx, dy);
+                const float fx = dx.x, fy = dy.x;
+                const float rad = pr.rh, ir = pr.ir;
+                const float rinv = __frcp_rn(pr.sh + lamf);
                 float F;
-                if (radd < P.h) {
+                if (f2_less(pr.rh, pr.rl, hf.x, hf.y)) {
                     F = c1f * (9.0f * rad * ih3f - 12.0f * ih2f) + c2f * (3.0f * rad * ih3f - 6.0f * ihf * ir);
                 } else {
-                    const float a = (float)(2.0 - radd * P.inv_h);
+                    const float a = f2_two_minus_prod(pr.rh, pr.rl, ihd.x, ihd.y);
                     F = -(c1f + c2f) * (3.0f * ihf * ir) * a * a;
                 }
                 const float kx = F * (-fx), ky = F * (-fy);
@@ -196,18 +204,9 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             const long e = ell(r, k, kmax);
             const int rj = D.nidx[e];
             const double dx = __ldg(D.x + rj) - xi, dy = __ldg(D.y + rj) - yi;
-            double rad, ir, rinv;
-            if (sizeof(T) == 4) {
-                // mixed: r and 1/r from Newton steps (no IEEE sqrt/division);
-                // stored in FP32, sums below stay FP64-accurate
-                const double s2 = dx * dx + dy * dy;
-                fast_r64(s2, rad, ir);
-                rinv = fast_rcp64(s2 + P.lam);
-            } else {
-                rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                ir = 1.0 / rad;
-                rinv = 1.0 / (rad * rad + P.lam);
-            }
+            const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+            const double ir = 1.0 / rad;
+            const double rinv = 1.0 / (rad * rad + P.lam);
             double F;
             if (rad < P.h) {
                 F = P.cn1 * (9.0 * rad * P.inv_h3 - 12.0 * P.inv_h2) + P.cn2 * (3.0 * rad * P.inv_h3 - 6.0 * P.inv_h * ir);
@@ -236,7 +235,9 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             const double det = a00 * a11 - a01 * a10;
             double c0 = 1.0, c1 = 0.0, c2 = 0.0, c3 = 1.0;
             if (fabs(det) >= BS_SP1EM5 && isfinite(det)) {
-                const double id = 1.0 / det;
+                // mixed: 1/det by a Newton step from the FP32 reciprocal
+                // (~1e-14; det is a sum of FP32-accurate terms)
+                const double id = sizeof(T) == 4 ? fast_rcp64(det) : 1.0 / det;
                 c0 = a11 * id;
                 c1 = -a01 * id;
                 c2 = -a10 * id;
@@ -255,28 +256,31 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             if (ok) {
                 // effpor's cell order (porous.f90:125-176): its own cell, then
                 // the other three of the same quadrant in the listed order
-                int ord[4];
-                if (own_q == 2) { ord[0] = cc[2]; ord[1] = cc[0]; ord[2] = cc[3]; ord[3] = cc[1]; }
-                else if (own_q == 0) { ord[0] = cc[0]; ord[1] = cc[2]; ord[2] = cc[1]; ord[3] = cc[3]; }
-                else if (own_q == 1) { ord[0] = cc[1]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[3]; }
-                else { ord[0] = cc[3]; ord[1] = cc[2]; ord[2] = cc[0]; ord[3] = cc[1]; }
                 const double wsolid = 1.0 - P.por * 1.0;
                 const float wsf = (float)wsolid, t2c = (float)(P.twoh * P.twoh);
                 Kahan32 sff;
                 const float t2f = (float)(P.twoh * P.twoh) * (1.0f + 1e-5f);
                 const float xri = D.xr[r], yri = D.yr[r];
-                for (int q = 0; q < 4; ++q) {
+                float4 pi4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (sizeof(T) == 4) pi4 = D.pos4[r];
+                for (int k = 0; k < 4; ++k) {
+                    const int q = (ordp >> (2 * k)) & 3;
+                    const int di = di0 + (q & 1), dj = dj0 + (q >> 1);
+                    const int cq = c + dj * P.celly + di;
                     float ox, oy;
-                    cell_offset(P, D.cell[r], ord[q], ox, oy);
-                    const int g1 = D.gcell_end[ord[q]];
-                    for (int g = D.gcell_start[ord[q]]; g < g1; ++g) {
+                    cell_offset(cwf, dj, di, ox, oy);
+                    const int g1 = D.gcell_end[cq];
+                    for (int g = D.gcell_start[cq]; g < g1; ++g) {
                         // FP32 prefilter (as in the neighbour scan): a grain
                         // rejected here is outside 2h in FP64 as well
                         const float fx = (__ldg(D.gxr + g) + ox) - xri, fy = (__ldg(D.gyr + g) + oy) - yri;
                         if (fx * fx + fy * fy > t2f) continue;
-                        const double dx = xi - D.gx[g], dy = yi - D.gy[g];
-                        if (sizeof(T) == 4) {   // mixed: FP32 (W(2h) = 0: the cut needs no exact test)
-                            const float ex = (float)dx, ey = (float)dy;
+                        if (sizeof(T) == 4) {
+                            // mixed: FP32 (W(2h) = 0: the cut needs no exact
+                            // test), the offset from the double-float positions
+                            const float4 g4 = __ldg(D.gpos4 + g);
+                            const float ex = pos_diff(pi4.x, pi4.y, g4.x, g4.y).x;
+                            const float ey = pos_diff(pi4.z, pi4.w, g4.z, g4.w).x;
                             const float s2 = ex * ex + ey * ey;
                             if (s2 < t2c) {
                                 float rad = 0.0f;   // grains may coincide with pore particles
@@ -288,6 +292,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                                 sff.add(wsf * bs_Wf(rad, P) * (float)D.gv[g]);
                             }
                         } else {
+                            const double dx = xi - D.gx[g], dy = yi - D.gy[g];
                             const double rad = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                             if (rad < P.twoh) sf = sf + wsolid * bs_W(rad, P) * D.gv[g];
                         }
@@ -304,14 +309,29 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 D.vol_new[r] = D.vol[r];
             } else {
                 D.rho_new[r] = rn;
-                D.vol_new[r] = D.mass[r] / rn;
+                D.vol_new[r] = sizeof(T) == 4 ? D.mass[r] * fast_rcp64(rn) : D.mass[r] / rn;
             }
             const double phi3 = phi * phi * phi;
-            const double Fch = 1.750 / sqrt(150.0 * phi3);
             const double vx = D.vx[r], vy = D.vy[r];
-            const double vm = sqrt(vx * vx + vy * vy);
-            res = -((bs_vis(od) / od) * P.lamk * ((1.0 - phi) * (1.0 - phi)) / (phi3 * (P.d50 * P.d50))) -
-                  ((Fch * vm * sqrt(P.lamk) * (1.0 - phi)) / (sqrt(phi3) * P.d50));
+            if (sizeof(T) == 4) {
+                // mixed: the same drag with Newton-step reciprocals and square
+                // roots (~1e-13 relative) in place of IEEE division and sqrt
+                double sp3, isp3, vm = 0.0, slk = 0.0, t;
+                fast_r64(150.0 * phi3, t, isp3);
+                const double Fch = 1.750 * isp3;
+                fast_r64(phi3, sp3, t);
+                const double v2 = vx * vx + vy * vy;
+                if (v2 > 0.0) fast_r64(v2, vm, t);
+                if (P.lamk > 0.0) fast_r64(P.lamk, slk, t);
+                const double om = 1.0 - phi;
+                res = -(bs_vis(od) * fast_rcp64(od) * P.lamk * (om * om) * fast_rcp64(phi3 * (P.d50 * P.d50))) -
+                      (Fch * vm * slk * om * fast_rcp64(sp3 * P.d50));
+            } else {
+                const double Fch = 1.750 / sqrt(150.0 * phi3);
+                const double vm = sqrt(vx * vx + vy * vy);
+                res = -((bs_vis(od) / od) * P.lamk * ((1.0 - phi) * (1.0 - phi)) / (phi3 * (P.d50 * P.d50))) -
+                      ((Fch * vm * sqrt(P.lamk) * (1.0 - phi)) / (sqrt(phi3) * P.d50));
+            }
         } else {
             D.rho_new[r] = D.rho[r];
             D.vol_new[r] = D.vol[r];
@@ -649,8 +669,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
         // x = (x + xs + dt*vx/porosity)/2 (integrator.f90:859-863), no FMA
         const double x = D.x[r], y = D.y[r];
         const double xn = __ddiv_rn(__dadd_rn(__dadd_rn(x, D.xs[r]), __ddiv_rn(__dmul_rn(dt, vx), phi)), 2.0);
+        const double yn = __ddiv_rn(__dadd_rn(__dadd_rn(y, D.ys[r]), __ddiv_rn(__dmul_rn(dt, vy), phi)), 2.0);
         D.x[r] = xn;
-        D.y[r] = __ddiv_rn(__dadd_rn(__dadd_rn(y, D.ys[r]), __ddiv_rn(__dmul_rn(dt, vy), phi)), 2.0);
+        D.y[r] = yn;
+        if (sizeof(T) == 4) D.pos4[r] = pos_split(xn, yn);
         // buffer release (integrator.f90:865-872)
         const ScenePar& P = D.par[R.s];
         if ((fl & BS_FLAG_BUFFER) && (xn > P.buf_lo) && (xn < P.buf_hi)) D.flags[r] = fl & ~BS_FLAG_BUFFER;
@@ -720,8 +742,10 @@ __global__ void k_apply_density(Dev D, int do_apply, int do_density) {
     if (D.tid[r] != BS_TID_FLUID) return;
     const uint8_t fl = D.flags[r];
     if (do_apply && !(fl & BS_FLAG_BUFFER)) {
-        D.x[r] = __dadd_rn(D.x[r], D.xs[r]);
-        D.y[r] = __dadd_rn(D.y[r], D.ys[r]);
+        const double x = __dadd_rn(D.x[r], D.xs[r]), y = __dadd_rn(D.y[r], D.ys[r]);
+        D.x[r] = x;
+        D.y[r] = y;
+        if (P.precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
         D.vx[r] = D.vx[r] + D.vxs[r];
         D.vy[r] = D.vy[r] + D.vys[r];
     }
@@ -1088,8 +1112,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_coll_apply(Dev D, int mode) {
     if (D.tid[r] != BS_TID_FLUID || (D.flags[r] & BS_FLAG_BUFFER)) return;
     if (mode == 0) {
         if (D.gradvx[r] >= 0.70) {
-            D.x[r] = __dadd_rn(D.x[r], D.xs[r]);
-            D.y[r] = __dadd_rn(D.y[r], D.ys[r]);
+            const double x = __dadd_rn(D.x[r], D.xs[r]), y = __dadd_rn(D.y[r], D.ys[r]);
+            D.x[r] = x;
+            D.y[r] = y;
+            if (D.par[R.s].precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
         }
     } else {
         D.vx[r] = __dadd_rn(D.vx[r], __dmul_rn(D.vxs[r], D.por[r]));

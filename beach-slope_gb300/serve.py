@@ -55,7 +55,7 @@ class Server:
         """Device bytes one slot of `rows` rows reserves: the per-row arrays
         (particles, neighbour list, matrix, multigrid, Krylov basis) at the
         measured bytes per row, the grains and the per-cell arrays."""
-        return rows * bytes_per_row + grains * 40.0 + template.cellx * template.celly * 120.0
+        return rows * bytes_per_row + grains * 56.0 + template.cellx * template.celly * 120.0
 
     @staticmethod
     def slots_for_memory(template, rows, grains, budget_bytes, bytes_per_row, max_slots=64):
