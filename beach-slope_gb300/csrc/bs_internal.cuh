@@ -66,7 +66,8 @@ struct SceneDyn {                 // per-scene dynamic state (device)
     double part_tmp;
     // FGMRES: Arnoldi column of the current cycle, cycle state (0 running,
     // 1 restart, 2 converged, 3 iteration cap) and the columns the update applies
-    int fg_j, fg_state, fg_k, fg_pad;
+    int fg_j, fg_state, fg_k;
+    int asm_split;                 // 1: the mixed assembly wrote aval32/aval_lo with aval (k_mx_convert skips the split)
     double fg_rinv;                // 1 / the norm of the vector the next column normalises
 };
 
@@ -150,6 +151,10 @@ struct Dev {
     double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
     double *tden, *whyd;            // WCSPH: continuity density, hydrostatic Tait density per row
     double *qa, *qu, *qw, *qi;      // per-row quotients of the sweeps (k_quot): rho/phi, u/phi, w/phi, 1/phi
+    // mixed: what a neighbour reads of a row in the assembly, packed by
+    // k_quot: (u/phi, w/phi) and (vxs, vys) as (hi, lo) FP32 pairs (their
+    // differences cancel), (rho/phi, m/rho, oden, 0) in FP32
+    float4 *qrec_u, *qrec_v, *qrec_a;
     double *con_new;
     // neighbour lists (ELL)
     int* ncount;

@@ -464,7 +464,8 @@ __global__ void k_mx_update(Dev D) {
     D.p[r] = D.p[r] + sqrt(Y.rnorm2) * (double)D.fd[r];
 }
 
-// FP32 copy of the assembled FP64 matrix values (inner operator)
+// FP32 copy of the assembled FP64 matrix values (inner operator): hi part
+// and the remainder; nothing to do where the mixed assembly already wrote them
 __global__ void k_mx_convert(Dev D) {
     BS_PDL_ENTRY();
     const int s = D.blk_scene[blockIdx.x];
@@ -473,7 +474,7 @@ __global__ void k_mx_convert(Dev D) {
         D.dyn[s].outer = 0;
         D.dyn[s].iters = 0;
     }
-    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    if (r >= D.par[s].row0 + D.dyn[s].n || D.dyn[s].asm_split) return;
     const double* A = (const double*)D.aval;
     float* F = D.aval32;
     const int n = D.ncount[r];

@@ -510,20 +510,138 @@ __global__ void k_quot(Dev D, int mode) {
         return;
     }
     const double ip = 1.0 / phi;
-    D.qa[r] = D.rho[r] * ip;
-    D.qu[r] = D.vxs[r] * ip;
-    D.qw[r] = D.vys[r] * ip;
+    const double qa = D.rho[r] * ip, qu = D.vxs[r] * ip, qw = D.vys[r] * ip;
+    D.qa[r] = qa;
+    D.qu[r] = qu;
+    D.qw[r] = qw;
     D.qi[r] = ip;
+    if (D.par[R.s].precision == BS_PREC_MIXED) {
+        D.qrec_u[r] = pos_split(qu, qw);
+        D.qrec_v[r] = pos_split(D.vxs[r], D.vys[r]);
+        D.qrec_a[r] = make_float4((float)qa, (float)D.vol[r], (float)D.oden[r], 0.0f);
+    }
 }
 
 // ppesolve assembly (isph.f90:115-456) with the quotients of k_quot:
 // rho_ij = 2 a_j a_i / (a_j + a_i) with a = rho/phi, the velocity terms as
 // rho_ij (vxs_j/phi_j - vxs_i/phi_i) -- the reference's expressions
 // regrouped, one division per fluid pair
+// The mixed form of the assembly: the same entries and right-hand side on
+// the FP32 pipe.  Pair offsets and the cancelling differences (u/phi, w/phi,
+// vxs, vys of the pair) are taken from double-float copies (pos4, qrec_u,
+// qrec_v: the FP32 rounding of the FP64 difference), the products in FP32,
+// the diagonal and the right-hand side as compensated sums; the Jacobi
+// scaling writes the FP64 values and their double-float split (aval32 +
+// aval_lo) for the solver.
+__device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
+    const ScenePar& P = D.par[R.s];
+    const int r = R.r;
+    const int ti = D.tid[r];
+    const uint8_t fl = D.flags[r];
+    const float4 pi4 = D.pos4[r];
+    const float4 ui = D.qrec_u[r], vi = D.qrec_v[r];
+    const float ai = D.qrec_a[r].x;                       // rho_i/phi_i
+    const float bi = (float)(D.qa[r] * D.qi[r]);          // rho_i/phi_i^2
+    const float c0 = (float)D.c0[r], c1 = (float)D.c1[r], c2 = (float)D.c2[r], c3 = (float)D.c3[r];
+    const bool freei = fl & BS_FLAG_FREE;
+    const float lampf = (float)(1.0 / (P.rho * P.rel_den));
+    const float voli = ti == BS_TID_WALL ? (float)(D.mass[r] / D.rho[r]) : 0.0f;
+    const int n = D.ncount[r];
+    const int kmax = D.kmax;
+    float* a32 = D.aval32;
+    Kahan32 dia, fv;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const int j = D.nidx[e];
+        const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
+        const float pd = ld<float>(D.nrinv, e);
+        const int tj = D.tid[j];
+        const float4 pj4 = __ldg(D.pos4 + j);
+        const float dxi = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x;   // x_i - x_j
+        const float dyi = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+        float off = 0.0f;
+        if (ti == BS_TID_FLUID) {
+            const float4 aj4 = __ldg(D.qrec_a + j);
+            const float lamp = (freei && tj == BS_TID_FLUID) ? (1.0f + aj4.z * lampf) : 1.0f;
+            const float pvol = aj4.y;
+            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float t12 = 2.0f * pvol * (Lx * dxi + Ly * dyi) * pd;
+            off = -t12;
+            dia.add(t12 * lamp);
+            float ax, ay;
+            if (tj == BS_TID_FLUID) {
+                const float aj = aj4.x;
+                const float rho_ij = 2.0f * aj * ai / (aj + ai);
+                const float4 uj = __ldg(D.qrec_u + j);
+                ax = rho_ij * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
+                ay = rho_ij * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
+            } else {
+                const float4 vj = __ldg(D.qrec_v + j);
+                ax = bi * pos_diff(vj.x, vj.y, vi.x, vi.y).x;
+                ay = bi * pos_diff(vj.z, vj.w, vi.z, vi.w).x;
+            }
+            fv.add(pvol * (ax * Lx + ay * Ly));
+        } else if (ti == BS_TID_GHOST) {
+            if (tj <= 2) {
+                const float t12 = 2.0f * __ldg(D.qrec_a + j).y * (z1 * dxi + z2 * dyi) * pd;
+                off = -t12;
+                dia.add(t12);
+            }
+        } else if (ti == BS_TID_WALL) {
+            if (tj == BS_TID_FLUID) {
+                const float d0 = (float)D.c0[j], d1 = (float)D.c1[j], d2 = (float)D.c2[j], d3 = (float)D.c3[j];
+                const float Lx = d0 * z1 + d1 * z2, Ly = d2 * z1 + d3 * z2;
+                const float t12 = 2.0f * voli * (Lx * dxi + Ly * dyi) * pd;
+                off = -t12;
+                dia.add(t12);
+                // a_j (u_j/phi_j - vxs_i/phi_i): vxs_i/phi_i is the row's own u/phi
+                const float aj = __ldg(D.qrec_a + j).x;
+                const float4 uj = __ldg(D.qrec_u + j);
+                const float ax = aj * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
+                const float ay = aj * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
+                fv.add(voli * (ax * Lx + ay * Ly));
+            } else {
+                const float t12 = 2.0f * __ldg(D.qrec_a + j).y * (z1 * dxi + z2 * dyi) * pd;
+                off = -t12;
+                dia.add(t12);
+            }
+        }
+        a32[e] = off;   // unscaled, scaled below
+    }
+    double extra = 0.0;
+    if (ti == BS_TID_GHOST && n > 0) {
+        const int j0 = D.nidx[ell(r, 0, kmax)];
+        if (j0 < r && D.tid[j0] == BS_TID_FLUID) extra = 1.0;
+    }
+    const double dd = dia.value();
+    if (!(dd != 0.0) || !isfinite(dd)) set_err(D, R.s, BS_ERR_ZERO_DIAG);
+    const double inv = fast_rcp64(dd);
+    D.adiag[r] = dd / dd + extra * inv;
+    D.rhs[r] = fv.value() * fast_rcp64(D.dyn[R.s].dt) * inv;
+    // Jacobi scaling: FP64 values for the FP64 residuals, and the
+    // double-float split off * (inv hi + inv lo) for the solver's SpMV
+    const float2 invd = f2_split(inv);
+    double* a = (double*)D.aval;
+    for (int k = 0; k < n; ++k) {
+        const long e = ell(r, k, kmax);
+        const float o = a32[e];
+        const float ph = __fmul_rn(o, invd.x);
+        const float2 v = f2_fast_two_sum(ph, __fmaf_rn(o, invd.y, __fmaf_rn(o, invd.x, -ph)));
+        a32[e] = v.x;
+        D.aval_lo[e] = v.y;
+        a[e] = (double)o * inv;
+    }
+    if (r == P.row0) D.dyn[R.s].asm_split = 1;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
+    if (sizeof(T) == 4) {
+        assemble_mixed(D, R);
+        return;
+    }
     const ScenePar& P = D.par[R.s];
     const int r = R.r;
     const int ti = D.tid[r];
