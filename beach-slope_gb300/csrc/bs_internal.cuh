@@ -131,7 +131,8 @@ struct Dev {
     // particle fields (current buffer)
     double *x, *y, *xs, *ys, *vx, *vy, *vxs, *vys, *p, *mass, *rho, *oden, *ovol, *con;
     float *xr, *yr;                 // position relative to the row's cell corner (xleft, ybot), FP32
-    float4* pos4;                   // mixed: position as (x hi, x lo, y hi, y lo) FP32 pairs (pos_split)
+    float4* pos4;                   // mixed: position as (x hi, x lo, y hi, y lo) FP32 pairs (pos_split),
+                                    // written by k_relpos and by the packs of the sweeps that read it (k_quot)
     double *vol, *nu;               // derived: m/rho, vis(oden)/oden
     int8_t* tid;
     uint8_t* flags;
@@ -151,10 +152,10 @@ struct Dev {
     double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
     double *tden, *whyd;            // WCSPH: continuity density, hydrostatic Tait density per row
     double *qa, *qu, *qw, *qi;      // per-row quotients of the sweeps (k_quot): rho/phi, u/phi, w/phi, 1/phi
-    // mixed: what a neighbour reads of a row in the assembly, packed by
-    // k_quot: (u/phi, w/phi) and (vxs, vys) as (hi, lo) FP32 pairs (their
-    // differences cancel), (rho/phi, m/rho, oden, 0) in FP32
-    float4 *qrec_u, *qrec_v, *qrec_a;
+    // mixed: what a neighbour sweep reads of a row's neighbours, packed per
+    // row by k_quot right before the sweep (the layout of each sweep is at
+    // k_quot); fields whose pair differences cancel as (hi, lo) FP32 pairs
+    float4 *rec0, *rec1, *rec2;
     double *con_new;
     // neighbour lists (ELL)
     int* ncount;

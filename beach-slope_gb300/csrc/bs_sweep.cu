@@ -382,7 +382,24 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
     T t1 = 0, t2 = 0, t3 = 0;
     const int n = D.ncount[r];
     const int kmax = D.kmax;
-    for (int k = 0; k < n; ++k) {
+    if (sizeof(T) == 4) {
+        // mixed: the neighbours' u/phi, w/phi as (hi, lo) pairs and volumes
+        // from the k_quot records, the differences rounded once to FP32
+        const float4 q4 = D.rec0[r];
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, kmax);
+            const int j = D.nidx[e];
+            const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
+            const float4 qj = __ldg(D.rec0 + j);
+            const float a = pos_diff(qj.x, qj.y, q4.x, q4.y).x, b = pos_diff(qj.z, qj.w, q4.z, q4.w).x;
+            const float V = __ldg(D.rec1 + j).x;
+            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            t1 += V * a * Lx;
+            t2 += V * b * Ly;
+            t3 += 0.5f * V * (a * Ly + b * Lx);
+        }
+    }
+    for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
         const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
@@ -445,7 +462,59 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
     const int n = D.ncount[r];
     const int kmax = D.kmax;
     const T two3 = (T)(2.0 / 3);
-    for (int k = 0; k < n; ++k) {
+    double sxd = 0.0, syd = 0.0;   // the sums as the final update reads them
+    if (sizeof(T) == 4) {
+        // mixed: everything a pair reads of its neighbour from the k_quot
+        // records (positions, velocities and tke as (hi, lo) pairs, the
+        // viscosities, volume and varts in FP32, nut < 1e-6 as a flag), on
+        // the FP32 pipe with compensated sums
+        const float4 pi4 = D.pos4[r], vi4 = D.rec0[r], ki4 = D.rec1[r];
+        const float nuif = ki4.w, nutif = ki4.z, vartsif = D.rec2[r].y;
+        const bool nutis = nuti < BS_SP1EM6;
+        const float iwo = (float)(1.0 / P.wo), phif = (float)phi, two3f = (float)(2.0 / 3);
+        Kahan32 kx, ky;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, kmax);
+            const int j = D.nidx[e];
+            const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
+            const float pd = ld<float>(D.nrinv, e);
+            const int tj = D.tid[j];
+            const float4 kj = __ldg(D.rec1 + j), wj = __ldg(D.rec2 + j);
+            float cmu;
+            if (tj == BS_TID_FLUID) {   // harmonic mean
+                const float nuj = kj.w;
+                cmu = 2.0f * nuif * nuj / (nuif + nuj);
+            } else {
+                cmu = nuif;
+            }
+            float vart = 0.0f;
+            if (freei) vart = vartsif;
+            else if (D.flags[j] & BS_FLAG_FREE) vart = bs_Wf(ld<float>(D.ndist, e), P) * wj.y * iwo;
+            const float pvol = wj.x;
+            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float4 pj4 = __ldg(D.pos4 + j), vj4 = __ldg(D.rec0 + j);
+            const float dxi = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dyi = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+            const float gg = 2.0f * pvol * (dxi * Lx + dyi * Ly) * pd;
+            const float ax = pos_diff(vi4.x, vi4.y, vj4.x, vj4.y).x * gg;
+            const float ay = pos_diff(vi4.z, vi4.w, vj4.z, vj4.w).x * gg;
+            kx.add(ax * (cmu + vart));
+            ky.add(ay * (cmu + vart));
+            if (tj > 2) {
+                const float nutj = kj.z;
+                float mix;
+                if (nutis && wj.z != 0.0f) mix = (nutif + nutj) * 0.5f;
+                else mix = (2.0f * nutif * nutj) / (nutif + nutj);
+                kx.add(ax * mix);
+                ky.add(ay * mix);
+            }
+            const float tk = pvol * pos_diff(kj.x, kj.y, ki4.x, ki4.y).x;
+            kx.add(-(tk * Lx * phif * two3f));
+            ky.add(-(tk * Ly * phif * two3f));
+        }
+        sxd = kx.value();
+        syd = ky.value();
+    }
+    for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
         const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
@@ -480,56 +549,100 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
         sx -= tk * Lx * (T)phi * two3;
         sy -= tk * Ly * (T)phi * two3;
     }
-    double vxs = (vxi + (dt * (double)sx)) / (1.0 - dt * D.resx[r] * phi);
-    double vys = (vyi + dt * ((double)sy)) / (1.0 - dt * D.resy[r] * phi);
+    if (sizeof(T) != 4) {
+        sxd = (double)sx;
+        syd = (double)sy;
+    }
+    double vxs = (vxi + (dt * sxd)) / (1.0 - dt * D.resx[r] * phi);
+    double vys = (vyi + dt * syd) / (1.0 - dt * D.resy[r] * phi);
     vys = vys + P.g * phi * dt;
     D.vxs[r] = vxs;
     D.vys[r] = vys;
 }
 
 // ------------------------------------------------------------- assembly
-// ppesolve, isph.f90:136-444: rows in the neighbour-list order (ascending
-// row = matid, so already column-sorted as after qsort), Jacobi-scaled.
 // Per-particle quotients of the neighbour sweeps (FP64 division is the
 // costly operation on this part; one division per particle instead of one
-// or more per pair).  mode 0 (assembly): qa = rho/phi, qu = vxs/phi,
-// qw = vys/phi, qi = 1/phi; mode 1 (eddyvis): qu = vx/phi, qw = vy/phi;
-// mode 2 (comp_vel): qa = rho/phi.
+// or more per pair) and, in the mixed form, the records the sweep reads of
+// a row's neighbours: each field converted to FP32 once per row instead of
+// once per pair, a field whose pair differences cancel as a (hi, lo) FP32
+// pair (the difference of two pairs rounds to the FP32 rounding of the FP64
+// difference), a threshold test on a neighbour's value as a flag taken on
+// the FP64 value.  Launched by the sweep's wrapper right before the sweep.
+//   mode 0 (assembly): qa = rho/phi, qu = vxs/phi, qw = vys/phi, qi = 1/phi;
+//     rec0 = (qu, qw) pairs, rec1 = (vxs, vys) pairs, rec2 = (qa, m/rho, oden, 0)
+//   mode 1 (eddyvis): qu = vx/phi, qw = vy/phi; rec0 = (qu, qw) pairs, rec1.x = m/rho
+//   mode 2 (comp_vel): qa = rho/phi; rec0 = (p, qa, m/rho, 0)
+//   mode 3 (int_vel, mixed only): rec0 = (vx, vy) pairs, rec1 = (tke pair, nut, nu),
+//     rec2 = (m/rho, varts, nut < 1e-6, 0)
+//   mode 4 (scalar sub-step, mixed only): rec0 = (Dp0, Dp1, Dp2, Dp3),
+//     rec1 = (Dt, con, phi, (phi < 0.7) + 2 (nut < 1e-6))
+//   mode 5 (opt2_shift, mixed only): rec0 = (vx, vy) pairs, rec1.x = m/rho
+// Modes 0, 3 and 4 also refresh the double-float positions.
 __global__ void k_quot(Dev D, int mode) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
     const int r = R.r;
     const double phi = D.por[r];
-    if (mode == 1) {
-        D.qu[r] = D.vx[r] / phi;
-        D.qw[r] = D.vy[r] / phi;
-        return;
+    const bool mixed = D.par[R.s].precision == BS_PREC_MIXED;
+    if (mixed && (mode == 0 || mode == 3 || mode == 4)) D.pos4[r] = pos_split(D.x[r], D.y[r]);
+    switch (mode) {
+    case 0: {
+        const double ip = 1.0 / phi;
+        const double qa = D.rho[r] * ip, qu = D.vxs[r] * ip, qw = D.vys[r] * ip;
+        D.qa[r] = qa;
+        D.qu[r] = qu;
+        D.qw[r] = qw;
+        D.qi[r] = ip;
+        if (mixed) {
+            D.rec0[r] = pos_split(qu, qw);
+            D.rec1[r] = pos_split(D.vxs[r], D.vys[r]);
+            D.rec2[r] = make_float4((float)qa, (float)D.vol[r], (float)D.oden[r], 0.0f);
+        }
+        break;
     }
-    if (mode == 2) {
-        D.qa[r] = D.rho[r] / phi;
-        return;
+    case 1: {
+        const double qu = D.vx[r] / phi, qw = D.vy[r] / phi;
+        D.qu[r] = qu;
+        D.qw[r] = qw;
+        if (mixed) {
+            D.rec0[r] = pos_split(qu, qw);
+            D.rec1[r] = make_float4((float)D.vol[r], 0.0f, 0.0f, 0.0f);
+        }
+        break;
     }
-    const double ip = 1.0 / phi;
-    const double qa = D.rho[r] * ip, qu = D.vxs[r] * ip, qw = D.vys[r] * ip;
-    D.qa[r] = qa;
-    D.qu[r] = qu;
-    D.qw[r] = qw;
-    D.qi[r] = ip;
-    if (D.par[R.s].precision == BS_PREC_MIXED) {
-        D.qrec_u[r] = pos_split(qu, qw);
-        D.qrec_v[r] = pos_split(D.vxs[r], D.vys[r]);
-        D.qrec_a[r] = make_float4((float)qa, (float)D.vol[r], (float)D.oden[r], 0.0f);
+    case 2: {
+        const double qa = D.rho[r] / phi;
+        D.qa[r] = qa;
+        if (mixed) D.rec0[r] = make_float4((float)D.p[r], (float)qa, (float)D.vol[r], 0.0f);
+        break;
+    }
+    case 3: {
+        const double nut = D.nut[r];
+        D.rec0[r] = pos_split(D.vx[r], D.vy[r]);
+        const float2 tk = f2_split(D.tke[r]);
+        D.rec1[r] = make_float4(tk.x, tk.y, (float)nut, (float)D.nu[r]);
+        D.rec2[r] = make_float4((float)D.vol[r], (float)D.varts[r], nut < BS_SP1EM6 ? 1.0f : 0.0f, 0.0f);
+        break;
+    }
+    case 4: {
+        D.rec0[r] = make_float4((float)D.Dp0[r], (float)D.Dp1[r], (float)D.Dp2[r], (float)D.Dp3[r]);
+        const float bits = (phi < 0.7 ? 1.0f : 0.0f) + (D.nut[r] < BS_SP1EM6 ? 2.0f : 0.0f);
+        D.rec1[r] = make_float4((float)D.Dt[r], (float)D.con[r], (float)phi, bits);
+        break;
+    }
+    case 5: {
+        D.rec0[r] = pos_split(D.vx[r], D.vy[r]);
+        D.rec1[r] = make_float4((float)D.vol[r], 0.0f, 0.0f, 0.0f);
+        break;
+    }
     }
 }
 
-// ppesolve assembly (isph.f90:115-456) with the quotients of k_quot:
-// rho_ij = 2 a_j a_i / (a_j + a_i) with a = rho/phi, the velocity terms as
-// rho_ij (vxs_j/phi_j - vxs_i/phi_i) -- the reference's expressions
-// regrouped, one division per fluid pair
 // The mixed form of the assembly: the same entries and right-hand side on
 // the FP32 pipe.  Pair offsets and the cancelling differences (u/phi, w/phi,
-// vxs, vys of the pair) are taken from double-float copies (pos4, qrec_u,
-// qrec_v: the FP32 rounding of the FP64 difference), the products in FP32,
+// vxs, vys of the pair) are taken from double-float copies (pos4 and the
+// k_quot records: the FP32 rounding of the FP64 difference), the products in FP32,
 // the diagonal and the right-hand side as compensated sums; the Jacobi
 // scaling writes the FP64 values and their double-float split (aval32 +
 // aval_lo) for the solver.
@@ -539,8 +652,8 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
     const int ti = D.tid[r];
     const uint8_t fl = D.flags[r];
     const float4 pi4 = D.pos4[r];
-    const float4 ui = D.qrec_u[r], vi = D.qrec_v[r];
-    const float ai = D.qrec_a[r].x;                       // rho_i/phi_i
+    const float4 ui = D.rec0[r], vi = D.rec1[r];
+    const float ai = D.rec2[r].x;                       // rho_i/phi_i
     const float bi = (float)(D.qa[r] * D.qi[r]);          // rho_i/phi_i^2
     const float c0 = (float)D.c0[r], c1 = (float)D.c1[r], c2 = (float)D.c2[r], c3 = (float)D.c3[r];
     const bool freei = fl & BS_FLAG_FREE;
@@ -561,7 +674,7 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
         const float dyi = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
         float off = 0.0f;
         if (ti == BS_TID_FLUID) {
-            const float4 aj4 = __ldg(D.qrec_a + j);
+            const float4 aj4 = __ldg(D.rec2 + j);
             const float lamp = (freei && tj == BS_TID_FLUID) ? (1.0f + aj4.z * lampf) : 1.0f;
             const float pvol = aj4.y;
             const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
@@ -572,18 +685,18 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
             if (tj == BS_TID_FLUID) {
                 const float aj = aj4.x;
                 const float rho_ij = 2.0f * aj * ai / (aj + ai);
-                const float4 uj = __ldg(D.qrec_u + j);
+                const float4 uj = __ldg(D.rec0 + j);
                 ax = rho_ij * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
                 ay = rho_ij * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
             } else {
-                const float4 vj = __ldg(D.qrec_v + j);
+                const float4 vj = __ldg(D.rec1 + j);
                 ax = bi * pos_diff(vj.x, vj.y, vi.x, vi.y).x;
                 ay = bi * pos_diff(vj.z, vj.w, vi.z, vi.w).x;
             }
             fv.add(pvol * (ax * Lx + ay * Ly));
         } else if (ti == BS_TID_GHOST) {
             if (tj <= 2) {
-                const float t12 = 2.0f * __ldg(D.qrec_a + j).y * (z1 * dxi + z2 * dyi) * pd;
+                const float t12 = 2.0f * __ldg(D.rec2 + j).y * (z1 * dxi + z2 * dyi) * pd;
                 off = -t12;
                 dia.add(t12);
             }
@@ -595,13 +708,13 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
                 off = -t12;
                 dia.add(t12);
                 // a_j (u_j/phi_j - vxs_i/phi_i): vxs_i/phi_i is the row's own u/phi
-                const float aj = __ldg(D.qrec_a + j).x;
-                const float4 uj = __ldg(D.qrec_u + j);
+                const float aj = __ldg(D.rec2 + j).x;
+                const float4 uj = __ldg(D.rec0 + j);
                 const float ax = aj * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
                 const float ay = aj * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
                 fv.add(voli * (ax * Lx + ay * Ly));
             } else {
-                const float t12 = 2.0f * __ldg(D.qrec_a + j).y * (z1 * dxi + z2 * dyi) * pd;
+                const float t12 = 2.0f * __ldg(D.rec2 + j).y * (z1 * dxi + z2 * dyi) * pd;
                 off = -t12;
                 dia.add(t12);
             }
@@ -634,6 +747,10 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
     if (r == P.row0) D.dyn[R.s].asm_split = 1;
 }
 
+// ppesolve assembly (isph.f90:115-456) with the quotients of k_quot:
+// rho_ij = 2 a_j a_i / (a_j + a_i) with a = rho/phi, the velocity terms as
+// rho_ij (vxs_j/phi_j - vxs_i/phi_i) -- the reference's expressions
+// regrouped, one division per fluid pair
 template <typename T>
 __global__ void __launch_bounds__(BS_THREADS) k_assemble(Dev D) {
     const RowCtx R = row_ctx(D);
@@ -753,7 +870,30 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
             T ax = 0, ay = 0;
             const int n = D.ncount[r];
             const int kmax = D.kmax;
-            for (int k = 0; k < n; ++k) {
+            double axd = 0.0, ayd = 0.0;
+            if (sizeof(T) == 4) {
+                // mixed: p, rho/phi and the volume of the neighbours from the
+                // k_quot records, the pair terms on the FP32 pipe, the
+                // pressure-gradient sums (which cancel) compensated
+                const float pif = (float)pi, aif = (float)ai, qff = (float)qf, phi2f = (float)(phi * phi);
+                const float rhoif = (float)rhoi;
+                Kahan32 kx, ky;
+                for (int k = 0; k < n; ++k) {
+                    const long e = ell(r, k, kmax);
+                    const int j = D.nidx[e];
+                    const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
+                    const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+                    const float4 qj = __ldg(D.rec0 + j);   // (p, rho/phi, m/rho)
+                    float q;
+                    if (D.tid[j] == BS_TID_FLUID) q = qff * qj.z * (qj.x * aif + pif * qj.y) / (aif + qj.y);
+                    else q = qj.z * phi2f * (qj.x + pif) / rhoif;
+                    kx.add(-(q * Lx));
+                    ky.add(-(q * Ly));
+                }
+                axd = kx.value();
+                ayd = ky.value();
+            }
+            for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
                 const long e = ell(r, k, kmax);
                 const int j = D.nidx[e];
                 const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
@@ -770,8 +910,12 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
                 ax -= q * Lx;
                 ay -= q * Ly;
             }
-            vx = D.vxs[r] + (double)ax * dt;
-            vy = D.vys[r] + (double)ay * dt;
+            if (sizeof(T) != 4) {
+                axd = (double)ax;
+                ayd = (double)ay;
+            }
+            vx = D.vxs[r] + axd * dt;
+            vy = D.vys[r] + ayd * dt;
             vel = sqrt(vx * vx + vy * vy) / phi;
             D.vx[r] = vx;
             D.vy[r] = vy;
@@ -790,7 +934,6 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
         const double yn = __ddiv_rn(__dadd_rn(__dadd_rn(y, D.ys[r]), __ddiv_rn(__dmul_rn(dt, vy), phi)), 2.0);
         D.x[r] = xn;
         D.y[r] = yn;
-        if (sizeof(T) == 4) D.pos4[r] = pos_split(xn, yn);
         // buffer release (integrator.f90:865-872)
         const ScenePar& P = D.par[R.s];
         if ((fl & BS_FLAG_BUFFER) && (xn > P.buf_lo) && (xn < P.buf_hi)) D.flags[r] = fl & ~BS_FLAG_BUFFER;
@@ -818,7 +961,27 @@ __global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
     const double vxi = D.vx[r], vyi = D.vy[r];
     T sxs = 0, sys = 0, a1 = 0, a2 = 0, b1 = 0, b2 = 0;
     const int kmax = D.kmax;
-    for (int k = 0; k < n; ++k) {
+    if (sizeof(T) == 4) {
+        // mixed: the neighbours' velocities as (hi, lo) pairs and volumes
+        // from the k_quot records, the differences rounded once to FP32
+        const float4 vi4 = D.rec0[r];
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, kmax);
+            const int j = D.nidx[e];
+            const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
+            const float V = __ldg(D.rec1 + j).x;
+            sxs += z1 * V;
+            sys += z2 * V;
+            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float4 vj4 = __ldg(D.rec0 + j);
+            const float du = pos_diff(vj4.x, vj4.y, vi4.x, vi4.y).x, dv = pos_diff(vj4.z, vj4.w, vi4.z, vi4.w).x;
+            a1 += Lx * du * V;
+            a2 += Ly * du * V;
+            b1 += Lx * dv * V;
+            b2 += Ly * dv * V;
+        }
+    }
+    for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
         const T z1 = ld<T>(D.nkx, e), z2 = ld<T>(D.nky, e);
@@ -863,7 +1026,6 @@ __global__ void k_apply_density(Dev D, int do_apply, int do_density) {
         const double x = __dadd_rn(D.x[r], D.xs[r]), y = __dadd_rn(D.y[r], D.ys[r]);
         D.x[r] = x;
         D.y[r] = y;
-        if (P.precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
         D.vx[r] = D.vx[r] + D.vxs[r];
         D.vy[r] = D.vy[r] + D.vys[r];
     }
@@ -939,37 +1101,43 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep, const
     const int n = D.ncount[r];
     const int kmax = D.kmax;
     if (sizeof(T) == 4) {
-        // mixed: the pair terms in FP32 from the FP32-stored pair data (the
-        // porosity thresholds on the FP64 values), summed in FP32
+        // mixed: the pair terms in FP32 from the FP32-stored pair data and the
+        // k_quot records (dispersion tensor, Dt, con, phi; the porosity and
+        // eddy-viscosity thresholds as flags taken on the FP64 values; the
+        // pair offset from the double-float positions), summed in FP32
         const float capf = (float)cap, ovf = (float)ovoli, phif = (float)phii, cof = (float)coni;
         const float P0 = (float)Pi0, P1 = (float)Pi1, P2 = (float)Pi2, P3 = (float)Pi3, Dtf = (float)Dti;
-        const bool nsmall = nuti < BS_SP1EM6;
+        const bool nsmall = nuti < BS_SP1EM6, psmall = phii < thr;
+        const float4 pi4 = D.pos4[r];
         float cdf = 0.0f;
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
             const int j = D.nidx[e];
             if (D.tid[j] != BS_TID_FLUID) continue;
-            const double phij = D.por[j];
-            const float pj = (float)phij;
-            const float dm = (float)ld<T>(D.ndist, e);
-            const float dx = (float)(xi - D.x[j]), dy = (float)(yi - D.y[j]);
+            const float4 sj = __ldg(D.rec1 + j);   // (Dt, con, phi, flags)
+            const int bits = (int)sj.w;
+            const float pj = sj.z;
+            const float dm = ld<float>(D.ndist, e);
+            const float4 pj4 = __ldg(D.pos4 + j);
+            const float dx = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dy = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
             float t1x;
-            if ((phii < thr) && (phij < thr)) {
-                const float Dxx = P0 + (float)D.Dp0[j], Dxy = P1 + (float)D.Dp1[j];
-                const float Dyx = P2 + (float)D.Dp2[j], Dyy = P3 + (float)D.Dp3[j];
+            if (psmall && (bits & 1)) {
+                const float4 dj = __ldg(D.rec0 + j);
+                const float Dxx = P0 + dj.x, Dxy = P1 + dj.y;
+                const float Dyx = P2 + dj.z, Dyy = P3 + dj.w;
                 const float ph = 0.5f / dm;
                 const float A = Dxx * dx * ph + Dxy * dy * ph, B = Dyx * dx * ph + Dyy * dy * ph;
                 t1x = 1.0f / (A * A + B * B);
                 t1x = (t1x <= capf) ? t1x : capf;
             } else {
-                const float Dj = (float)D.Dt[j];
-                if (nsmall && (D.nut[j] < BS_SP1EM6)) t1x = (Dtf + Dj) * 0.5f;
+                const float Dj = sj.x;
+                if (nsmall && (bits & 2)) t1x = (Dtf + Dj) * 0.5f;
                 else t1x = 2.0f * Dtf * Dj / (Dtf + Dj);
             }
             const float t3 = ovf * (phif + pj) / (phif * pj);
             const float F = bs_Ff(dm, P);
-            const float pd = (float)ld<T>(D.nrinv, e);
-            const float dc = cof - (float)D.con[j];
+            const float pd = ld<float>(D.nrinv, e);
+            const float dc = cof - sj.y;
             cdf += t1x * t3 * dc * (dx * (F * dx) + dy * (F * dy)) * pd;
         }
         cd = cdf;
@@ -1233,7 +1401,6 @@ __global__ void __launch_bounds__(BS_THREADS) k_coll_apply(Dev D, int mode) {
             const double x = __dadd_rn(D.x[r], D.xs[r]), y = __dadd_rn(D.y[r], D.ys[r]);
             D.x[r] = x;
             D.y[r] = y;
-            if (D.par[R.s].precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
         }
     } else {
         D.vx[r] = __dadd_rn(D.vx[r], __dmul_rn(D.vxs[r], D.por[r]));
@@ -1350,7 +1517,10 @@ void eddy(const Dev& D, const Launch& L, int precision, int with_eddy, int with_
     BS_PLAIN(K_EDDY, k_quot, D, 1);
     BS_DISPATCH(K_EDDY, precision, k_eddy, D, with_eddy, with_varts, with_disp);
 }
-void int_vel(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_INTVEL, precision, k_intvel, D); }
+void int_vel(const Dev& D, const Launch& L, int precision) {
+    if (precision == BS_PREC_MIXED) BS_PLAIN(K_INTVEL, k_quot, D, 3);
+    BS_DISPATCH(K_INTVEL, precision, k_intvel, D);
+}
 void assemble(const Dev& D, const Launch& L, int precision) {
     BS_PLAIN(K_ASSEMBLE, k_quot, D, 0);
     BS_DISPATCH(K_ASSEMBLE, precision, k_assemble, D);
@@ -1359,13 +1529,17 @@ void comp_vel(const Dev& D, const Launch& L, int precision, int do_vel, int do_p
     if (do_vel) BS_PLAIN(K_COMPVEL, k_quot, D, 2);
     BS_DISPATCH(K_COMPVEL, precision, k_compvel, D, do_vel, do_pos);
 }
-void shift(const Dev& D, const Launch& L, int precision) { BS_DISPATCH(K_SHIFT, precision, k_shift, D); }
+void shift(const Dev& D, const Launch& L, int precision) {
+    if (precision == BS_PREC_MIXED) BS_PLAIN(K_SHIFT, k_quot, D, 5);
+    BS_DISPATCH(K_SHIFT, precision, k_shift, D);
+}
 void apply_density(const Dev& D, const Launch& L, int do_apply, int do_density) {
     BS_PLAIN(K_APPLY, k_apply_density, D, do_apply, do_density);
 }
 void disp(const Dev& D, const Launch& L) { BS_PLAIN(K_DISP, k_disp, D); }
 void velmag(const Dev& D, const Launch& L) { BS_PLAIN(K_VELMAG, k_velmag, D); }
 void scalar(const Dev& D, const Launch& L, int precision, int substep, const int* jdev) {
+    if (precision == BS_PREC_MIXED) BS_PLAIN(K_SCALAR, k_quot, D, 4);
     BS_DISPATCH(K_SCALAR, precision, k_scalar, D, substep, jdev);
 }
 void wc_continuity(const Dev& D, const Launch& L, int precision) {
