@@ -10,8 +10,9 @@
 // (destination cell, arrival category) over rows that are already sorted by
 // source cell, so a counting sort over BS_NCAT buckets per cell reproduces
 // it exactly:  k_rank (one warp per source cell: codes + ballot ranks +
-// bucket counts) -> k_cell_prefix (per cell: prefix over its buckets) ->
-// k_scan_cells (per scene: exclusive scan of cell totals) -> k_permute.
+// bucket counts) -> k_scan_part (per cell: prefix over its buckets; per
+// chunk of cells: the total) -> k_scan_apply (per scene: exclusive scan of
+// the cell totals) -> k_permute.
 #include "bs_internal.cuh"
 
 namespace {
@@ -118,64 +119,79 @@ __global__ void k_rank(Dev D, int projection, int cutoff) {
     }
 }
 
-__global__ void k_cell_prefix(Dev D) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= D.ncell_total) return;
-    int* b = D.bucket + (long)c * BS_NCAT;
-    int acc = 0;
-#pragma unroll
-    for (int d = 0; d < BS_NCAT; ++d) {
-        const int v = b[d];
-        b[d] = acc;
-        acc += v;
-    }
-    D.cell_total[c] = acc;
-}
-
-// one block per scene: exclusive scan of the scene's cell totals
-// One block per scene (1024 threads): each thread sums a contiguous run of
-// cells, the run totals are scanned across the block (warp shuffles, then
-// the 32 warp totals), and each thread writes its run's ranges -- two passes
-// over the cells instead of a barrier-bound scan per 1024 cells.
-__global__ void k_scan_cells(Dev D) {
-    const int s = blockIdx.x;
+// Per-scene exclusive scan of the cell totals in two passes over chunks of
+// BS_SCAN_CHUNK cells, block (k, s) = chunk k of scene s.  Pass 1: each
+// cell's prefix over its buckets (the rows of each category before it) and
+// its total, and the chunk's total.
+__global__ void __launch_bounds__(BS_SCAN_CHUNK) k_scan_part(Dev D) {
+    const int s = blockIdx.y, k = blockIdx.x;
     const ScenePar& P = D.par[s];
-    __shared__ int wsum[32];
-    __shared__ int total;
-    const int nb = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int per = (P.ncell + nb - 1) / nb;
-    const int q0 = t * per, q1 = min(P.ncell, q0 + per);
-    const int* __restrict__ tot = D.cell_total + P.cell0;
-    int loc = 0;
-    for (int q = q0; q < q1; ++q) loc += tot[q];
-    int inc = loc;   // inclusive scan within the warp
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += v;
+    if (k * BS_SCAN_CHUNK >= P.ncell) return;
+    __shared__ int ws[BS_SCAN_CHUNK / 32];
+    const int q = k * BS_SCAN_CHUNK + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int acc = 0;
+    if (q < P.ncell) {
+        int* b = D.bucket + (long)(P.cell0 + q) * BS_NCAT;
+#pragma unroll
+        for (int d = 0; d < BS_NCAT; ++d) {
+            const int v = b[d];
+            b[d] = acc;
+            acc += v;
+        }
+        D.cell_total[P.cell0 + q] = acc;
     }
-    if (lane == 31) wsum[w] = inc;
+    int v = acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) ws[w] = v;
     __syncthreads();
     if (w == 0) {
-        const int nw = nb >> 5;
-        int x = lane < nw ? wsum[lane] : 0;
+        int a = ws[lane];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) D.scan_part[s * D.scan_chunks + k] = a;
+    }
+}
+
+// Pass 2: the chunk's exclusive scan, offset by the totals of the scene's
+// chunks before it, as the cells' row ranges in the permuted order; the
+// scene's last chunk records the new particle count.
+__global__ void __launch_bounds__(BS_SCAN_CHUNK) k_scan_apply(Dev D) {
+    const int s = blockIdx.y, k = blockIdx.x;
+    const ScenePar& P = D.par[s];
+    if (k * BS_SCAN_CHUNK >= P.ncell) return;
+    __shared__ int ws[BS_SCAN_CHUNK / 32];
+    __shared__ int base;
+    const int q = k * BS_SCAN_CHUNK + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w == 0) {
+        int a = 0;
+        for (int i = lane; i < k; i += 32) a += D.scan_part[s * D.scan_chunks + i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) base = a;
+    }
+    const int v = q < P.ncell ? D.cell_total[P.cell0 + q] : 0;
+    int inc = v;   // inclusive scan within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int x = ws[lane];
         for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += v;
+            const int u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
         }
-        if (lane < nw) wsum[lane] = x;   // inclusive warp prefix
-        if (lane == nw - 1) total = x;
+        ws[lane] = x;   // inclusive warp prefix
     }
     __syncthreads();
-    int run = P.row0 + (w ? wsum[w - 1] : 0) + inc - loc;
-    for (int q = q0; q < q1; ++q) {
-        const int v = tot[q];
-        D.cell_start2[P.cell0 + q] = run;
-        D.cell_end2[P.cell0 + q] = run + v;
-        run += v;
+    if (q < P.ncell) {
+        const int start = P.row0 + base + (w ? ws[w - 1] : 0) + inc - v;
+        D.cell_start2[P.cell0 + q] = start;
+        D.cell_end2[P.cell0 + q] = start + v;
     }
-    if (t == 0) {
+    if (threadIdx.x == 0 && (k + 1) * BS_SCAN_CHUNK >= P.ncell) {
         D.dyn[s].n_prev = D.dyn[s].n;
-        D.dyn[s].n = total;
+        D.dyn[s].n = base + ws[BS_SCAN_CHUNK / 32 - 1];
     }
 }
 
@@ -239,25 +255,57 @@ __global__ void k_cellmax(Dev D, int do_cellmax) {
     }
 }
 
-// one block per scene
+// Per-scene maxima over the interior cells of the cell maxima (k_cellmax)
+// for the timestep rule (integrator.f90:885-953): one thread per cell, a
+// segmented warp maximum over the warp's cells of one scene, one atomic
+// maximum per segment on the bit patterns (non-negative doubles order as
+// unsigned integers).  A value that is not positive counts as 0, as in the
+// rule's running fmax from 0, which passes over NaN.
+__global__ void k_scene_max(Dev D) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int s = -1;
+    unsigned long long v0 = 0ull, v1 = 0ull;
+    if (c < D.ncell_total) {
+        s = D.cell_scene[c];
+        const ScenePar& P = D.par[s];
+        const int lc = c - P.cell0;
+        const int i = lc % P.celly + 1, j = lc / P.celly + 1;
+        if (!D.dyn[s].hold && i >= 2 && i <= P.celly - 1 && j >= 2 && j <= P.cellx - 1) {
+            const double a = D.cell_maxvel[c], b = D.cell_maxeddy[c];
+            v0 = a > 0.0 ? (unsigned long long)__double_as_longlong(a) : 0ull;
+            v1 = b > 0.0 ? (unsigned long long)__double_as_longlong(b) : 0ull;
+        }
+    }
+    for (int o = 1; o < 32; o <<= 1) {   // cells of one scene are contiguous
+        const unsigned long long a = __shfl_down_sync(0xffffffffu, v0, o), b = __shfl_down_sync(0xffffffffu, v1, o);
+        const int so = __shfl_down_sync(0xffffffffu, s, o);
+        if (lane + o < 32 && so == s) {
+            v0 = a > v0 ? a : v0;
+            v1 = b > v1 ? b : v1;
+        }
+    }
+    const int sp = __shfl_up_sync(0xffffffffu, s, 1);
+    if (s >= 0 && (lane == 0 || sp != s)) {
+        if (v0) atomicMax(D.scene_max + 2 * s, v0);
+        if (v1) atomicMax(D.scene_max + 2 * s + 1, v1);
+    }
+}
+
+// the timestep rule per scene from the maxima of k_scene_max (which it
+// clears for the next step)
 __global__ void k_timestep(Dev D) {
-    const int s = blockIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= D.nscene) return;
+    unsigned long long* m = D.scene_max + 2 * s;
+    const double umax = __longlong_as_double((long long)m[0]);
+    double numax = __longlong_as_double((long long)m[1]);
+    m[0] = 0ull;
+    m[1] = 0ull;
     if (D.dyn[s].hold) return;
     const ScenePar& P = D.par[s];
-    __shared__ double sh[2 * 32];
-    double v[2] = {0.0, 0.0};
-    for (int q = threadIdx.x; q < P.ncell; q += blockDim.x) {
-        const int lc = q;
-        const int i = lc % P.celly + 1, j = lc / P.celly + 1;
-        if (i < 2 || i > P.celly - 1 || j < 2 || j > P.cellx - 1) continue;
-        v[0] = fmax(v[0], D.cell_maxvel[P.cell0 + q]);
-        v[1] = fmax(v[1], D.cell_maxeddy[P.cell0 + q]);
-    }
-    block_max<2>(v, sh);
-    if (threadIdx.x == 0) {
+    {
         SceneDyn& Y = D.dyn[s];
-        const double umax = v[0];
-        double numax = v[1];
         Y.umax = umax;
         const double sig1 = P.sig1, dl = P.dl, mu = P.mu, rho = P.rho, t = Y.t;
         double dt = Y.dt;
@@ -443,10 +491,10 @@ void rebin(const Dev& D, const Launch& L, int projection, int cutoff) {
     k_rank<<<gdiv((long)D.ncell_total * 32, BS_THREADS), BS_THREADS, 0, L.stream>>>(D, projection, cutoff);
     tend(L, q);
     q = tbegin(L, K_CELLPREFIX);
-    k_cell_prefix<<<gdiv(D.ncell_total, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
+    k_scan_part<<<dim3(D.scan_chunks, D.nscene), BS_SCAN_CHUNK, 0, L.stream>>>(D);
     tend(L, q);
     q = tbegin(L, K_SCANCELLS);
-    k_scan_cells<<<D.nscene, 1024, 0, L.stream>>>(D);
+    k_scan_apply<<<dim3(D.scan_chunks, D.nscene), BS_SCAN_CHUNK, 0, L.stream>>>(D);
     tend(L, q);
     q = tbegin(L, K_PERMUTE);
     k_permute<<<L.nblk_rows, BS_THREADS, 0, L.stream>>>(D, projection);
@@ -476,8 +524,11 @@ void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_tim
         tend(L, q);
     }
     if (do_timestep) {
-        const int q = tbegin(L, K_TIMESTEP);
-        k_timestep<<<D.nscene, BS_THREADS, 0, L.stream>>>(D);
+        int q = tbegin(L, K_TIMESTEP);
+        k_scene_max<<<gdiv(D.ncell_total, BS_THREADS), BS_THREADS, 0, L.stream>>>(D);
+        tend(L, q);
+        q = tbegin(L, K_TIMESTEP);
+        k_timestep<<<gdiv(D.nscene, 64), 64, 0, L.stream>>>(D);
         tend(L, q);
     }
 }

@@ -553,7 +553,13 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(sr, R); A(srhat, R); A(sp, R); A(sp2, R); A(sv, R); A(sv2, R); A(ss, R); A(st, R); A(sxd, R);
     A(cell_start, C); A(cell_end, C); A(cell_start2, C); A(cell_end2, C);
     A(bucket, C * BS_NCAT); A(cell_total, C); A(coderank, R);
-    A(cell_maxvel, C); A(cell_maxeddy, C);
+    A(cell_maxvel, C); A(cell_maxeddy, C); A(scene_max, (size_t)2 * nscenes);
+    {
+        int mc = 1;
+        for (const ScenePar& P : ctx->hpar) mc = std::max(mc, (P.ncell + BS_SCAN_CHUNK - 1) / BS_SCAN_CHUNK);
+        D.scan_chunks = mc;
+        A(scan_part, (size_t)mc * nscenes);
+    }
     A(gx, (size_t)gr); A(gy, (size_t)gr); A(gv, (size_t)gr); A(gcell_start, C); A(gcell_end, C);
     A(gxr, (size_t)gr); A(gyr, (size_t)gr); A(gpos4, (size_t)gr); A(xr, R); A(yr, R);
     if (ctx->precision == BS_PREC_MIXED) {

@@ -24,6 +24,7 @@
 #define BS_THREADS 256
 #define BS_NCAT 10      // bucket categories per cell in the re-bin (see k_rank)
 #define BS_MAXDOT 8     // partial sums per block in the solver
+#define BS_SCAN_CHUNK 1024  // cells per block of the re-bin's cell scan
 #define BS_FG_MAXM 150  // longest FGMRES restart cycle (the reference's MKL default)
 
 // constants with the reference's literal precision (default REAL = single)
@@ -194,6 +195,9 @@ struct Dev {
     int* cell_total;                // [ncell_total]
     int* coderank;                  // per row: code<<24 | rank
     double *cell_maxvel, *cell_maxeddy;
+    int* scan_part;                 // per scene x chunk of BS_SCAN_CHUNK cells: the chunk's row total (re-bin scan)
+    int scan_chunks;                // chunks of the scene with the most cells
+    unsigned long long* scene_max;  // per scene: the timestep rule's |vel| and |nut| maxima (bit patterns), k_scene_max
     // grains (static, sorted by cell)
     double *gx, *gy, *gv;           // gv = mass/density
     float *gxr, *gyr;               // grain position relative to its cell corner, FP32
@@ -240,10 +244,25 @@ __device__ __forceinline__ double bs_W(double r, const ScenePar& P) {
     return P.cn1 * t1 + P.cn2 * t2;
 }
 
-__device__ __forceinline__ float bs_Wf(float r, const ScenePar& P) {
-    const float q = r * (float)P.inv_h;
+// The kernel's constants in FP32, converted once per row (a conversion from
+// FP64 issues on the FP64 pipe)
+struct KerF {
+    float h, ih, ih2, ih3, c1, c2;
+};
+__device__ __forceinline__ KerF ker_f(const ScenePar& P) {
+    KerF K;
+    K.h = (float)P.h;
+    K.ih = (float)P.inv_h;
+    K.ih2 = (float)P.inv_h2;
+    K.ih3 = (float)P.inv_h3;
+    K.c1 = (float)P.cn1;
+    K.c2 = (float)P.cn2;
+    return K;
+}
+__device__ __forceinline__ float bs_Wf(float r, const KerF& K) {
+    const float q = r * K.ih;
     float t1, t2;
-    if (r < (float)P.h) {
+    if (r < K.h) {
         t1 = 4.0f - 6.0f * q * q + 3.0f * q * q * q;
         t2 = q * q * q - 6.0f * q + 6.0f;
     } else {
@@ -251,7 +270,7 @@ __device__ __forceinline__ float bs_Wf(float r, const ScenePar& P) {
         t1 = a * a * a;
         t2 = t1;
     }
-    return (float)P.cn1 * t1 + (float)P.cn2 * t2;
+    return K.c1 * t1 + K.c2 * t2;
 }
 
 // r = sqrt(s) and 1/r in FP64 from an FP32 rsqrt seed and one Newton step
@@ -375,17 +394,15 @@ __device__ __forceinline__ double bs_F(double r, const ScenePar& P) {
     const double c = (3.0 * P.inv_h / r) * a * a;
     return -(P.cn1 + P.cn2) * c;
 }
-__device__ __forceinline__ float bs_Ff(float r, const ScenePar& P) {
-    const float ih = (float)P.inv_h, ih2 = (float)P.inv_h2, ih3 = (float)P.inv_h3;
-    const float c1 = (float)P.cn1, c2 = (float)P.cn2;
-    if (r < (float)P.h) {
-        const float t1 = 9.0f * r * ih3 - 12.0f * ih2;
-        const float t2 = 3.0f * r * ih3 - 6.0f * ih / r;
-        return c1 * t1 + c2 * t2;
+__device__ __forceinline__ float bs_Ff(float r, const KerF& K) {
+    if (r < K.h) {
+        const float t1 = 9.0f * r * K.ih3 - 12.0f * K.ih2;
+        const float t2 = 3.0f * r * K.ih3 - 6.0f * K.ih / r;
+        return K.c1 * t1 + K.c2 * t2;
     }
-    const float a = 2.0f - r * ih;
-    const float c = (3.0f * ih / r) * a * a;
-    return -(c1 + c2) * c;
+    const float a = 2.0f - r * K.ih;
+    const float c = (3.0f * K.ih / r) * a * a;
+    return -(K.c1 + K.c2) * c;
 }
 
 // viscosity (integrator.f90:12-30)

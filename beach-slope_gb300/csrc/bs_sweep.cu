@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 const double wsolid = 1.0 - P.por * 1.0;
                 const float wsf = (float)wsolid, t2c = (float)(P.twoh * P.twoh);
                 Kahan32 sff;
+                const KerF KF = ker_f(P);
                 const float t2f = (float)(P.twoh * P.twoh) * (1.0f + 1e-5f);
                 const float xri = D.xr[r], yri = D.yr[r];
                 float4 pi4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                                     ir = ir * (1.5f - 0.5f * s2 * ir * ir);
                                     rad = s2 * ir;
                                 }
-                                sff.add(wsf * bs_Wf(rad, P) * (float)D.gv[g]);
+                                sff.add(wsf * bs_Wf(rad, KF) * (float)D.gv[g]);
                             }
                         } else {
                             const double dx = xi - D.gx[g], dy = yi - D.gy[g];
@@ -472,6 +473,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
         const float nuif = ki4.w, nutif = ki4.z, vartsif = D.rec2[r].y;
         const bool nutis = nuti < BS_SP1EM6;
         const float iwo = (float)(1.0 / P.wo), phif = (float)phi, two3f = (float)(2.0 / 3);
+        const KerF KF = ker_f(P);
         Kahan32 kx, ky;
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
@@ -489,7 +491,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
             }
             float vart = 0.0f;
             if (freei) vart = vartsif;
-            else if (D.flags[j] & BS_FLAG_FREE) vart = bs_Wf(ld<float>(D.ndist, e), P) * wj.y * iwo;
+            else if (D.flags[j] & BS_FLAG_FREE) vart = bs_Wf(ld<float>(D.ndist, e), KF) * wj.y * iwo;
             const float pvol = wj.x;
             const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
             const float4 pj4 = __ldg(D.pos4 + j), vj4 = __ldg(D.rec0 + j);
@@ -1109,6 +1111,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep, const
         const float P0 = (float)Pi0, P1 = (float)Pi1, P2 = (float)Pi2, P3 = (float)Pi3, Dtf = (float)Dti;
         const bool nsmall = nuti < BS_SP1EM6, psmall = phii < thr;
         const float4 pi4 = D.pos4[r];
+        const KerF KF = ker_f(P);
         float cdf = 0.0f;
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
@@ -1135,7 +1138,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep, const
                 else t1x = 2.0f * Dtf * Dj / (Dtf + Dj);
             }
             const float t3 = ovf * (phif + pj) / (phif * pj);
-            const float F = bs_Ff(dm, P);
+            const float F = bs_Ff(dm, KF);
             const float pd = ld<float>(D.nrinv, e);
             const float dc = cof - sj.y;
             cdf += t1x * t3 * dc * (dx * (F * dx) + dy * (F * dy)) * pd;
