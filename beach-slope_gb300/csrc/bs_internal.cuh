@@ -467,7 +467,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_MG_SUB, K_COLL, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_MG_SUB, K_COLL, K_MG_L0REST, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {

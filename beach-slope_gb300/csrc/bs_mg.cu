@@ -196,44 +196,54 @@ __device__ __forceinline__ T ell_dot(const T* __restrict__ A, const int* __restr
     return acc;
 }
 
+// Level 0, pass 1: the residual after the pre-sweep from zero, v = xin - A u
+// (u = omega xin / adiag, written with the input), one thread per row on the
+// aligned row blocks (coalesced slices of the ELL), into zz (free until the
+// prolongation)
+template <typename T>
+__global__ void k_mg_l0_resid(Dev D) {
+    BS_PDL_ENTRY();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = D.blk_scene[r / BS_ALIGN];
+    if (mg_skip(D, s)) return;
+    if (r >= D.par[s].row0 + D.dyn[s].n) return;
+    const T* __restrict__ u = (const T*)D.mg.u;
+    const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
+    T v = ((const T*)D.mg.xin)[r];
+    if (D.mg.pre0) v -= ell_dot<T>(A, D.nidx, u, r, D.ncount[r], D.kmax, ((const T*)D.mg.adiagT)[r] * u[r]);
+    ((T*)D.mg.zz)[r] = v;
+}
+
+// Level 0, pass 2: restriction of that residual to the half-cells, a thread
+// per half-cell summing the rows of its quadrant in row order (the four
+// threads of a cell read the cell's rows together; one wave of threads)
 template <typename T>
 __global__ void k_mg_l0_down(Dev D) {
     BS_PDL_ENTRY();
-    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t >> 2, quad = t & 3;   // quad = lower | right << 1, as mg.sub
     if (c >= D.ncell_total) return;
     const int s = D.cell_scene[c];
     if (mg_skip(D, s) || c - D.par[s].cell0 >= D.par[s].ncell) return;
-    const T* __restrict__ xin = (const T*)D.mg.xin;
-    const T* __restrict__ u = (const T*)D.mg.u;
-    const T* __restrict__ ad = (const T*)D.mg.adiagT;
-    const T* __restrict__ A = (const T*)(sizeof(T) == 8 ? D.aval : (void*)D.aval32);
-    const int* __restrict__ idx = D.nidx;
+    const T* __restrict__ zz = (const T*)D.mg.zz;
     const uint8_t* __restrict__ sub = D.mg.sub;
     const int r0 = D.cell_start[c], r1 = D.cell_end[c];
-    T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-    for (int r = r0 + lane; r < r1; r += 32) {
-        T v = xin[r];
-        if (D.mg.pre0) v -= ell_dot<T>(A, idx, u, r, D.ncount[r], D.kmax, ad[r] * u[r]);
-        const int t = sub[r];
-        q0 += (t == 0) ? v : (T)0;
-        q1 += (t == 1) ? v : (T)0;
-        q2 += (t == 2) ? v : (T)0;
-        q3 += (t == 3) ? v : (T)0;
+    T q = 0;
+    int r = r0;
+    for (; r + 4 <= r1; r += 4) {   // four rows' loads in flight
+        const T v0 = zz[r], v1 = zz[r + 1], v2 = zz[r + 2], v3 = zz[r + 3];
+        const int t0 = sub[r], t1 = sub[r + 1], t2 = sub[r + 2], t3 = sub[r + 3];
+        q += (t0 == quad) ? v0 : (T)0;
+        q += (t1 == quad) ? v1 : (T)0;
+        q += (t2 == quad) ? v2 : (T)0;
+        q += (t3 == quad) ? v3 : (T)0;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
-        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
-        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
-        q3 += __shfl_xor_sync(0xffffffffu, q3, o);
-    }
-    if (lane < 4) {
-        const ScenePar& P = D.par[s];
-        const int lc = c - P.cell0;
-        const int i0 = lc % P.celly, j0 = lc / P.celly;
-        const int Q = D.mg.off[1][s] + (2 * j0 + (lane >> 1)) * (2 * P.celly) + 2 * i0 + (lane & 1);
-        ((T*)D.mg.r[1])[Q] = lane == 0 ? q0 : lane == 1 ? q1 : lane == 2 ? q2 : q3;
-    }
+    for (; r < r1; ++r) q += (sub[r] == quad) ? zz[r] : (T)0;
+    const ScenePar& P = D.par[s];
+    const int lc = c - P.cell0;
+    const int i0 = lc % P.celly, j0 = lc / P.celly;
+    const int Q = D.mg.off[1][s] + (2 * j0 + (quad >> 1)) * (2 * P.celly) + 2 * i0 + (quad & 1);
+    ((T*)D.mg.r[1])[Q] = q;
 }
 
 // zz = u + cscale * e1[half-cell]: the level-0 value after the coarse correction
@@ -858,7 +868,10 @@ template <typename T>
 void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
     (void)in;   // the Krylov stream already wrote the input (mg_put_input)
     int q = tbegin(L, K_MG_L0DOWN);
-    launch_pdl(L, k_mg_l0_down<T>, gdiv((long)D.ncell_total * 32, L.mg0_tpb), L.mg0_tpb, 0, D);
+    launch_pdl(L, k_mg_l0_resid<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D);
+    tend(L, q);
+    q = tbegin(L, K_MG_L0REST);
+    launch_pdl(L, k_mg_l0_down<T>, gdiv((long)D.ncell_total * 4, 128), 128, 0, D);
     tend(L, q);
     cycle_t<T>(D, L, 1, 0);
     q = tbegin(L, K_MG_PROLONG);
@@ -868,6 +881,7 @@ void apply_t(const Dev& D, const Launch& L, const double* in, double* out) {
     if (D.mg.post0 == 2) {
         launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 1);
         launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 2);
+        *L.launches += 1;
     } else {
         launch_pdl(L, k_mg_l0_up<T>, row_blocks(L, L.mg0_tpb), L.mg0_tpb, 0, D, out, 0);
     }

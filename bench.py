@@ -200,7 +200,9 @@ def algorithmic_bytes(ctx, kernel, precision, basis_reads=None):
             # values (FP64) + column index per nonzero; diag, count, input, output, dot operand per row
             tot += nnz * (8 + 4) + n * (8 + 4 + 8 + 8 + 8)
         elif kernel == "mg_l0_down":
-            tot += nnz * (w + 4) + n * (8 + 4 + w + 8) + n / 27.0 * w
+            # the particle-level residual pass: values + index per nonzero;
+            # input, own smoothed value, diagonal, output and count per row
+            tot += nnz * (w + 4) + n * (4 * w + 4)
         elif kernel == "mg_l0_up":
             tot += nnz * (w + 4) + n * (8 + 4 + w + 8 + 4 + 8)
         elif kernel == "search_effpor":
