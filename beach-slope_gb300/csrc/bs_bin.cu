@@ -339,6 +339,40 @@ __global__ void k_advance_time(Dev D) {
     if (s < D.nscene) D.dyn[s].t = D.dyn[s].t + D.dyn[s].dt;
 }
 
+// A scene's upload, placed: the caller copied the host's arrays in input
+// order into the alternate particle buffers (x2 ... con2, tid2, flags2,
+// pid2), each particle's bucket (2 cell + fluid) into cell2 and, into
+// coderank, the input index of every binned row (the host's stable counting
+// sort by cell, walls first, input order: boundary.f90:140-190,
+// internal.f90:73-95).  Row r gathers its particle and sets the fields the
+// upload starts from: xs = x, ys = y, vxs = vys = 0, porosity 1.
+__global__ void k_upload_gather(Dev D, int row0, int n, int cell0, int has_flags, int has_pid) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int i = D.coderank[row0 + q];
+    const int r = row0 + q, g = row0 + i;
+    const double x = D.x2[g], y = D.y2[g];
+    D.x[r] = x;
+    D.y[r] = y;
+    D.xs[r] = x;
+    D.ys[r] = y;
+    D.vx[r] = D.vx2[g];
+    D.vy[r] = D.vy2[g];
+    D.p[r] = D.p2[g];
+    D.mass[r] = D.mass2[g];
+    D.rho[r] = D.rho2[g];
+    D.oden[r] = D.oden2[g];
+    D.ovol[r] = D.ovol2[g];
+    D.con[r] = D.con2[g];
+    D.vxs[r] = 0.0;
+    D.vys[r] = 0.0;
+    D.por[r] = 1.0;
+    D.tid[r] = D.tid2[g];
+    D.flags[r] = has_flags ? D.flags2[g] : (uint8_t)0;
+    D.pid[r] = has_pid ? D.pid2[g] : i + 1;
+    D.cell[r] = D.cell2[g] / 2 + cell0;
+}
+
 // derived per-particle fields after upload / density update
 __global__ void k_derive(Dev D) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -536,6 +570,13 @@ void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_tim
 void advance_time(const Dev& D, const Launch& L) {
     const int q = tbegin(L, K_ADVANCE);
     k_advance_time<<<gdiv(D.nscene, 64), 64, 0, L.stream>>>(D);
+    tend(L, q);
+}
+
+void upload_gather(const Dev& D, const Launch& L, int row0, int n, int cell0, int has_flags, int has_pid) {
+    if (n <= 0) return;
+    const int q = tbegin(L, K_DERIVE);
+    k_upload_gather<<<gdiv(n, BS_THREADS), BS_THREADS, 0, L.stream>>>(D, row0, n, cell0, has_flags, has_pid);
     tend(L, q);
 }
 

@@ -772,49 +772,33 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
         std::vector<int> fill(bstart.begin(), bstart.end() - 1);
         for (int q = 0; q < n; ++q) ord[fill[bucket[q]]++] = q;
     }
-    std::vector<double> f64[16];
-    const double* src[] = {st->x, st->y, st->vx, st->vy, st->p, st->mass, st->rho, st->oden, st->ovol, st->con};
-    for (int f = 0; f < 10; ++f) {
-        f64[f].resize(n);
-        for (int q = 0; q < n; ++q) f64[f][q] = src[f][ord[q]];
+    // cell ranges from the bucket starts (cell c = buckets 2c, 2c+1; empty
+    // cells: start == end, ranges stay monotone)
+    std::vector<int> cstart(P.ncell), cend(P.ncell);
+    for (int c = 0; c < P.ncell; ++c) {
+        cstart[c] = P.row0 + bstart[2 * (size_t)c];
+        cend[c] = P.row0 + bstart[2 * (size_t)c + 2];
     }
-    std::vector<int8_t> tid(n);
-    std::vector<uint8_t> flags(n);
-    std::vector<int> pid(n), cellv(n);
-    std::vector<int> cstart(P.ncell, 0), cend(P.ncell, 0);
-    for (int q = 0; q < n; ++q) {
-        tid[q] = (int8_t)st->tid[ord[q]];
-        flags[q] = st->flags ? st->flags[ord[q]] : 0;
-        pid[q] = st->pid ? st->pid[ord[q]] : ord[q] + 1;
-        cellv[q] = bucket[ord[q]] / 2 + P.cell0;
-    }
-    {   // cell ranges (empty cells: start == end, ranges stay monotone)
-        std::vector<int> cnt(P.ncell, 0);
-        for (int q = 0; q < n; ++q) cnt[cellv[q] - P.cell0]++;
-        int acc = P.row0;
-        for (int c = 0; c < P.ncell; ++c) {
-            cstart[c] = acc;
-            acc += cnt[c];
-            cend[c] = acc;
-        }
-    }
+    // the arrays in input order into the alternate buffers, the order and
+    // buckets beside them, then one gather kernel places every row
     Dev& D = ctx->D;
     const size_t off = P.row0;
-    double* dst[] = {D.x, D.y, D.vx, D.vy, D.p, D.mass, D.rho, D.oden, D.ovol, D.con};
-    for (int f = 0; f < 10; ++f) CK(cudaMemcpy(dst[f] + off, f64[f].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    std::vector<double> zero(n, 0.0);
-    CK(cudaMemcpy(D.xs + off, f64[0].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.ys + off, f64[1].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.vxs + off, zero.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.vys + off, zero.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    std::vector<double> one(n, 1.0);
-    CK(cudaMemcpy(D.por + off, one.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.tid + off, tid.data(), n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.flags + off, flags.data(), n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.pid + off, pid.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.cell + off, cellv.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.cell_start + P.cell0, cstart.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.cell_end + P.cell0, cend.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice));
+    const double* src[] = {st->x, st->y, st->vx, st->vy, st->p, st->mass, st->rho, st->oden, st->ovol, st->con};
+    double* stage[] = {D.x2, D.y2, D.vx2, D.vy2, D.p2, D.mass2, D.rho2, D.oden2, D.ovol2, D.con2};
+    for (int f = 0; f < 10; ++f)
+        CK(cudaMemcpyAsync(stage[f] + off, src[f], sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<int8_t> tid(n);
+    for (int q = 0; q < n; ++q) tid[q] = (int8_t)st->tid[q];
+    CK(cudaMemcpyAsync(D.tid2 + off, tid.data(), n, cudaMemcpyHostToDevice, ctx->stream));
+    if (st->flags) CK(cudaMemcpyAsync(D.flags2 + off, st->flags, n, cudaMemcpyHostToDevice, ctx->stream));
+    if (st->pid) CK(cudaMemcpyAsync(D.pid2 + off, st->pid, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(D.cell2 + off, bucket.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(D.coderank + off, ord.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(D.cell_start + P.cell0, cstart.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(D.cell_end + P.cell0, cend.data(), sizeof(int) * P.ncell, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    bs::upload_gather(D, launch_of(ctx), P.row0, n, P.cell0, st->flags ? 1 : 0, st->pid ? 1 : 0);
     // grains: sorted by cell
     const int ng = gr ? gr->n : 0;
     if (ng > ctx->gcap[s]) return fail(ctx, BS_E_CAPACITY, "more grains than the grain capacity");

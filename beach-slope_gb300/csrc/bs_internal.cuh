@@ -596,6 +596,8 @@ void wc_rows(const Dev& D, const Launch& L, int mode);
 void wc_wall_pressure(const Dev& D, const Launch& L, int precision);
 void advance_time(const Dev& D, const Launch& L);
 void derive_fields(const Dev& D, const Launch& L);
+// an uploaded scene's rows into their binned order (see k_upload_gather)
+void upload_gather(const Dev& D, const Launch& L, int row0, int n, int cell0, int has_flags, int has_pid);
 // solver
 void solve_fp64(const Dev& D, const Launch& L, int maxit, int check_every, int precond, int mg_precision,
                 int* d_all_conv, int* h_all_conv_pinned, cudaEvent_t ev);
