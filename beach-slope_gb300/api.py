@@ -38,6 +38,8 @@ def _load():
         "bs_prime_scene": (C.c_int, [vp, i32]),
         "bs_write_combined": (C.c_int, [vp, i32, C.c_char_p, C.c_char_p]),
         "bs_download": (C.c_int, [vp, i32, vp]),
+        "bs_download_async": (C.c_int, [vp, i32, vp]),
+        "bs_download_wait": (C.c_int, [vp, i32, vp]),
         "bs_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(vp)]),
         "bs_host_free": (C.c_int, [vp]),
         "bs_scene_info_get": (C.c_int, [vp, i32, vp]),
@@ -191,6 +193,25 @@ class Context:
         st, res = abi.state_out(n, full, out)
         self._check(lib.bs_download(self.h, s, C.byref(st)), "download")
         return res
+
+    def capacity_rows(self, s=0):
+        """Rows the library reserves for scene s (its capacity rounded up to 256)."""
+        return (int(self._caps[s]) + 255) // 256 * 256
+
+    def download_async(self, s=0, out=None):
+        """Start a read-back of scene s that overlaps the steps submitted after
+        it (bs_download_async); out: a pinned_state() dict of at least
+        capacity_rows(s) rows.  Returns a handle for download_wait."""
+        rows = self.capacity_rows(s)
+        st, res = abi.state_out(rows, False, out)
+        self._check(lib.bs_download_async(self.h, s, C.byref(st)), "download_async")
+        return (s, st, res)
+
+    def download_wait(self, handle):
+        """Finish a read-back started by download_async: views of its n rows."""
+        s, st, res = handle
+        self._check(lib.bs_download_wait(self.h, s, C.byref(st)), "download_wait")
+        return {k: v[:st.n] for k, v in res.items()}
 
     def neighbours(self, s=0):
         n = self.info(s)["n"]

@@ -373,6 +373,19 @@ __global__ void k_upload_gather(Dev D, int row0, int n, int cell0, int has_flags
     D.cell[r] = D.cell2[g] / 2 + cell0;
 }
 
+// Rows [row0, row0 + n) of the requested fields into the snapshot buffer
+// (same row positions), one launch in stream order after a step: the copy
+// to the host then reads the snapshot while the next steps run.
+__global__ void k_snapshot(const __grid_constant__ bs::SnapArgs a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.n) return;
+    const int r = a.row0 + q;
+    for (int f = 0; f < a.nf; ++f) a.dst[f][r] = a.src[f][r];
+    if (a.tid) a.tid_dst[r] = a.tid[r];
+    if (a.pid) a.pid_dst[r] = a.pid[r];
+    if (a.flags) a.flags_dst[r] = a.flags[r];
+}
+
 // derived per-particle fields after upload / density update
 __global__ void k_derive(Dev D) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -570,6 +583,13 @@ void cell_max_timestep(const Dev& D, const Launch& L, int do_cellmax, int do_tim
 void advance_time(const Dev& D, const Launch& L) {
     const int q = tbegin(L, K_ADVANCE);
     k_advance_time<<<gdiv(D.nscene, 64), 64, 0, L.stream>>>(D);
+    tend(L, q);
+}
+
+void snapshot(const Launch& L, const SnapArgs& a) {
+    if (a.n <= 0) return;
+    const int q = tbegin(L, K_DERIVE);
+    k_snapshot<<<gdiv(a.n, BS_THREADS), BS_THREADS, 0, L.stream>>>(a);
     tend(L, q);
 }
 

@@ -59,6 +59,15 @@ struct bs_ctx {
     std::vector<std::array<Zone, 2>> zones;
     bool any_zone = false;
     std::vector<SceneDyn> hdyn;   // host copy of the scenes' dynamic state (schedule of the zones)
+    // asynchronous read-back (bs_download_async): the device snapshot (per
+    // field a region of nrow_total rows, then tid and pid as int32, flags,
+    // the scenes' dynamic state), the copy stream and its events, the host
+    // copy of each scene's dynamic state at its snapshot
+    char* snap = nullptr;
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t ev_snap = nullptr;
+    std::vector<cudaEvent_t> ev_copied;   // per scene: its last copy to the host
+    SceneDyn* h_snapdyn = nullptr;
     // multigrid levels run as one clustered launch per visit (mg_sub option)
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
     // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
@@ -731,11 +740,17 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
 int bs_destroy(bs_ctx* ctx) {
     if (!ctx) return BS_E_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->cstream) cudaStreamSynchronize(ctx->cstream);
     for (void* q : ctx->allocs) cudaFree(q);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->evsync) cudaEventDestroy(ctx->evsync);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->h_snapdyn) cudaFreeHost(ctx->h_snapdyn);
+    if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
+    for (auto& e : ctx->ev_copied)
+        if (e) cudaEventDestroy(e);
+    if (ctx->cstream) cudaStreamDestroy(ctx->cstream);
     if (ctx->timer.ready)
         for (auto& e : ctx->timer.ev) cudaEventDestroy(e);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -864,6 +879,75 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->assembled = false;
     return check_launch(ctx);
+}
+
+int bs_download_async(bs_ctx* ctx, int32_t s, bs_state* o) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !o) return BS_E_ARG;
+    if (o->cell || o->coff) return fail(ctx, BS_E_ARG, "cell and coff are not read back asynchronously");
+    const ScenePar& P = ctx->hpar[s];
+    if (o->n < P.cap) return fail(ctx, BS_E_CAPACITY, "asynchronous read-back buffers hold fewer rows than the scene's capacity");
+    Dev& D = ctx->D;
+    const size_t R = ctx->nrow_total;
+    double* outs[BS_SNAP_MAXF] = {o->x, o->y, o->vx, o->vy, o->p, o->mass, o->rho, o->oden, o->ovol, o->con,
+                                  o->xs, o->ys, o->vxs, o->vys, o->porosity, o->resx, o->resy, o->nut, o->tke,
+                                  o->varts, o->gradvx, o->vel, o->cdiff};
+    const double* srcs[BS_SNAP_MAXF] = {D.x, D.y, D.vx, D.vy, D.p, D.mass, D.rho, D.oden, D.ovol, D.con,
+                                        D.xs, D.ys, D.vxs, D.vys, D.por, D.resx, D.resy, D.nut, D.tke,
+                                        D.varts, D.gradvx, D.vel, D.cdiff};
+    if (!ctx->snap) {   // first use: snapshot buffer, copy stream, events, pinned dynamic state
+        const size_t bytes = R * (BS_SNAP_MAXF * sizeof(double) + 2 * sizeof(int) + 1) +
+                             sizeof(SceneDyn) * (size_t)ctx->nscene + 256;
+        if (int rc = dalloc(ctx, &ctx->snap, bytes)) return rc;
+        CK(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming));
+        ctx->ev_copied.assign(ctx->nscene, nullptr);
+        for (auto& e : ctx->ev_copied) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaMallocHost(&ctx->h_snapdyn, sizeof(SceneDyn) * (size_t)ctx->nscene));
+    }
+    char* base = ctx->snap;
+    double* fsnap = (double*)base;                                  // field f: fsnap + f R
+    int* tsnap = (int*)(base + R * BS_SNAP_MAXF * sizeof(double));  // tid, then pid
+    uint8_t* flsnap = (uint8_t*)(tsnap + 2 * R);
+    SceneDyn* dsnap = (SceneDyn*)(((uintptr_t)(flsnap + R) + 255) & ~(uintptr_t)255);
+    // the scene's previous read-back must have left its rows of the snapshot
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[s], 0));
+    bs::SnapArgs a{};
+    int fidx[BS_SNAP_MAXF];
+    for (int f = 0; f < BS_SNAP_MAXF; ++f)
+        if (outs[f]) {
+            fidx[a.nf] = f;
+            a.src[a.nf] = srcs[f];
+            a.dst[a.nf] = fsnap + (size_t)f * R;
+            a.nf++;
+        }
+    a.row0 = P.row0;
+    a.n = P.cap;
+    if (o->tid) { a.tid = D.tid; a.tid_dst = tsnap; }
+    if (o->pid) { a.pid = D.pid; a.pid_dst = tsnap + R; }
+    if (o->flags) { a.flags = D.flags; a.flags_dst = flsnap; }
+    bs::snapshot(launch_of(ctx), a);
+    CK(cudaMemcpyAsync(dsnap + s, D.dyn + s, sizeof(SceneDyn), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->ev_snap, ctx->stream));
+    // the copy to the host on the copy stream, behind the snapshot
+    CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_snap, 0));
+    const size_t off = P.row0, n = (size_t)P.cap;
+    for (int k = 0; k < a.nf; ++k)
+        CK(cudaMemcpyAsync(outs[fidx[k]], fsnap + (size_t)fidx[k] * R + off, sizeof(double) * n,
+                           cudaMemcpyDeviceToHost, ctx->cstream));
+    if (o->tid) CK(cudaMemcpyAsync(o->tid, tsnap + off, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->cstream));
+    if (o->pid) CK(cudaMemcpyAsync(o->pid, tsnap + R + off, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->cstream));
+    if (o->flags) CK(cudaMemcpyAsync(o->flags, flsnap + off, n, cudaMemcpyDeviceToHost, ctx->cstream));
+    CK(cudaMemcpyAsync(ctx->h_snapdyn + s, dsnap + s, sizeof(SceneDyn), cudaMemcpyDeviceToHost, ctx->cstream));
+    CK(cudaEventRecord(ctx->ev_copied[s], ctx->cstream));
+    return check_launch(ctx);
+}
+
+int bs_download_wait(bs_ctx* ctx, int32_t s, bs_state* o) {
+    if (!ctx || s < 0 || s >= ctx->nscene || !o) return BS_E_ARG;
+    if (ctx->ev_copied.empty()) return fail(ctx, BS_E_ARG, "no asynchronous read-back was started");
+    CK(cudaEventSynchronize(ctx->ev_copied[s]));
+    o->n = ctx->h_snapdyn[s].n;
+    return 0;
 }
 
 int bs_host_alloc(size_t bytes, void** p) {

@@ -596,6 +596,21 @@ void wc_rows(const Dev& D, const Launch& L, int mode);
 void wc_wall_pressure(const Dev& D, const Launch& L, int precision);
 void advance_time(const Dev& D, const Launch& L);
 void derive_fields(const Dev& D, const Launch& L);
+// state snapshot of one scene for an asynchronous read-back (k_snapshot):
+// nf FP64 fields, and tid (widened to int32), pid and flags where non-null
+#define BS_SNAP_MAXF 23
+struct SnapArgs {
+    const double* src[BS_SNAP_MAXF];
+    double* dst[BS_SNAP_MAXF];
+    int nf, row0, n;
+    const int8_t* tid;
+    int* tid_dst;
+    const int* pid;
+    int* pid_dst;
+    const uint8_t* flags;
+    uint8_t* flags_dst;
+};
+void snapshot(const Launch& L, const SnapArgs& a);
 // an uploaded scene's rows into their binned order (see k_upload_gather)
 void upload_gather(const Dev& D, const Launch& L, int row0, int n, int cell0, int has_flags, int has_pid);
 // solver

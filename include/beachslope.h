@@ -243,6 +243,19 @@ int bs_upload(struct bs_ctx* ctx, int32_t scene, const bs_state* st, const bs_gr
 int bs_host_alloc(size_t bytes, void** p);
 int bs_host_free(void* p);
 int bs_download(struct bs_ctx* ctx, int32_t scene, bs_state* st);
+/* Read-back that overlaps the steps that follow (the reference writes its
+ * state between steps, output.f90:188-222; a host loop here can keep the GPU
+ * stepping meanwhile).  Snapshots the scene's rows of the non-null fields of
+ * st on the device in stream order after the work already submitted (the next
+ * bs_step can be called at once), then copies the snapshot into st's buffers
+ * on a copy stream.  st's buffers hold the scene's capacity rows (bs_create's
+ * capacity rounded up to a multiple of 256; st->n gives their size) and stay
+ * untouched until bs_download_wait, which waits for the copy and sets st->n to
+ * the particle count at the snapshot; rows beyond it are padding.  cell and
+ * coff are not available here (bs_download).  Pinned buffers (bs_host_alloc)
+ * let the copy overlap compute; one read-back in flight per scene. */
+int bs_download_async(struct bs_ctx* ctx, int32_t scene, bs_state* st);
+int bs_download_wait(struct bs_ctx* ctx, int32_t scene, bs_state* st);
 int bs_scene_info_get(struct bs_ctx* ctx, int32_t scene, bs_scene_info* out);
 int bs_clear_errors(struct bs_ctx* ctx);
 int bs_sync(struct bs_ctx* ctx);
