@@ -4,11 +4,13 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstddef>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bs_internal.cuh"
@@ -775,13 +777,28 @@ int bs_upload(bs_ctx* ctx, int32_t s, const bs_state* st, const bs_grains* gr) {
     // bin: (cell key, walls first, input order) -- boundary.f90:140-190,
     // internal.f90:73-95 -- as a stable counting sort over 2 buckets per cell
     std::vector<int> bucket(n), ord(n), bstart(2 * (size_t)P.ncell + 1, 0);
-    for (int q = 0; q < n; ++q) {
-        int ci, cj;
-        if (!locate(p, st->x[q], st->y[q], &ci, &cj)) return fail(ctx, BS_E_DOMAIN, "particle outside the interior cell grid");
-        const int k = (cj - 1) * p.celly + (ci - 1);
-        bucket[q] = 2 * k + (st->tid[q] == BS_TID_FLUID ? 1 : 0);
-        bstart[bucket[q] + 1]++;
+    {   // each particle's bucket on the host's cores (independent per particle)
+        const int T = std::max(1, std::min(16, std::min((int)std::thread::hardware_concurrency(), n / 16384)));
+        std::atomic<int> outside{0};
+        auto part = [&](int t) {
+            const int q0 = (int)((long)n * t / T), q1 = (int)((long)n * (t + 1) / T);
+            for (int q = q0; q < q1; ++q) {
+                int ci, cj;
+                if (!locate(p, st->x[q], st->y[q], &ci, &cj)) {
+                    outside = 1;
+                    bucket[q] = 0;
+                    continue;
+                }
+                bucket[q] = 2 * ((cj - 1) * p.celly + (ci - 1)) + (st->tid[q] == BS_TID_FLUID ? 1 : 0);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < T; ++t) pool.emplace_back(part, t);
+        part(0);
+        for (auto& th : pool) th.join();
+        if (outside) return fail(ctx, BS_E_DOMAIN, "particle outside the interior cell grid");
     }
+    for (int q = 0; q < n; ++q) bstart[bucket[q] + 1]++;
     for (size_t b = 0; b < 2 * (size_t)P.ncell; ++b) bstart[b + 1] += bstart[b];
     {
         std::vector<int> fill(bstart.begin(), bstart.end() - 1);
