@@ -162,6 +162,7 @@ def main():
     ap.add_argument("--precision", nargs="+", default=["mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=0,
                     help="tune the batch of this many seeded beach scenes instead of single scenes")
+    ap.add_argument("--steps", type=int, default=2, help="timed steps per candidate")
     args = ap.parse_args()
     for prec_name in args.precision:
         prec = abi.PREC_MIXED if prec_name == "mixed" else abi.PREC_FP64
@@ -173,7 +174,7 @@ def main():
             ctx.step(2)
             n = sum(len(q["x"]) for q in S)
             print(f"{prec_name} batch of {len(P)} scenes, n={n}", flush=True)
-            best, ms, _ = tune(ctx, G)
+            best, ms, _ = tune(ctx, G, steps=args.steps)
             print(f"  best {best} {ms:.2f} ms/step", flush=True)
             save(prec, n, best, ms, f"batch of {len(P)} beach scenes", scenes=len(P))
             ctx.close()
@@ -185,7 +186,7 @@ def main():
             ctx.step(2)
             n = len(st["x"])
             print(f"{prec_name} dx={dx} n={n}", flush=True)
-            best, ms, _ = tune(ctx, [gr])
+            best, ms, _ = tune(ctx, [gr], steps=args.steps)
             print(f"  best {best} {ms:.2f} ms/step", flush=True)
             save(prec, n, best, ms, f"beach dx={dx}")
             ctx.close()
