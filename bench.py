@@ -166,7 +166,7 @@ TIMED_KERNELS = ("search_effpor", "bicg_it1_spmv", "bicg_it2_spmv", "mg_l0_down"
 # every launch of seven solves of the double-float form (k_fg_arn1<1>) the
 # mixed bench times.
 TRAFFIC_RATIO = {"search_effpor": 0.46, "bicg_it1_spmv": 0.99, "bicg_it2_spmv": 0.99,
-                 "mg_l0_down": 0.98, "mg_l0_up": 0.93, "fg_arnoldi_spmv": 0.90, "fg_project": 0.97}
+                 "mg_l0_down": 0.99, "mg_l0_up": 0.93, "fg_arnoldi_spmv": 0.90, "fg_project": 0.97}
 
 
 def fg_columns(iters, restart):
