@@ -7,7 +7,7 @@ restart length), then the multigrid cycle shape (W-cycle depth,
 pre-smoothing on the particle and cell levels, Jacobi damping,
 coarse-correction scale, coarsest sweeps, the clustered subtree, the
 second particle-level post-sweep, the exact coarse solve, the double-float
-FGMRES basis), the
+FGMRES basis, the FP64 form's cycle in FP32), the
 threads per block of the neighbour sweeps and of the particle-level
 multigrid kernels, then the restart length again --
 and keeps the fastest configuration whose solves converged without error
@@ -23,7 +23,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "tuning.json")
 OPTIONS = ("ppe_restart", "ppe_solver", "mg_wlev", "mg_pre0", "mg_prec", "mg_post0", "mg_omega", "mg_cscale",
-           "mg_coarse_sweeps", "mg_sub", "mg_exact", "fg_df", "sweep_tpb", "mg0_tpb")
+           "mg_coarse_sweeps", "mg_sub", "mg_exact", "fg_df", "mg_fp32", "sweep_tpb", "mg0_tpb")
 
 
 def bucket(n_particles):
@@ -101,7 +101,7 @@ def tune(ctx, grains, steps=2, verbose=True):
 
     base = {"ppe_restart": 30, "ppe_solver": 0, "mg_wlev": 2, "mg_pre0": 1, "mg_prec": 1, "mg_omega": 0.9,
             "mg_cscale": 1.5, "mg_coarse_sweeps": 10, "mg_sub": 0, "mg_post0": 1, "fg_df": 1,
-            "sweep_tpb": 256, "mg0_tpb": 256, "mg_exact": 0}
+            "sweep_tpb": 256, "mg0_tpb": 256, "mg_exact": 0, "mg_fp32": 0}
     best, best_ms = dict(base), run(base)
     solver_stage = [{"ppe_solver": 0}] + [{"ppe_solver": 1, "ppe_restart": r} for r in (20, 30, 50, 80, 120)]
     stages = [
@@ -115,6 +115,7 @@ def tune(ctx, grains, steps=2, verbose=True):
         [{"mg_sub": 1}],
         [{"mg_post0": 2}],
         [{"fg_df": 0}],
+        [{"mg_fp32": 1}],   # the FP64 form's cycle in FP32 (no effect in the mixed form)
         # launch shapes: threads per block of the neighbour sweeps and of the
         # particle-level multigrid kernels (same results, different occupancy)
         [{"sweep_tpb": t} for t in (64, 128, 256)],

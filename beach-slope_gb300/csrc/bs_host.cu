@@ -74,6 +74,9 @@ struct bs_ctx {
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
     // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
     int fg_df_on = 1;
+    // option "mg_fp32": the FP64 form's multigrid preconditioner in FP32 (the
+    // mixed form's cycle; the Krylov solve and its stopping test stay FP64)
+    int mg_fp32 = 0;
     // threads per block of the neighbour sweeps and of the particle-level
     // multigrid kernels (options "sweep_tpb", "mg0_tpb"; the autotuner picks them)
     int sweep_tpb = BS_THREADS, mg0_tpb = BS_THREADS;
@@ -184,6 +187,9 @@ int fg_ensure(bs_ctx* ctx) {
     return 0;
 }
 
+// precision of the multigrid preconditioner's cycle (its setup, matrix copy and level arrays)
+int mg_prec_of(const bs_ctx* c) { return (c->precision == BS_PREC_MIXED || c->mg_fp32) ? BS_PREC_MIXED : BS_PREC_FP64; }
+
 bs::Launch launch_of(bs_ctx* c) {
     bs::Launch L;
     L.stream = c->stream;
@@ -245,8 +251,8 @@ void mg_sub_choose(bs_ctx* c) {
         const int cs = std::max(1, (mx + 1023) / 1024);
         if (cs > 16 || (long)cs * c->nscene > c->sm_count) continue;
         if (M.nlev - l + 1 > BS_MG_SUBL || mg_sub_nops(c, l) > BS_MG_MAXOPS) continue;
-        const size_t smem = 2 * (size_t)M.coarse_max * (c->precision == BS_PREC_MIXED ? sizeof(float) : sizeof(double));
-        if (bs::mg_sub_max_clusters(c->precision, cs, smem) < 1) continue;
+        const size_t smem = 2 * (size_t)M.coarse_max * (mg_prec_of(c) == BS_PREC_MIXED ? sizeof(float) : sizeof(double));
+        if (bs::mg_sub_max_clusters(mg_prec_of(c), cs, smem) < 1) continue;
         c->mgsub_level = l;
         c->mgsub_cs = cs;
         return;
@@ -415,12 +421,12 @@ int st_solve(bs_ctx* c) {
         // the double-float basis serves the preconditioned mixed solve (the
         // basis is only read by the Gram-Schmidt passes there)
         c->D.fg_df = (c->fg_df_on && c->precision == BS_PREC_MIXED && c->prm[0].ppe_precond) ? 1 : 0;
-        bs::solve_fgmres(c->D, L, maxit, c->prm[0].ppe_precond ? 2 : 8, c->prm[0].ppe_precond, c->precision,
+        bs::solve_fgmres(c->D, L, maxit, c->prm[0].ppe_precond ? 2 : 8, c->prm[0].ppe_precond, mg_prec_of(c),
                          c->d_nconv, c->h_pinned, c->evsync);
     } else if (c->precision == BS_PREC_MIXED && c->prm[0].mixed_max_outer > 0)
         bs::solve_mixed(c->D, L, maxit, 8, c->d_nconv, c->h_pinned, c->evsync);
     else
-        bs::solve_fp64(c->D, L, maxit, c->prm[0].ppe_precond ? 4 : 8, c->prm[0].ppe_precond, c->precision,
+        bs::solve_fp64(c->D, L, maxit, c->prm[0].ppe_precond ? 4 : 8, c->prm[0].ppe_precond, mg_prec_of(c),
                        c->d_nconv, c->h_pinned, c->evsync);
     return 0;
 }
@@ -1149,6 +1155,14 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else if (k == "mg_sub" && (value == 0 || value == 1)) ctx->mgsub_on = (int)value;
     else if (k == "fg_df" && (value == 0 || value == 1)) ctx->fg_df_on = (int)value;
+    else if (k == "mg_fp32" && (value == 0 || value == 1)) {
+        if (value == 1 && ctx->precision != BS_PREC_MIXED && !ctx->D.aval32) {   // the FP32 matrix copy
+            const size_t E = (size_t)ctx->nrow_total * ctx->kmax;
+            if (int rc = dalloc(ctx, &ctx->D.aval32, E)) return rc;
+            if (int rc = dalloc(ctx, &ctx->D.aval_lo, E)) return rc;
+        }
+        ctx->mg_fp32 = (int)value;
+    }
     else if (k == "ppe_solver" && (value == BS_SOLVER_BICGSTAB || value == BS_SOLVER_FGMRES))
         for (auto& p : ctx->prm) p.ppe_solver = (int32_t)value;
     else if (k == "ppe_restart" && value >= 1 && value <= BS_FG_MAXM)
@@ -1197,6 +1211,7 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;
     else if (k == "mg_sub") *value = ctx->mgsub_on;
     else if (k == "fg_df") *value = ctx->fg_df_on;
+    else if (k == "mg_fp32") *value = ctx->mg_fp32;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
     else if (k == "mg_exact") *value = M.exact;
@@ -1678,7 +1693,7 @@ std::vector<unsigned char> step_key(const bs_ctx* c, int flags) {
     const int v[] = {flags, c->precision, c->prm[0].ppe_solver, c->prm[0].ppe_restart, c->prm[0].ppe_precond,
                      c->prm[0].mixed_max_outer, max_ppe_maxit(c), c->mgsub_on, c->mgsub_level, c->mgsub_cs,
                      c->fg_df_on, c->disp_ready ? 1 : 0, any_scalar_on(c) ? 1 : 0, c->nblk_total,
-                     c->sweep_tpb, c->mg0_tpb};
+                     c->sweep_tpb, c->mg0_tpb, c->mg_fp32};
     key_put(k, v);
     for (const auto& m : c->mglev) key_put(k, m);
     k.insert(k.end(), c->mgneed.begin(), c->mgneed.end());
@@ -1737,9 +1752,9 @@ bool record_step(bs_ctx* ctx, int flags) {
     const int precond = ctx->prm[0].ppe_precond;
     bool ok;
     if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
-        ok = bs::capture_fgmres(D, L, ctx->side, maxit, precond ? 2 : 8, precond, ctx->precision, ctx->d_nconv);
+        ok = bs::capture_fgmres(D, L, ctx->side, maxit, precond ? 2 : 8, precond, mg_prec_of(ctx), ctx->d_nconv);
     else
-        ok = bs::capture_fp64(D, L, ctx->side, maxit, precond ? 4 : 8, precond, ctx->precision, ctx->d_nconv);
+        ok = bs::capture_fp64(D, L, ctx->side, maxit, precond ? 4 : 8, precond, mg_prec_of(ctx), ctx->d_nconv);
     if (!ok) return false;
     bs::comp_vel(D, L, ctx->precision, 1, 1);
     bs::cell_max_timestep(D, L, 1, 0);

@@ -334,7 +334,10 @@ int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path,
  * top, V-cycle below), "mg_sub" (0/1: the small levels of a visit as one
  * clustered launch), "ppe_precond", "fg_df" (0/1, default 1: the FGMRES basis
  * of the preconditioned mixed solve as double-float (hi, lo) FP32 pairs, its
- * dots on the FP32 pipe, h_{j+1,j} from the Gram relation), "sweep_tpb" /
+ * dots on the FP32 pipe, h_{j+1,j} from the Gram relation), "mg_fp32" (0/1,
+ * default 0: the FP64 form's multigrid preconditioner in FP32 like the mixed
+ * form's; the Krylov solve, its residuals and stopping test stay FP64, so the
+ * pressure solves the same FP64 system to the same tolerance), "sweep_tpb" /
  * "mg0_tpb" (64, 128 or 256 threads per block of the neighbour sweeps / of
  * the particle-level multigrid kernels; every row is computed the same way
  * whatever the block size), "step_graph" (0/1, default 1: each bs_step is
