@@ -614,7 +614,7 @@ const char* const kernel_names[K_COUNT] = {
     "mx_residual", "mx_convert", "bicg_p_update", "bicg_s_update", "mx_update", "mg_galerkin0",
     "mg_galerkin", "mg_l0_down", "mg_down", "mg_coarse", "mg_up", "mg_l0_up", "mg_l0_prolong",
     "mg_resid", "relpos", "wc_continuity", "wc_rows", "wc_wall_pressure",
-    "fg_start", "fg_put", "fg_arnoldi_spmv", "fg_project", "fg_update", "buffer_exchange", "wall_ghost", "mg_subtree", "collision_shift", "mg_l0_restrict"};
+    "fg_start", "fg_put", "fg_arnoldi_spmv", "fg_project", "fg_update", "buffer_exchange", "wall_ghost", "mg_subtree", "collision_shift", "mg_l0_restrict", "mg_tail"};
 
 // Accumulate the finished launches of the ring in order; with wait, block on
 // the oldest pending end event (used when the ring is full).

@@ -72,6 +72,10 @@ struct bs_ctx {
     SceneDyn* h_snapdyn = nullptr;
     // multigrid levels run as one clustered launch per visit (mg_sub option)
     int mgsub_on = 0, mgsub_level = 0, mgsub_cs = 1, sm_count = 0;
+    // the last two levels of a visit in one block per scene (option mg_tail,
+    // default on: bit-identical to the separate launches): the level it
+    // starts at (0: off or no level qualifies)
+    int mgtail_on = 1, mgtail_level = 0;
     // FGMRES basis as double-float (hi, lo) FP32 pairs in the preconditioned mixed solve
     int fg_df_on = 1;
     // option "mg_fp32": the FP64 form's multigrid preconditioner in FP32 (the
@@ -201,6 +205,7 @@ bs::Launch launch_of(bs_ctx* c) {
     L.mglev = c->mglev.empty() ? nullptr : c->mglev.data();
     L.mgneed = c->mgneed.empty() ? nullptr : c->mgneed.data();
     L.mgsub_level = c->mgsub_level;
+    L.mgtail = c->mgtail_level;
     L.mgsub_cs = c->mgsub_cs;
     L.sweep_tpb = c->sweep_tpb;
     L.mg0_tpb = c->mg0_tpb;
@@ -256,6 +261,30 @@ void mg_sub_choose(bs_ctx* c) {
         c->mgsub_level = l;
         c->mgsub_cs = cs;
         return;
+    }
+}
+
+// The level whose visits run with the coarsest level in one block per scene
+// (k_mg_tail): every scene that has it has its coarsest level right below it,
+// with at most 1024 cells on it and 256 on the coarsest; 0 when none does or
+// the option, the exact coarse solve or the clustered subtree is on.
+int coarsest_level(const bs_ctx* c, int s);
+void mg_tail_choose(bs_ctx* c) {
+    const MgDev& M = c->D.mg;
+    c->mgtail_level = 0;
+    if (!c->mgtail_on || M.exact || c->mgsub_level || c->mglev.empty()) return;
+    for (int l = 1; l < M.nlev; ++l) {
+        bool ok = true, any = false;
+        for (int s = 0; s < c->nscene && ok; ++s) {
+            if (coarsest_level(c, s) < l) continue;
+            any = true;
+            const int mf = c->mglev[l].nx[s] * c->mglev[l].ny[s], mc = c->mglev[l + 1].nx[s] * c->mglev[l + 1].ny[s];
+            ok = coarsest_level(c, s) == l + 1 && mf <= 1024 && mc <= 256;
+        }
+        if (ok && any) {
+            c->mgtail_level = l;
+            return;
+        }
     }
 }
 
@@ -316,6 +345,7 @@ void mg_tables(bs_ctx* c) {
         }
     }
     mg_sub_choose(c);
+    mg_tail_choose(c);
 }
 
 // per-scene constants that do not depend on the layout
@@ -1155,6 +1185,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     else if (k == "ppe_precond") for (auto& p : ctx->prm) p.ppe_precond = (int32_t)value;
     else if (k == "mg_sub" && (value == 0 || value == 1)) ctx->mgsub_on = (int)value;
     else if (k == "fg_df" && (value == 0 || value == 1)) ctx->fg_df_on = (int)value;
+    else if (k == "mg_tail" && (value == 0 || value == 1)) ctx->mgtail_on = (int)value;
     else if (k == "mg_fp32" && (value == 0 || value == 1)) {
         if (value == 1 && ctx->precision != BS_PREC_MIXED && !ctx->D.aval32) {   // the FP32 matrix copy
             const size_t E = (size_t)ctx->nrow_total * ctx->kmax;
@@ -1191,6 +1222,7 @@ int bs_set_option(bs_ctx* ctx, const char* name, double value) {
     if (ctx->prm[0].ppe_solver == BS_SOLVER_FGMRES)
         if (int rc = fg_ensure(ctx)) return rc;
     mg_sub_choose(ctx);   // the W depth changes the visits' op lists
+    mg_tail_choose(ctx);
     ctx->graph.valid = false;   // the captured iteration holds the old values
     return 0;
 }
@@ -1211,6 +1243,8 @@ int bs_get_option(bs_ctx* ctx, const char* name, double* value) {
     else if (k == "ppe_solver") *value = ctx->prm[0].ppe_solver;
     else if (k == "mg_sub") *value = ctx->mgsub_on;
     else if (k == "fg_df") *value = ctx->fg_df_on;
+    else if (k == "mg_tail") *value = ctx->mgtail_on;
+    else if (k == "mg_tail_level") *value = ctx->mgtail_level;
     else if (k == "mg_fp32") *value = ctx->mg_fp32;
     else if (k == "mg_sub_level") *value = ctx->mgsub_level;
     else if (k == "ppe_restart") *value = ctx->prm[0].ppe_restart;
@@ -1693,7 +1727,7 @@ std::vector<unsigned char> step_key(const bs_ctx* c, int flags) {
     const int v[] = {flags, c->precision, c->prm[0].ppe_solver, c->prm[0].ppe_restart, c->prm[0].ppe_precond,
                      c->prm[0].mixed_max_outer, max_ppe_maxit(c), c->mgsub_on, c->mgsub_level, c->mgsub_cs,
                      c->fg_df_on, c->disp_ready ? 1 : 0, any_scalar_on(c) ? 1 : 0, c->nblk_total,
-                     c->sweep_tpb, c->mg0_tpb, c->mg_fp32};
+                     c->sweep_tpb, c->mg0_tpb, c->mg_fp32, c->mgtail_level};
     key_put(k, v);
     for (const auto& m : c->mglev) key_put(k, m);
     k.insert(k.end(), c->mgneed.begin(), c->mgneed.end());

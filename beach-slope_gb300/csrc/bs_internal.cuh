@@ -467,7 +467,7 @@ enum KId {
     K_BICG_INIT, K_BICG_IT1, K_BICG_IT2, K_BICG_IT3, K_TRUERES, K_ADVANCE, K_DERIVE, K_VELMAG,
     K_PROJECTION, K_MX_INIT, K_MX_IT1, K_MX_IT2, K_MX_IT3, K_MX_RES, K_MX_CONV, K_BICG_PUPD, K_BICG_SUPD,
     K_MX_UPD, K_MG_GAL0, K_MG_GALC, K_MG_L0DOWN, K_MG_DOWN, K_MG_COARSE, K_MG_UP, K_MG_L0UP, K_MG_PROLONG,
-    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_MG_SUB, K_COLL, K_MG_L0REST, K_COUNT
+    K_MG_RESID, K_RELPOS, K_WC_CONT, K_WC_ROWS, K_WC_WALLP, K_FG_START, K_FG_PUT, K_FG_ARN, K_FG_ORTH, K_FG_UPD, K_BUFX, K_GHOST, K_MG_SUB, K_COLL, K_MG_L0REST, K_MG_TAIL, K_COUNT
 };
 extern const char* const kernel_names[K_COUNT];
 struct KTimer {
@@ -509,6 +509,7 @@ struct Launch {
     const unsigned char* mgneed;   // per level: bit0 some scene visits it, bit1 restriction and
                                    // prolongation to the next level, bit2 coarsest-level solve
     int mgsub_level, mgsub_cs;     // first level of the clustered subtree (0: per-level launches), CTAs per cluster
+    int mgtail;                    // level whose visits run with the coarsest level in one block (0: none)
     int sweep_tpb;                 // threads per block of the neighbour sweeps (64, 128 or 256)
     int mg0_tpb;                   // threads per block of the particle-level multigrid kernels
     const MgExact* exact;          // the scenes' exactly solved levels (when D.mg.exact)

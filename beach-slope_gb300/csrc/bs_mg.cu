@@ -508,6 +508,151 @@ __device__ __forceinline__ void op_coarse(const MgDev& M, const LevelS& F, int a
     for (int q = threadIdx.x; q < m; q += blockDim.x) out[F.off + q] = acc ? out[F.off + q] + z[q] : z[q];
 }
 
+// ---- the last two levels of a visit in one block (option mg_tail)
+// Scene k's visit of level l (F, at most 1024 cells) whose next level C (at
+// most BS_MG_TAIL_C cells) is its coarsest: pre-sweep and restriction
+// (op_down), the coarsest-level Jacobi sweeps (op_coarse; with wcycle the
+// residual op_resid and a second solve added, as a W-cycle level visits its
+// next level twice) and prolongation + post-sweep (op_up), one thread per
+// cell of F, both levels in shared memory between the operations instead of
+// a launch each.  Every value is formed by the same operations in the same
+// order as the separate launches (bit-identical).
+#define BS_MG_TAIL_F 1024
+#define BS_MG_TAIL_C 256
+template <typename T>
+__global__ void __launch_bounds__(BS_MG_TAIL_F) k_mg_tail(Dev D, __grid_constant__ const MgLevel F,
+                                                          __grid_constant__ const MgLevel C, int acc, int wcycle) {
+    BS_PDL_ENTRY();
+    __shared__ T R[BS_MG_TAIL_F], Y[BS_MG_TAIL_F], RS[BS_MG_TAIL_F], DV[BS_MG_TAIL_F];
+    __shared__ T RC[BS_MG_TAIL_C], ZC[BS_MG_TAIL_C], ZC2[BS_MG_TAIL_C], ZA[BS_MG_TAIL_C];
+    const MgDev& M = D.mg;
+    const int k = blockIdx.x;
+    const LevelS f = view_of(F, k), c = view_of(C, k);
+    const int mf = f.nx * f.ny, mc = c.nx * c.ny;
+    if (mf == 0) return;
+    const int t = threadIdx.x;
+    const T w = (T)M.omega, cs = (T)M.cscale;
+    const T* __restrict__ Af = (const T*)M.A[f.l];
+    const T* __restrict__ Ac = (const T*)M.A[c.l];
+    // fine cell t: its stencil in registers, r and D^-1 in shared memory
+    const bool fa = t < mf;
+    const int fi = t % f.ny, fj = t / f.ny;
+    T a9[9];
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        const int ni = fi + (s % 3) - 1, nj = fj + (s / 3) - 1;
+        a9[s] = (fa && !(ni < 0 || nj < 0 || ni >= f.ny || nj >= f.nx)) ? __ldg(Af + (long)s * f.n + f.off + t) : (T)0;
+    }
+    if (fa) {
+        R[t] = ((const T*)M.r[f.l])[f.off + t];
+        DV[t] = __ldg((const T*)M.dinv[f.l] + f.off + t);
+    }
+    // coarse cell t: its stencil, D^-1 (and r below) in registers
+    const bool ca = t < mc;
+    const int ci = t % c.ny, cj = t / c.ny;
+    T c9[9], dc = 0;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        const int ni = ci + (s % 3) - 1, nj = cj + (s / 3) - 1;
+        c9[s] = (ca && !(ni < 0 || nj < 0 || ni >= c.ny || nj >= c.nx)) ? __ldg(Ac + (long)s * c.n + c.off + t) : (T)0;
+    }
+    if (ca) dc = __ldg((const T*)M.dinv[c.l] + c.off + t);
+    __syncthreads();
+    // op_down: the pre-sweep from zero and each fine cell's residual
+    if (fa) Y[t] = w * R[t] * DV[t];
+    __syncthreads();
+    if (fa) {
+        T ax = 0;
+        if (M.prec) {
+#pragma unroll
+            for (int s = 0; s < 9; ++s) {
+                const int ni = fi + (s % 3) - 1, nj = fj + (s / 3) - 1;
+                if (ni < 0 || nj < 0 || ni >= f.ny || nj >= f.nx) continue;
+                ax += a9[s] * Y[nj * f.ny + ni];
+            }
+            RS[t] = R[t] - ax;
+        } else {
+            RS[t] = R[t];
+        }
+    }
+    __syncthreads();
+    // restriction: the 2x2 box's children, b outer, a inner
+    T rcv = 0;
+    if (ca) {
+        T sum = 0;
+        for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {   // a child beyond the grid adds 0, as in k_mg_down
+                const int gi = 2 * ci + a, gj = 2 * cj + b;
+                sum += (gi < f.ny && gj < f.nx) ? RS[gj * f.ny + gi] : (T)0;
+            }
+        rcv = sum;
+        RC[t] = sum;
+    }
+    // op_coarse: damped Jacobi from zero, one coarse cell per thread
+    auto jacobi = [&](T rhs, T* z, T* z2) {
+        if (ca) z[t] = 0;
+        __syncthreads();
+        for (int it = 0; it < M.coarse_sweeps; ++it) {
+            if (ca) {
+                T ax = 0;
+#pragma unroll
+                for (int s = 0; s < 9; ++s) {
+                    const int ni = ci + (s % 3) - 1, nj = cj + (s / 3) - 1;
+                    if (ni < 0 || nj < 0 || ni >= c.ny || nj >= c.nx) continue;
+                    ax += c9[s] * z[nj * c.ny + ni];
+                }
+                z2[t] = z[t] + w * dc * (rhs - ax);
+            }
+            __syncthreads();
+            if (ca) z[t] = z2[t];
+            __syncthreads();
+        }
+    };
+    jacobi(rcv, ZC, ZC2);
+    if (wcycle) {
+        // op_resid on the coarsest level, then the second solve added to z
+        T r2 = 0;
+        if (ca) {
+            T ax = 0;
+#pragma unroll
+            for (int s = 0; s < 9; ++s) {
+                const int ni = ci + (s % 3) - 1, nj = cj + (s / 3) - 1;
+                if (ni < 0 || nj < 0 || ni >= c.ny || nj >= c.nx) continue;
+                ax += c9[s] * ZC[nj * c.ny + ni];
+            }
+            r2 = rcv - ax;
+            ZA[t] = ZC[t];
+        }
+        __syncthreads();
+        jacobi(r2, ZC, ZC2);
+        if (ca) ZC[t] = ZA[t] + ZC[t];
+        __syncthreads();
+    }
+    // op_up: prolongation (scaled, constant per box) + one post-sweep
+    if (fa) {
+        const T wp = M.prec ? w : (T)0;
+        T zv[9];
+#pragma unroll
+        for (int s = 0; s < 9; ++s) {
+            const int ni = fi + (s % 3) - 1, nj = fj + (s / 3) - 1;
+            const bool in = !(ni < 0 || nj < 0 || ni >= f.ny || nj >= f.nx);
+            const int nb = nj * f.ny + ni;
+            zv[s] = in ? wp * R[nb] * DV[nb] + cs * ZC[(nj / 2) * c.ny + (ni / 2)] : (T)0;
+        }
+        const T zc = zv[4];
+        T ax = 0;
+#pragma unroll
+        for (int s = 0; s < 9; ++s) {
+            const int ni = fi + (s % 3) - 1, nj = fj + (s / 3) - 1;
+            if (ni < 0 || nj < 0 || ni >= f.ny || nj >= f.nx) continue;
+            ax += a9[s] * zv[s];
+        }
+        const T v = zc + w * DV[t] * (R[t] - ax);
+        T* zo = (T*)M.z[f.l];
+        zo[f.off + t] = acc ? zo[f.off + t] + v : v;
+    }
+}
+
 // ---- one launch per level operation
 // A quad of lanes per coarse cell: lane (a, b) smooths child (a, b), the
 // first lane adds the four values in op_down's order (b outer, a inner), so
@@ -815,6 +960,12 @@ void cycle_t(const Dev& D, const Launch& L, int l, int acc) {
     const unsigned char need = L.mgneed[l];
     if (!(need & 1)) return;
     int q;
+    if (l == L.mgtail) {   // this level and the coarsest below it: one block per scene
+        q = tbegin(L, K_MG_TAIL);
+        launch_pdl(L, k_mg_tail<T>, D.nscene, BS_MG_TAIL_F, 0, D, G[l], G[l + 1], acc, l <= D.mg.wlev ? 1 : 0);
+        tend(L, q);
+        return;
+    }
     if (l == L.mgsub_level) {   // this level and everything below: one clustered launch
         MgSub S;
         S.l0 = l;

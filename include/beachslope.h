@@ -337,12 +337,16 @@ int bs_write_combined(struct bs_ctx* ctx, int32_t scene, const char* fluid_path,
  * dots on the FP32 pipe, h_{j+1,j} from the Gram relation), "mg_fp32" (0/1,
  * default 0: the FP64 form's multigrid preconditioner in FP32 like the mixed
  * form's; the Krylov solve, its residuals and stopping test stay FP64, so the
- * pressure solves the same FP64 system to the same tolerance), "sweep_tpb" /
+ * pressure solves the same FP64 system to the same tolerance), "mg_tail" (0/1,
+ * default 1: each visit of the level above the coarsest, with the coarsest
+ * solve, as one block per scene in shared memory -- bit-identical to the
+ * separate launches; used where every scene ends on the same two levels of at
+ * most 1024 and 256 cells), "sweep_tpb" /
  * "mg0_tpb" (64, 128 or 256 threads per block of the neighbour sweeps / of
  * the particle-level multigrid kernels; every row is computed the same way
  * whatever the block size), "step_graph" (0/1, default 1: each bs_step is
  * one captured CUDA graph with the loops on the device);
- * bs_get_option also reads "mg_levels", "mg_sub_level", "step_graph_steps"
+ * bs_get_option also reads "mg_levels", "mg_sub_level", "mg_tail_level", "step_graph_steps"
  * and "step_graph_cached". */
 int bs_set_option(struct bs_ctx* ctx, const char* name, double value);
 int bs_get_option(struct bs_ctx* ctx, const char* name, double* value);
