@@ -132,7 +132,7 @@ struct Dev {
     // particle fields (current buffer)
     double *x, *y, *xs, *ys, *vx, *vy, *vxs, *vys, *p, *mass, *rho, *oden, *ovol, *con;
     float *xr, *yr;                 // position relative to the row's cell corner (xleft, ybot), FP32
-    float4* pos4;                   // mixed: position as (x hi, x lo, y hi, y lo) FP32 pairs (pos_split),
+    float4* pos4;                   // mixed: position as (x hi, x lo, y hi, y lo) FP32 pairs (f2_split2),
                                     // written by k_relpos and by the packs of the sweeps that read it (k_quot)
     double *vol, *nu;               // derived: m/rho, vis(oden)/oden
     int8_t* tid;
@@ -327,15 +327,16 @@ __device__ __forceinline__ float2 f2_split(double v) {
     const float h = __double2float_rn(v);
     return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
 }
-// a position row as (x hi, x lo, y hi, y lo)
-__device__ __forceinline__ float4 pos_split(double x, double y) {
+// two doubles as (x hi, x lo, y hi, y lo): a position, a velocity, a pair
+// of quotients
+__device__ __forceinline__ float4 f2_split2(double x, double y) {
     const float2 a = f2_split(x), b = f2_split(y);
     return make_float4(a.x, a.y, b.x, b.y);
 }
-// b - a of two double-float coordinates, renormalised (.x = fl32 of the
+// b - a of two double-float values, renormalised (.x = fl32 of the
 // difference): the hi parts subtracted exactly, the lo parts added; absolute
-// error within ~2^-46 max(|a|, |b|) (1e-13 m on a 4 m domain)
-__device__ __forceinline__ float2 pos_diff(float bh, float bl, float ah, float al) {
+// error within ~2^-46 max(|a|, |b|) (1e-13 m for positions on a 4 m domain)
+__device__ __forceinline__ float2 f2_diff(float bh, float bl, float ah, float al) {
     const float2 s = f2_two_sum(bh, -ah);
     return f2_two_sum(s.x, __fadd_rn(s.y, __fsub_rn(bl, al)));
 }

@@ -74,7 +74,7 @@ __global__ void k_relpos(Dev D) {
     const double x = D.x[r], y = D.y[r];
     D.xr[r] = (float)(x - cell_xleft(P, j));
     D.yr[r] = (float)(y - cell_ybot(P, i));
-    if (P.precision == BS_PREC_MIXED) D.pos4[r] = pos_split(x, y);
+    if (P.precision == BS_PREC_MIXED) D.pos4[r] = f2_split2(x, y);
 }
 
 template <typename T>
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         if (sizeof(T) == 4) {
             // mixed: the pair quantities are stored in FP32 and computed on
             // the FP32 pipe from double-float positions: the offset x_j - x_i
-            // (pos_diff, ~1e-13 m), r and 1/r (pair_r, r to ~2^-44 before
+            // (f2_diff, ~1e-13 m), r and 1/r (pair_r, r to ~2^-44 before
             // rounding) and 2 - r/h (near the cut-off the kernel gradient
             // goes as (2 - r/h)^2, so an FP32 r would put errors of 1e-4
             // relative into it); each stored value is the FP32 rounding of
@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 const long e = ell(r, k, kmax);
                 const int rj = D.nidx[e];
                 const float4 pj4 = __ldg(D.pos4 + rj);
-                const float2 dx = pos_diff(pj4.x, pj4.y, pi4.x, pi4.y);
-                const float2 dy = pos_diff(pj4.z, pj4.w, pi4.z, pi4.w);
+                const float2 dx = f2_diff(pj4.x, pj4.y, pi4.x, pi4.y);
+                const float2 dy = f2_diff(pj4.z, pj4.w, pi4.z, pi4.w);
                 const PairR pr = pair_r(dx, dy);
                 const float fx = dx.x, fy = dy.x;
                 const float rad = pr.rh, ir = pr.ir;
@@ -280,8 +280,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                             // mixed: FP32 (W(2h) = 0: the cut needs no exact
                             // test), the offset from the double-float positions
                             const float4 g4 = __ldg(D.gpos4 + g);
-                            const float ex = pos_diff(pi4.x, pi4.y, g4.x, g4.y).x;
-                            const float ey = pos_diff(pi4.z, pi4.w, g4.z, g4.w).x;
+                            const float ex = f2_diff(pi4.x, pi4.y, g4.x, g4.y).x;
+                            const float ey = f2_diff(pi4.z, pi4.w, g4.z, g4.w).x;
                             const float s2 = ex * ex + ey * ey;
                             if (s2 < t2c) {
                                 float rad = 0.0f;   // grains may coincide with pore particles
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
             const int j = D.nidx[e];
             const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
             const float4 qj = __ldg(D.rec0 + j);
-            const float a = pos_diff(qj.x, qj.y, q4.x, q4.y).x, b = pos_diff(qj.z, qj.w, q4.z, q4.w).x;
+            const float a = f2_diff(qj.x, qj.y, q4.x, q4.y).x, b = f2_diff(qj.z, qj.w, q4.z, q4.w).x;
             const float V = __ldg(D.rec1 + j).x;
             const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
             t1 += V * a * Lx;
@@ -495,10 +495,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
             const float pvol = wj.x;
             const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
             const float4 pj4 = __ldg(D.pos4 + j), vj4 = __ldg(D.rec0 + j);
-            const float dxi = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dyi = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+            const float dxi = f2_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dyi = f2_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
             const float gg = 2.0f * pvol * (dxi * Lx + dyi * Ly) * pd;
-            const float ax = pos_diff(vi4.x, vi4.y, vj4.x, vj4.y).x * gg;
-            const float ay = pos_diff(vi4.z, vi4.w, vj4.z, vj4.w).x * gg;
+            const float ax = f2_diff(vi4.x, vi4.y, vj4.x, vj4.y).x * gg;
+            const float ay = f2_diff(vi4.z, vi4.w, vj4.z, vj4.w).x * gg;
             kx.add(ax * (cmu + vart));
             ky.add(ay * (cmu + vart));
             if (tj > 2) {
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
                 kx.add(ax * mix);
                 ky.add(ay * mix);
             }
-            const float tk = pvol * pos_diff(kj.x, kj.y, ki4.x, ki4.y).x;
+            const float tk = pvol * f2_diff(kj.x, kj.y, ki4.x, ki4.y).x;
             kx.add(-(tk * Lx * phif * two3f));
             ky.add(-(tk * Ly * phif * two3f));
         }
@@ -587,7 +587,7 @@ __global__ void k_quot(Dev D, int mode) {
     const int r = R.r;
     const double phi = D.por[r];
     const bool mixed = D.par[R.s].precision == BS_PREC_MIXED;
-    if (mixed && (mode == 0 || mode == 3 || mode == 4)) D.pos4[r] = pos_split(D.x[r], D.y[r]);
+    if (mixed && (mode == 0 || mode == 3 || mode == 4)) D.pos4[r] = f2_split2(D.x[r], D.y[r]);
     switch (mode) {
     case 0: {
         const double ip = 1.0 / phi;
@@ -597,8 +597,8 @@ __global__ void k_quot(Dev D, int mode) {
         D.qw[r] = qw;
         D.qi[r] = ip;
         if (mixed) {
-            D.rec0[r] = pos_split(qu, qw);
-            D.rec1[r] = pos_split(D.vxs[r], D.vys[r]);
+            D.rec0[r] = f2_split2(qu, qw);
+            D.rec1[r] = f2_split2(D.vxs[r], D.vys[r]);
             D.rec2[r] = make_float4((float)qa, (float)D.vol[r], (float)D.oden[r], 0.0f);
         }
         break;
@@ -608,7 +608,7 @@ __global__ void k_quot(Dev D, int mode) {
         D.qu[r] = qu;
         D.qw[r] = qw;
         if (mixed) {
-            D.rec0[r] = pos_split(qu, qw);
+            D.rec0[r] = f2_split2(qu, qw);
             D.rec1[r] = make_float4((float)D.vol[r], 0.0f, 0.0f, 0.0f);
         }
         break;
@@ -621,7 +621,7 @@ __global__ void k_quot(Dev D, int mode) {
     }
     case 3: {
         const double nut = D.nut[r];
-        D.rec0[r] = pos_split(D.vx[r], D.vy[r]);
+        D.rec0[r] = f2_split2(D.vx[r], D.vy[r]);
         const float2 tk = f2_split(D.tke[r]);
         D.rec1[r] = make_float4(tk.x, tk.y, (float)nut, (float)D.nu[r]);
         D.rec2[r] = make_float4((float)D.vol[r], (float)D.varts[r], nut < BS_SP1EM6 ? 1.0f : 0.0f, 0.0f);
@@ -634,7 +634,7 @@ __global__ void k_quot(Dev D, int mode) {
         break;
     }
     case 5: {
-        D.rec0[r] = pos_split(D.vx[r], D.vy[r]);
+        D.rec0[r] = f2_split2(D.vx[r], D.vy[r]);
         D.rec1[r] = make_float4((float)D.vol[r], 0.0f, 0.0f, 0.0f);
         break;
     }
@@ -672,8 +672,8 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
         const float pd = ld<float>(D.nrinv, e);
         const int tj = D.tid[j];
         const float4 pj4 = __ldg(D.pos4 + j);
-        const float dxi = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x;   // x_i - x_j
-        const float dyi = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+        const float dxi = f2_diff(pi4.x, pi4.y, pj4.x, pj4.y).x;   // x_i - x_j
+        const float dyi = f2_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
         float off = 0.0f;
         if (ti == BS_TID_FLUID) {
             const float4 aj4 = __ldg(D.rec2 + j);
@@ -688,12 +688,12 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
                 const float aj = aj4.x;
                 const float rho_ij = 2.0f * aj * ai / (aj + ai);
                 const float4 uj = __ldg(D.rec0 + j);
-                ax = rho_ij * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
-                ay = rho_ij * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
+                ax = rho_ij * f2_diff(uj.x, uj.y, ui.x, ui.y).x;
+                ay = rho_ij * f2_diff(uj.z, uj.w, ui.z, ui.w).x;
             } else {
                 const float4 vj = __ldg(D.rec1 + j);
-                ax = bi * pos_diff(vj.x, vj.y, vi.x, vi.y).x;
-                ay = bi * pos_diff(vj.z, vj.w, vi.z, vi.w).x;
+                ax = bi * f2_diff(vj.x, vj.y, vi.x, vi.y).x;
+                ay = bi * f2_diff(vj.z, vj.w, vi.z, vi.w).x;
             }
             fv.add(pvol * (ax * Lx + ay * Ly));
         } else if (ti == BS_TID_GHOST) {
@@ -712,8 +712,8 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
                 // a_j (u_j/phi_j - vxs_i/phi_i): vxs_i/phi_i is the row's own u/phi
                 const float aj = __ldg(D.rec2 + j).x;
                 const float4 uj = __ldg(D.rec0 + j);
-                const float ax = aj * pos_diff(uj.x, uj.y, ui.x, ui.y).x;
-                const float ay = aj * pos_diff(uj.z, uj.w, ui.z, ui.w).x;
+                const float ax = aj * f2_diff(uj.x, uj.y, ui.x, ui.y).x;
+                const float ay = aj * f2_diff(uj.z, uj.w, ui.z, ui.w).x;
                 fv.add(voli * (ax * Lx + ay * Ly));
             } else {
                 const float t12 = 2.0f * __ldg(D.rec2 + j).y * (z1 * dxi + z2 * dyi) * pd;
@@ -976,7 +976,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
             sys += z2 * V;
             const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
             const float4 vj4 = __ldg(D.rec0 + j);
-            const float du = pos_diff(vj4.x, vj4.y, vi4.x, vi4.y).x, dv = pos_diff(vj4.z, vj4.w, vi4.z, vi4.w).x;
+            const float du = f2_diff(vj4.x, vj4.y, vi4.x, vi4.y).x, dv = f2_diff(vj4.z, vj4.w, vi4.z, vi4.w).x;
             a1 += Lx * du * V;
             a2 += Ly * du * V;
             b1 += Lx * dv * V;
@@ -1122,7 +1122,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_scalar(Dev D, int substep, const
             const float pj = sj.z;
             const float dm = ld<float>(D.ndist, e);
             const float4 pj4 = __ldg(D.pos4 + j);
-            const float dx = pos_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dy = pos_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+            const float dx = f2_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dy = f2_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
             float t1x;
             if (psmall && (bits & 1)) {
                 const float4 dj = __ldg(D.rec0 + j);
