@@ -580,14 +580,16 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
 //   mode 4 (scalar sub-step, mixed only): rec0 = (Dp0, Dp1, Dp2, Dp3),
 //     rec1 = (Dt, con, phi, (phi < 0.7) + 2 (nut < 1e-6))
 //   mode 5 (opt2_shift, mixed only): rec0 = (vx, vy) pairs, rec1.x = m/rho
-// Modes 0, 3 and 4 also refresh the double-float positions.
+//   mode 6 (WCSPH continuity, mixed only): rec0 = (vx, vy) pairs,
+//     rec1 = (rho, hydrostatic density) pairs, rec2.x = m
+// Modes 0, 3, 4 and 6 also refresh the double-float positions.
 __global__ void k_quot(Dev D, int mode) {
     const RowCtx R = row_ctx(D);
     if (!R.active) return;
     const int r = R.r;
     const double phi = D.por[r];
     const bool mixed = D.par[R.s].precision == BS_PREC_MIXED;
-    if (mixed && (mode == 0 || mode == 3 || mode == 4)) D.pos4[r] = f2_split2(D.x[r], D.y[r]);
+    if (mixed && (mode == 0 || mode == 3 || mode == 4 || mode == 6)) D.pos4[r] = f2_split2(D.x[r], D.y[r]);
     switch (mode) {
     case 0: {
         const double ip = 1.0 / phi;
@@ -636,6 +638,12 @@ __global__ void k_quot(Dev D, int mode) {
     case 5: {
         D.rec0[r] = f2_split2(D.vx[r], D.vy[r]);
         D.rec1[r] = make_float4((float)D.vol[r], 0.0f, 0.0f, 0.0f);
+        break;
+    }
+    case 6: {
+        D.rec0[r] = f2_split2(D.vx[r], D.vy[r]);
+        D.rec1[r] = f2_split2(D.rho[r], D.whyd[r]);
+        D.rec2[r] = make_float4((float)D.mass[r], 0.0f, 0.0f, 0.0f);
         break;
     }
     }
@@ -1220,6 +1228,38 @@ __global__ void __launch_bounds__(BS_THREADS) k_wc_continuity(Dev D) {
     const double dfac = ((delt * 2) * h1) * co;
     double term1 = 0.0, term2 = 0.0;
     const int n = D.ncount[r];
+    if (sizeof(T) == 4) {
+        // mixed: the neighbours' velocities, densities and hydrostatic
+        // densities as (hi, lo) pairs and masses from the k_quot records, the
+        // pair offsets from the double-float positions, each cancelling
+        // difference rounded once to FP32; the pair terms on the FP32 pipe,
+        // the sums compensated
+        const float4 pi4 = D.pos4[r], vi4 = D.rec0[r], di4 = D.rec1[r];
+        const float c0f = (float)c0, c1f = (float)c1, c2f = (float)c2, c3f = (float)c3;
+        const float dfacf = (float)dfac, lamf = (float)lam, rhoif = di4.x;
+        const float sg = (P.wc_form == 0) ? 1.0f : -1.0f;
+        Kahan32 k1, k2;
+        for (int k = 0; k < n; ++k) {
+            const long e = ell(r, k, D.kmax);
+            const int j = D.nidx[e];
+            const float rad = ld<float>(D.ndist, e);
+            const float wx = ld<float>(D.nkx, e), wy = ld<float>(D.nky, e);
+            const float4 dj4 = __ldg(D.rec1 + j), vj4 = __ldg(D.rec0 + j), pj4 = __ldg(D.pos4 + j);
+            const float hd = f2_diff(dj4.z, dj4.w, di4.z, di4.w).x;
+            if (P.wc_form == 0) k2 = Kahan32{hd, 0.0f};
+            const float gx = c0f * wx + c1f * wy;
+            const float gy = c2f * wx + c3f * wy;
+            const float mj = __ldg(D.rec2 + j).x, rhoj = dj4.x;
+            const float vr = mj / rhoj, den = rad * rad + lamf;
+            const float drho = f2_diff(dj4.x, dj4.y, di4.x, di4.y).x - hd;
+            const float dxi = f2_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dyi = f2_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
+            const float dvx = f2_diff(vj4.x, vj4.y, vi4.x, vi4.y).x, dvy = f2_diff(vj4.z, vj4.w, vi4.z, vi4.w).x;
+            k1.add(-(((mj * dvx) * gx) * (rhoif / rhoj)) + (((dfacf * drho) * (sg * dxi)) * gx) * vr / den);
+            k2.add(-(((mj * dvy) * gy) * (rhoif / rhoj)) + (((dfacf * drho) * (sg * dyi)) * gy) * vr / den);
+        }
+        D.tden[r] = rhoi + (k1.value() + k2.value()) * dt;
+        return;
+    }
     for (int k = 0; k < n; ++k) {
         const long e = ell(r, k, D.kmax);
         const int j = D.nidx[e];
@@ -1547,6 +1587,7 @@ void scalar(const Dev& D, const Launch& L, int precision, int substep, const int
 }
 void wc_continuity(const Dev& D, const Launch& L, int precision) {
     BS_PLAIN(K_WC_CONT, k_wc_hyd, D);
+    if (precision == BS_PREC_MIXED) BS_PLAIN(K_WC_CONT, k_quot, D, 6);
     BS_DISPATCH(K_WC_CONT, precision, k_wc_continuity, D);
 }
 void wc_rows(const Dev& D, const Launch& L, int mode) { BS_PLAIN(K_WC_ROWS, k_wc_rows, D, mode); }
