@@ -355,6 +355,13 @@ void fill_par(ScenePar& P, const bs_params& p, int kmax) {
     P.cn1 = 0.1 * (10.0 / (BS_C28 * (p.h * p.h)));
     P.cn2 = (1.0 - 0.1) * (1.0 / (BS_C3 * (p.h * p.h)));
     P.wo = 0.1 * 4.0 * (10.0 / (BS_C28 * (p.h * p.h))) + (1.0 - 0.1) * 6.0 * (1.0 / (BS_C3 * (p.h * p.h)));
+    const double kr = P.cn2 / P.cn1, k3 = 3.0 * (1.0 + kr);
+    P.kq_s = (float)(P.cn1 * P.inv_h2);
+    P.kq_rho_h = (float)kr;
+    P.kq_rho_l = (float)(kr - (double)P.kq_rho_h);
+    P.kq_k3_h = (float)k3;
+    P.kq_k3_l = (float)(k3 - (double)P.kq_k3_h);
+    P.kq_pad = 0.0f;
     P.rho = p.rho; P.rhomin = p.rhomin; P.rhomax = p.rhomax; P.rel_den = p.rel_den; P.g = p.g;
     P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;
     P.freethr = p.lamfs * p.maxdivr; P.csh = p.csh; P.maxshift = p.maxshift; P.sig1 = p.sig1;

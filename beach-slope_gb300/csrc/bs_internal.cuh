@@ -53,6 +53,9 @@ struct ScenePar {                 // per-scene constants
     int adaptive_dt, scalar_on, precision, stop_rule;
     int nblk, blk0, max_outer, mg_lev;   // mg_lev: this scene's coarsest multigrid level
     int grp0, pad_grp;                    // first group of 32 row blocks (two-level reductions)
+    // the kernel gradient on the FP32 pipe as F = kq_s g(q), q = r/h:
+    // kq_s = fl32(cn1/h^2), (hi, lo) pairs of cn2/cn1 and 3 (1 + cn2/cn1)
+    float kq_s, kq_rho_h, kq_rho_l, kq_k3_h, kq_k3_l, kq_pad;
 };
 
 struct SceneDyn {                 // per-scene dynamic state (device)
@@ -373,6 +376,42 @@ __device__ __forceinline__ PairR pair_r(float2 dx, float2 dy) {
 __device__ __forceinline__ bool f2_less(float rh, float rl, float ch, float cl) {
     return rh < ch || (rh == ch && rl < cl);
 }
+// Double-float arithmetic on (hi, lo) pairs (relative error ~2^-44; the
+// lo * lo terms are below it)
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return f2_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 f2_mulf(float2 a, float b) {
+    const float p = __fmul_rn(a.x, b);
+    return f2_fast_two_sum(p, __fmaf_rn(a.y, b, __fmaf_rn(a.x, b, -p)));
+}
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+    const float2 s = f2_two_sum(a.x, b.x);
+    return f2_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+// 1/a by one Newton step from the FP32 reciprocal
+__device__ __forceinline__ float2 f2_rcp(float2 a) {
+    const float y = __frcp_rn(a.x);
+    const float e = __fmaf_rn(-a.y, y, __fmaf_rn(-a.x, y, 1.0f));
+    return f2_fast_two_sum(y, __fmul_rn(y, e));
+}
+// fl32(a b) of two double-float values (one rounding up to ties)
+__device__ __forceinline__ float f2_prod_rn(float2 a, float2 b) {
+    return __fmaf_rn(a.x, b.x, __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+}
+// a += k (rh + re) for a double-float accumulator a, an FP32 k and a
+// double-float (rh, re): the product's rounding error kept in the lo part
+__device__ __forceinline__ void f2_acc_prod(float2& a, float k, float rh, float re) {
+    const float th = __fmul_rn(k, rh);
+    const float te = __fmaf_rn(k, re, __fmaf_rn(k, rh, -th));
+    const float2 t = f2_two_sum(a.x, th);
+    a.x = t.x;
+    a.y = __fadd_rn(a.y, __fadd_rn(t.y, te));
+}
 // fl32(2 - r * ih) for a double-float r and ih = (ihh, ihl), r ih in [1, 2]
 // (2 - p exact by Sterbenz)
 __device__ __forceinline__ float f2_two_minus_prod(float rh, float rl, float ihh, float ihl) {
@@ -410,6 +449,36 @@ __device__ __forceinline__ float bs_Ff(float r, const KerF& K) {
 __device__ __forceinline__ double bs_vis(double oden) {
     const double Sp = oden - 1000.0;
     return (1.002 + 0.001652 * Sp + 0.0000083 * (Sp * Sp)) * 0.001;
+}
+
+// A row's gradient-correction matrix C as (hi, lo) pairs for the FP32 pipe:
+// a corrected gradient component c_a z1 + c_b z2 with the lo parts added, so
+// that its one FP32 error is the rounding of the pair's own value.  C rounded
+// to FP32 once per row would give every pair of the row the same relative
+// error, which the row's sums (divergences, matrix entries) carry whole.
+struct CorrF {
+    float c0h, c0l, c1h, c1l, c2h, c2l, c3h, c3l;
+    __device__ __forceinline__ float lx(float z1, float z2) const {
+        return __fmaf_rn(c0h, z1, __fmaf_rn(c1h, z2, __fmaf_rn(c0l, z1, __fmul_rn(c1l, z2))));
+    }
+    __device__ __forceinline__ float ly(float z1, float z2) const {
+        return __fmaf_rn(c2h, z1, __fmaf_rn(c3h, z2, __fmaf_rn(c2l, z1, __fmul_rn(c3l, z2))));
+    }
+    // the same components as (hi, lo) pairs
+    __device__ __forceinline__ float2 lx2(float z1, float z2) const { return comp(c0h, c0l, c1h, c1l, z1, z2); }
+    __device__ __forceinline__ float2 ly2(float z1, float z2) const { return comp(c2h, c2l, c3h, c3l, z1, z2); }
+    __device__ __forceinline__ static float2 comp(float ah, float al, float bh, float bl, float z1, float z2) {
+        const float p1 = __fmul_rn(ah, z1), p2 = __fmul_rn(bh, z2);
+        const float2 s = f2_two_sum(p1, p2);
+        float lo = __fmaf_rn(ah, z1, -p1);
+        lo = __fadd_rn(lo, __fmaf_rn(bh, z2, -p2));
+        lo = __fmaf_rn(al, z1, __fmaf_rn(bl, z2, __fadd_rn(lo, s.y)));
+        return f2_fast_two_sum(s.x, lo);
+    }
+};
+__device__ __forceinline__ CorrF corr_f(const Dev& D, int r) {
+    const float2 a = f2_split(D.c0[r]), b = f2_split(D.c1[r]), c = f2_split(D.c2[r]), d = f2_split(D.c3[r]);
+    return CorrF{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y};
 }
 
 __device__ __forceinline__ void set_err(const Dev& D, int s, unsigned bits) {

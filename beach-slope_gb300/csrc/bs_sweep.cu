@@ -155,14 +155,28 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             // mixed: the pair quantities are stored in FP32 and computed on
             // the FP32 pipe from double-float positions: the offset x_j - x_i
             // (f2_diff, ~1e-13 m), r and 1/r (pair_r, r to ~2^-44 before
-            // rounding) and 2 - r/h (near the cut-off the kernel gradient
-            // goes as (2 - r/h)^2, so an FP32 r would put errors of 1e-4
-            // relative into it); each stored value is the FP32 rounding of
-            // the FP64 one up to ties.  The correction sums are compensated
-            // FP32 sums.
-            Kahan32 f00, f01, f10, f11;
-            const float ihf = (float)P.inv_h, ih2f = (float)P.inv_h2, ih3f = (float)P.inv_h3;
-            const float c1f = (float)P.cn1, c2f = (float)P.cn2;
+            // rounding); r and 1/(r^2 + lam) are the FP32 roundings of the
+            // FP64 values up to ties.  The kernel gradient is F = S g(q),
+            // q = r/h, with one FP32 scale S = cn1/h^2:
+            //   q < 1: g = (9q - 12) + (cn2/cn1)(3q - 6/q)
+            //   q >= 1: g = -3 (1 + cn2/cn1) (2 - q)^2 / q
+            // g in double-float arithmetic (q, 1/q and the ratios as (hi, lo)
+            // pairs) and each stored component F (x_i - x_j) rounded once.
+            // Wall particles sit on a lattice and fluid particles stay near
+            // one, so many pairs share an offset and the same rounding: FP32
+            // arithmetic in F would act as a small change of the kernel's
+            // shape, which no sum averages out (~1e-6 in the pressure of
+            // coarse scenes); so would FP32 constants per term (1/h, 1/h^2,
+            // 1/h^3, cn1, cn2 each rounded).  S is the same for every
+            // gradient of the scene: it cancels in the corrected gradients
+            // and the Jacobi-scaled rows and elsewhere acts as one rounded
+            // constant.  The correction sums take the stored components times
+            // V (x_j - x_i) with the products' rounding errors kept
+            // (double-float accumulators): the correction matrix multiplies
+            // every pair of the row, so its errors do not average out either.
+            float2 s00 = make_float2(0.f, 0.f), s01 = s00, s10 = s00, s11 = s00;
+            const float kqs = P.kq_s;
+            const float2 kr = make_float2(P.kq_rho_h, P.kq_rho_l), k3 = make_float2(P.kq_k3_h, P.kq_k3_l);
             const float2 hf = f2_split(P.h), ihd = f2_split(P.inv_h);
             const float lamf = (float)P.lam;
             const float4 pi4 = D.pos4[r];
@@ -173,32 +187,42 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 const float2 dx = f2_diff(pj4.x, pj4.y, pi4.x, pi4.y);
                 const float2 dy = f2_diff(pj4.z, pj4.w, pi4.z, pi4.w);
                 const PairR pr = pair_r(dx, dy);
-                const float fx = dx.x, fy = dy.x;
-                const float rad = pr.rh, ir = pr.ir;
+                const float rad = pr.rh;
                 const float rinv = __frcp_rn(pr.sh + lamf);
-                float F;
+                const float2 q = f2_mul(make_float2(pr.rh, pr.rl), ihd);
+                const float2 iq = f2_rcp(q);
+                float2 g;
                 if (f2_less(pr.rh, pr.rl, hf.x, hf.y)) {
-                    F = c1f * (9.0f * rad * ih3f - 12.0f * ih2f) + c2f * (3.0f * rad * ih3f - 6.0f * ihf * ir);
+                    const float2 t1 = f2_add(f2_mulf(q, 9.0f), make_float2(-12.0f, 0.0f));
+                    const float2 t2 = f2_add(f2_mulf(q, 3.0f), f2_mulf(iq, -6.0f));
+                    g = f2_add(t1, f2_mul(kr, t2));
                 } else {
-                    const float a = f2_two_minus_prod(pr.rh, pr.rl, ihd.x, ihd.y);
-                    F = -(c1f + c2f) * (3.0f * ihf * ir) * a * a;
+                    const float2 s = f2_two_sum(2.0f, -q.x);   // exact: q in [1, 2]
+                    const float2 a = f2_fast_two_sum(s.x, __fsub_rn(s.y, q.y));
+                    g = f2_mul(k3, f2_mul(f2_mul(a, a), iq));
+                    g = make_float2(-g.x, -g.y);
                 }
-                const float kx = F * (-fx), ky = F * (-fy);
+                const float2 F = f2_mulf(g, kqs);
+                const float kx = -f2_prod_rn(F, dx), ky = -f2_prod_rn(F, dy);
                 st<T>(D.ndist, e, (T)rad);
                 st<T>(D.nrinv, e, (T)rinv);
                 st<T>(D.nkx, e, (T)kx);
                 st<T>(D.nky, e, (T)ky);
-                const float vj = (float)D.vol[rj];
-                const float res1 = vj * fx, res3 = vj * fy;
-                f00.add(kx * res1);
-                f01.add(ky * res1);
-                f10.add(kx * res3);
-                f11.add(ky * res3);
+                // V (dx hi + dx lo) as (hi, lo) from V as (hi, lo)
+                const float2 vj = f2_split(D.vol[rj]);
+                const float r1h = __fmul_rn(vj.x, dx.x);
+                const float r1e = __fmaf_rn(vj.y, dx.x, __fmaf_rn(vj.x, dx.y, __fmaf_rn(vj.x, dx.x, -r1h)));
+                const float r3h = __fmul_rn(vj.x, dy.x);
+                const float r3e = __fmaf_rn(vj.y, dy.x, __fmaf_rn(vj.x, dy.y, __fmaf_rn(vj.x, dy.x, -r3h)));
+                f2_acc_prod(s00, kx, r1h, r1e);
+                f2_acc_prod(s01, ky, r1h, r1e);
+                f2_acc_prod(s10, kx, r3h, r3e);
+                f2_acc_prod(s11, ky, r3h, r3e);
             }
-            a00 = f00.value();
-            a01 = f01.value();
-            a10 = f10.value();
-            a11 = f11.value();
+            a00 = (double)s00.x + (double)s00.y;
+            a01 = (double)s01.x + (double)s01.y;
+            a10 = (double)s10.x + (double)s10.y;
+            a11 = (double)s11.x + (double)s11.y;
         }
         for (int k = 0; k < (sizeof(T) == 4 ? 0 : n); ++k) {
             const long e = ell(r, k, kmax);
@@ -387,6 +411,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
         // mixed: the neighbours' u/phi, w/phi as (hi, lo) pairs and volumes
         // from the k_quot records, the differences rounded once to FP32
         const float4 q4 = D.rec0[r];
+        const CorrF cf = corr_f(D, r);
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
             const int j = D.nidx[e];
@@ -394,7 +419,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_eddy(Dev D, int with_eddy, int w
             const float4 qj = __ldg(D.rec0 + j);
             const float a = f2_diff(qj.x, qj.y, q4.x, q4.y).x, b = f2_diff(qj.z, qj.w, q4.z, q4.w).x;
             const float V = __ldg(D.rec1 + j).x;
-            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float Lx = cf.lx(z1, z2), Ly = cf.ly(z1, z2);
             t1 += V * a * Lx;
             t2 += V * b * Ly;
             t3 += 0.5f * V * (a * Ly + b * Lx);
@@ -474,6 +499,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
         const bool nutis = nuti < BS_SP1EM6;
         const float iwo = (float)(1.0 / P.wo), phif = (float)phi, two3f = (float)(2.0 / 3);
         const KerF KF = ker_f(P);
+        const CorrF cf = corr_f(D, r);
         Kahan32 kx, ky;
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
@@ -493,7 +519,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_intvel(Dev D) {
             if (freei) vart = vartsif;
             else if (D.flags[j] & BS_FLAG_FREE) vart = bs_Wf(ld<float>(D.ndist, e), KF) * wj.y * iwo;
             const float pvol = wj.x;
-            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float Lx = cf.lx(z1, z2), Ly = cf.ly(z1, z2);
             const float4 pj4 = __ldg(D.pos4 + j), vj4 = __ldg(D.rec0 + j);
             const float dxi = f2_diff(pi4.x, pi4.y, pj4.x, pj4.y).x, dyi = f2_diff(pi4.z, pi4.w, pj4.z, pj4.w).x;
             const float gg = 2.0f * pvol * (dxi * Lx + dyi * Ly) * pd;
@@ -652,10 +678,14 @@ __global__ void k_quot(Dev D, int mode) {
 // The mixed form of the assembly: the same entries and right-hand side on
 // the FP32 pipe.  Pair offsets and the cancelling differences (u/phi, w/phi,
 // vxs, vys of the pair) are taken from double-float copies (pos4 and the
-// k_quot records: the FP32 rounding of the FP64 difference), the products in FP32,
-// the diagonal and the right-hand side as compensated sums; the Jacobi
-// scaling writes the FP64 values and their double-float split (aval32 +
-// aval_lo) for the solver.
+// k_quot records), the matrix entries in FP32 with a compensated diagonal.
+// The right-hand side is a divergence: its pair terms cancel to a small sum,
+// which would carry each term's FP32 rounding many times over, so each term
+// (the velocity difference and the corrected gradient as (hi, lo) pairs, their
+// dot product) is double-float and so is the sum; the density and volume
+// factors, smooth over a row's pairs, stay FP32.  The Jacobi scaling writes
+// the FP64 values and their double-float split (aval32 + aval_lo) for the
+// solver.
 __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
     const ScenePar& P = D.par[R.s];
     const int r = R.r;
@@ -665,14 +695,15 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
     const float4 ui = D.rec0[r], vi = D.rec1[r];
     const float ai = D.rec2[r].x;                       // rho_i/phi_i
     const float bi = (float)(D.qa[r] * D.qi[r]);          // rho_i/phi_i^2
-    const float c0 = (float)D.c0[r], c1 = (float)D.c1[r], c2 = (float)D.c2[r], c3 = (float)D.c3[r];
+    const CorrF cf = corr_f(D, r);
     const bool freei = fl & BS_FLAG_FREE;
     const float lampf = (float)(1.0 / (P.rho * P.rel_den));
     const float voli = ti == BS_TID_WALL ? (float)(D.mass[r] / D.rho[r]) : 0.0f;
     const int n = D.ncount[r];
     const int kmax = D.kmax;
     float* a32 = D.aval32;
-    Kahan32 dia, fv;
+    Kahan32 dia;
+    float2 fv = make_float2(0.0f, 0.0f);
     for (int k = 0; k < n; ++k) {
         const long e = ell(r, k, kmax);
         const int j = D.nidx[e];
@@ -687,23 +718,23 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
             const float4 aj4 = __ldg(D.rec2 + j);
             const float lamp = (freei && tj == BS_TID_FLUID) ? (1.0f + aj4.z * lampf) : 1.0f;
             const float pvol = aj4.y;
-            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
-            const float t12 = 2.0f * pvol * (Lx * dxi + Ly * dyi) * pd;
+            const float2 Lx = cf.lx2(z1, z2), Ly = cf.ly2(z1, z2);
+            const float t12 = 2.0f * pvol * (Lx.x * dxi + Ly.x * dyi) * pd;
             off = -t12;
             dia.add(t12 * lamp);
-            float ax, ay;
+            float2 ax, ay;
             if (tj == BS_TID_FLUID) {
                 const float aj = aj4.x;
                 const float rho_ij = 2.0f * aj * ai / (aj + ai);
                 const float4 uj = __ldg(D.rec0 + j);
-                ax = rho_ij * f2_diff(uj.x, uj.y, ui.x, ui.y).x;
-                ay = rho_ij * f2_diff(uj.z, uj.w, ui.z, ui.w).x;
+                ax = f2_mulf(f2_diff(uj.x, uj.y, ui.x, ui.y), rho_ij);
+                ay = f2_mulf(f2_diff(uj.z, uj.w, ui.z, ui.w), rho_ij);
             } else {
                 const float4 vj = __ldg(D.rec1 + j);
-                ax = bi * f2_diff(vj.x, vj.y, vi.x, vi.y).x;
-                ay = bi * f2_diff(vj.z, vj.w, vi.z, vi.w).x;
+                ax = f2_mulf(f2_diff(vj.x, vj.y, vi.x, vi.y), bi);
+                ay = f2_mulf(f2_diff(vj.z, vj.w, vi.z, vi.w), bi);
             }
-            fv.add(pvol * (ax * Lx + ay * Ly));
+            fv = f2_add(fv, f2_mulf(f2_add(f2_mul(ax, Lx), f2_mul(ay, Ly)), pvol));
         } else if (ti == BS_TID_GHOST) {
             if (tj <= 2) {
                 const float t12 = 2.0f * __ldg(D.rec2 + j).y * (z1 * dxi + z2 * dyi) * pd;
@@ -712,17 +743,17 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
             }
         } else if (ti == BS_TID_WALL) {
             if (tj == BS_TID_FLUID) {
-                const float d0 = (float)D.c0[j], d1 = (float)D.c1[j], d2 = (float)D.c2[j], d3 = (float)D.c3[j];
-                const float Lx = d0 * z1 + d1 * z2, Ly = d2 * z1 + d3 * z2;
-                const float t12 = 2.0f * voli * (Lx * dxi + Ly * dyi) * pd;
+                const CorrF cj = corr_f(D, j);
+                const float2 Lx = cj.lx2(z1, z2), Ly = cj.ly2(z1, z2);
+                const float t12 = 2.0f * voli * (Lx.x * dxi + Ly.x * dyi) * pd;
                 off = -t12;
                 dia.add(t12);
                 // a_j (u_j/phi_j - vxs_i/phi_i): vxs_i/phi_i is the row's own u/phi
                 const float aj = __ldg(D.rec2 + j).x;
                 const float4 uj = __ldg(D.rec0 + j);
-                const float ax = aj * f2_diff(uj.x, uj.y, ui.x, ui.y).x;
-                const float ay = aj * f2_diff(uj.z, uj.w, ui.z, ui.w).x;
-                fv.add(voli * (ax * Lx + ay * Ly));
+                const float2 ax = f2_mulf(f2_diff(uj.x, uj.y, ui.x, ui.y), aj);
+                const float2 ay = f2_mulf(f2_diff(uj.z, uj.w, ui.z, ui.w), aj);
+                fv = f2_add(fv, f2_mulf(f2_add(f2_mul(ax, Lx), f2_mul(ay, Ly)), voli));
             } else {
                 const float t12 = 2.0f * __ldg(D.rec2 + j).y * (z1 * dxi + z2 * dyi) * pd;
                 off = -t12;
@@ -740,7 +771,7 @@ __device__ __forceinline__ void assemble_mixed(const Dev& D, const RowCtx& R) {
     if (!(dd != 0.0) || !isfinite(dd)) set_err(D, R.s, BS_ERR_ZERO_DIAG);
     const double inv = fast_rcp64(dd);
     D.adiag[r] = dd / dd + extra * inv;
-    D.rhs[r] = fv.value() * fast_rcp64(D.dyn[R.s].dt) * inv;
+    D.rhs[r] = ((double)fv.x + (double)fv.y) * fast_rcp64(D.dyn[R.s].dt) * inv;
     // Jacobi scaling: FP64 values for the FP64 residuals, and the
     // double-float split off * (inv hi + inv lo) for the solver's SpMV
     const float2 invd = f2_split(inv);
@@ -886,13 +917,14 @@ __global__ void __launch_bounds__(BS_THREADS) k_compvel(Dev D, int do_vel, int d
                 // k_quot records, the pair terms on the FP32 pipe, the
                 // pressure-gradient sums (which cancel) compensated
                 const float pif = (float)pi, aif = (float)ai, qff = (float)qf, phi2f = (float)(phi * phi);
+                const CorrF cf = corr_f(D, r);
                 const float rhoif = (float)rhoi;
                 Kahan32 kx, ky;
                 for (int k = 0; k < n; ++k) {
                     const long e = ell(r, k, kmax);
                     const int j = D.nidx[e];
                     const float z1 = ld<float>(D.nkx, e), z2 = ld<float>(D.nky, e);
-                    const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+                    const float Lx = cf.lx(z1, z2), Ly = cf.ly(z1, z2);
                     const float4 qj = __ldg(D.rec0 + j);   // (p, rho/phi, m/rho)
                     float q;
                     if (D.tid[j] == BS_TID_FLUID) q = qff * qj.z * (qj.x * aif + pif * qj.y) / (aif + qj.y);
@@ -975,6 +1007,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
         // mixed: the neighbours' velocities as (hi, lo) pairs and volumes
         // from the k_quot records, the differences rounded once to FP32
         const float4 vi4 = D.rec0[r];
+        const CorrF cf = corr_f(D, r);
         for (int k = 0; k < n; ++k) {
             const long e = ell(r, k, kmax);
             const int j = D.nidx[e];
@@ -982,7 +1015,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_shift(Dev D) {
             const float V = __ldg(D.rec1 + j).x;
             sxs += z1 * V;
             sys += z2 * V;
-            const float Lx = c0 * z1 + c1 * z2, Ly = c2 * z1 + c3 * z2;
+            const float Lx = cf.lx(z1, z2), Ly = cf.ly(z1, z2);
             const float4 vj4 = __ldg(D.rec0 + j);
             const float du = f2_diff(vj4.x, vj4.y, vi4.x, vi4.y).x, dv = f2_diff(vj4.z, vj4.w, vi4.z, vi4.w).x;
             a1 += Lx * du * V;
@@ -1235,7 +1268,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_wc_continuity(Dev D) {
         // difference rounded once to FP32; the pair terms on the FP32 pipe,
         // the sums compensated
         const float4 pi4 = D.pos4[r], vi4 = D.rec0[r], di4 = D.rec1[r];
-        const float c0f = (float)c0, c1f = (float)c1, c2f = (float)c2, c3f = (float)c3;
+        const CorrF cf = corr_f(D, r);
         const float dfacf = (float)dfac, lamf = (float)lam, rhoif = di4.x;
         const float sg = (P.wc_form == 0) ? 1.0f : -1.0f;
         Kahan32 k1, k2;
@@ -1247,8 +1280,8 @@ __global__ void __launch_bounds__(BS_THREADS) k_wc_continuity(Dev D) {
             const float4 dj4 = __ldg(D.rec1 + j), vj4 = __ldg(D.rec0 + j), pj4 = __ldg(D.pos4 + j);
             const float hd = f2_diff(dj4.z, dj4.w, di4.z, di4.w).x;
             if (P.wc_form == 0) k2 = Kahan32{hd, 0.0f};
-            const float gx = c0f * wx + c1f * wy;
-            const float gy = c2f * wx + c3f * wy;
+            const float gx = cf.lx(wx, wy);
+            const float gy = cf.ly(wx, wy);
             const float mj = __ldg(D.rec2 + j).x, rhoj = dj4.x;
             const float vr = mj / rhoj, den = rad * rad + lamf;
             const float drho = f2_diff(dj4.x, dj4.y, di4.x, di4.y).x - hd;
