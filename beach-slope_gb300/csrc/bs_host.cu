@@ -617,7 +617,7 @@ int bs_create(int32_t nscenes, const bs_params* params, const int32_t* capacity,
     A(gx, (size_t)gr); A(gy, (size_t)gr); A(gv, (size_t)gr); A(gcell_start, C); A(gcell_end, C);
     A(gxr, (size_t)gr); A(gyr, (size_t)gr); A(gpos4, (size_t)gr); A(xr, R); A(yr, R);
     if (ctx->precision == BS_PREC_MIXED) {
-        A(pos4, R); A(rec0, R); A(rec1, R); A(rec2, R);
+        A(pos4, R); A(rec0, R); A(rec1, R); A(rec2, R); A(volf2, R); A(cfa, R); A(cfb, R);
     }
     A(part, (size_t)blk * BS_MAXDOT);
     A(err_word, 1);

@@ -152,6 +152,7 @@ struct Dev {
     // per-particle properties (recomputed after every re-bin)
     double *por, *resx, *resy, *nut, *tke, *varts, *gradvx, *vel, *cdiff;
     double *c0, *c1, *c2, *c3;      // coff (L^-1), search.f90:276-278
+    float4 *cfa, *cfb;              // mixed: the same as (hi, lo) FP32 pairs, (c0, c1) and (c2, c3), written by k_search
     double *Dp0, *Dp1, *Dp2, *Dp3, *Dt;   // scalar dispersion per particle
     double *rho_new, *vol_new;      // effpor output (ping-pong with rho/vol)
     double *tden, *whyd;            // WCSPH: continuity density, hydrostatic Tait density per row
@@ -160,6 +161,7 @@ struct Dev {
     // row by k_quot right before the sweep (the layout of each sweep is at
     // k_quot); fields whose pair differences cancel as (hi, lo) FP32 pairs
     float4 *rec0, *rec1, *rec2;
+    float2* volf2;                  // mixed: volume as an (hi, lo) FP32 pair, written by k_relpos for k_search
     double *con_new;
     // neighbour lists (ELL)
     int* ncount;
@@ -476,9 +478,10 @@ struct CorrF {
         return f2_fast_two_sum(s.x, lo);
     }
 };
+// C of row r from the (hi, lo) pairs the mixed search writes
 __device__ __forceinline__ CorrF corr_f(const Dev& D, int r) {
-    const float2 a = f2_split(D.c0[r]), b = f2_split(D.c1[r]), c = f2_split(D.c2[r]), d = f2_split(D.c3[r]);
-    return CorrF{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y};
+    const float4 a = __ldg(D.cfa + r), b = __ldg(D.cfb + r);
+    return CorrF{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
 
 __device__ __forceinline__ void set_err(const Dev& D, int s, unsigned bits) {

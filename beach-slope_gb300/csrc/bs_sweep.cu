@@ -74,7 +74,10 @@ __global__ void k_relpos(Dev D) {
     const double x = D.x[r], y = D.y[r];
     D.xr[r] = (float)(x - cell_xleft(P, j));
     D.yr[r] = (float)(y - cell_ybot(P, i));
-    if (P.precision == BS_PREC_MIXED) D.pos4[r] = f2_split2(x, y);
+    if (P.precision == BS_PREC_MIXED) {
+        D.pos4[r] = f2_split2(x, y);
+        D.volf2[r] = f2_split(D.vol[r]);
+    }
 }
 
 template <typename T>
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 st<T>(D.nkx, e, (T)kx);
                 st<T>(D.nky, e, (T)ky);
                 // V (dx hi + dx lo) as (hi, lo) from V as (hi, lo)
-                const float2 vj = f2_split(D.vol[rj]);
+                const float2 vj = __ldg(D.volf2 + rj);
                 const float r1h = __fmul_rn(vj.x, dx.x);
                 const float r1e = __fmaf_rn(vj.y, dx.x, __fmaf_rn(vj.x, dx.y, __fmaf_rn(vj.x, dx.x, -r1h)));
                 const float r3h = __fmul_rn(vj.x, dy.x);
@@ -268,6 +271,11 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 c3 = a00 * id;
             }
             D.c0[r] = c0; D.c1[r] = c1; D.c2[r] = c2; D.c3[r] = c3;
+            if (sizeof(T) == 4) {
+                const float2 a = f2_split(c0), b = f2_split(c1), cc = f2_split(c2), d = f2_split(c3);
+                D.cfa[r] = make_float4(a.x, a.y, b.x, b.y);
+                D.cfb[r] = make_float4(cc.x, cc.y, d.x, d.y);
+            }
             if ((gv <= P.freethr) && !(fl & BS_FLAG_BUFFER)) fl |= BS_FLAG_FREE;
         }
         D.gradvx[r] = gv;
