@@ -25,7 +25,8 @@
 //  * Convergence is judged on the recursive residual, as bs_bicgstab_csr
 //    judges it; *relres reports the true residual ||b - A x|| / ||b||
 //    computed after the last iteration.  The flag is read back to the host
-//    every four iterations (the call waits for its stream there).
+//    every four iterations (the call waits for its stream there), so the
+//    call cannot run on a stream that is being captured.
 #include <cuda_runtime.h>
 
 #include <cmath>

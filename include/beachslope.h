@@ -445,7 +445,8 @@ int bs_fgmres_csr(int32_t n, const int32_t* row_ptr, const int32_t* col, const d
  * device current); make it before any stream capture.  Convergence is judged
  * on the recursive residual, as in bs_bicgstab_csr; *relres is the true
  * residual ||b - A x|| / ||b|| after the last iteration; the convergence flag
- * is read back every four iterations (the call waits for `stream` there).
+ * is read back every four iterations (the call waits for `stream` there), so
+ * the call must not be made on a stream that is being captured into a graph.
  * `stream` is a cudaStream_t (NULL: the default stream). */
 int bs_bicgstab_csr_noalloc(int32_t n, const int32_t* d_row_ptr, const int32_t* d_col, const double* d_val,
                             const double* d_b, double* d_x, double tol, int32_t maxit, void* stream,
