@@ -63,7 +63,10 @@ extern "C" {
 
 /* precision modes */
 #define BS_PREC_FP64   0   /* plain FP64 drop-in                                      */
-#define BS_PREC_MIXED  1   /* FP32 sweeps/SpMV, FP64 dots, residual, refinement, positions */
+#define BS_PREC_MIXED  1   /* pair values stored in FP32 (each the FP32 rounding of the
+                              FP64 value); neighbour sweeps on the FP32 pipe, double-float
+                              where terms cancel; FP32 multigrid cycle, double-float FGMRES
+                              basis; FP64 Krylov loop, residuals and positions */
 
 /* PPE stopping rules */
 #define BS_STOP_RELRES     0  /* ||b - A x||_2 / ||b||_2 <= ppe_tol                    */
