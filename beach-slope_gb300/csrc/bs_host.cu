@@ -361,6 +361,8 @@ void fill_par(ScenePar& P, const bs_params& p, int kmax) {
     P.kq_rho_l = (float)(kr - (double)P.kq_rho_h);
     P.kq_k3_h = (float)k3;
     P.kq_k3_l = (float)(k3 - (double)P.kq_k3_h);
+    P.kq_lam_h = (float)P.lam;
+    P.kq_lam_l = (float)(P.lam - (double)P.kq_lam_h);
     P.kq_pad = 0.0f;
     P.rho = p.rho; P.rhomin = p.rhomin; P.rhomax = p.rhomax; P.rel_den = p.rel_den; P.g = p.g;
     P.mu = p.mu; P.tschmidt = p.tschmidt; P.por = p.por; P.lamk = p.lamk; P.d50 = p.d50;

@@ -54,8 +54,8 @@ struct ScenePar {                 // per-scene constants
     int nblk, blk0, max_outer, mg_lev;   // mg_lev: this scene's coarsest multigrid level
     int grp0, pad_grp;                    // first group of 32 row blocks (two-level reductions)
     // the kernel gradient on the FP32 pipe as F = kq_s g(q), q = r/h:
-    // kq_s = fl32(cn1/h^2), (hi, lo) pairs of cn2/cn1 and 3 (1 + cn2/cn1)
-    float kq_s, kq_rho_h, kq_rho_l, kq_k3_h, kq_k3_l, kq_pad;
+    // kq_s = fl32(cn1/h^2), (hi, lo) pairs of cn2/cn1, 3 (1 + cn2/cn1) and lam
+    float kq_s, kq_rho_h, kq_rho_l, kq_k3_h, kq_k3_l, kq_lam_h, kq_lam_l, kq_pad;
 };
 
 struct SceneDyn {                 // per-scene dynamic state (device)
@@ -350,9 +350,9 @@ __device__ __forceinline__ float2 f2_diff(float bh, float bl, float ah, float al
 // step from the FP32 reciprocal square root y (r = r0 + (s - r0^2) y / 2,
 // r0 = fl(s y); the residual s - r0^2 exact by Sterbenz and FMA), and 1/r
 // by one Newton step y (1 + (1 - r y)).  rh = fl32(r) and ir = fl32(1/r)
-// up to ties (relative error of r before rounding ~2^-44); sh = fl32(s).
+// up to ties (relative error of r before rounding ~2^-44); s = sh + sl.
 struct PairR {
-    float rh, rl, ir, sh;
+    float rh, rl, ir, sh, sl;
 };
 __device__ __forceinline__ PairR pair_r(float2 dx, float2 dy) {
     const float p1 = __fmul_rn(dx.x, dx.x);
@@ -372,6 +372,7 @@ __device__ __forceinline__ PairR pair_r(float2 dx, float2 dy) {
     o.rl = r.y;
     o.ir = __fmaf_rn(y, t, y);
     o.sh = s.x;
+    o.sl = s.y;
     return o;
 }
 // r < c for a double-float r and a double c given as (ch, cl)
@@ -401,15 +402,11 @@ __device__ __forceinline__ float2 f2_rcp(float2 a) {
     const float e = __fmaf_rn(-a.y, y, __fmaf_rn(-a.x, y, 1.0f));
     return f2_fast_two_sum(y, __fmul_rn(y, e));
 }
-// fl32(a b) of two double-float values (one rounding up to ties)
-__device__ __forceinline__ float f2_prod_rn(float2 a, float2 b) {
-    return __fmaf_rn(a.x, b.x, __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
-}
-// a += k (rh + re) for a double-float accumulator a, an FP32 k and a
-// double-float (rh, re): the product's rounding error kept in the lo part
-__device__ __forceinline__ void f2_acc_prod(float2& a, float k, float rh, float re) {
-    const float th = __fmul_rn(k, rh);
-    const float te = __fmaf_rn(k, re, __fmaf_rn(k, rh, -th));
+// a += (kh + kl)(rh + re) for a double-float accumulator a and two
+// double-float factors: the product's rounding error kept in the lo part
+__device__ __forceinline__ void f2_acc_prod(float2& a, float2 k, float rh, float re) {
+    const float th = __fmul_rn(k.x, rh);
+    const float te = __fmaf_rn(k.y, rh, __fmaf_rn(k.x, re, __fmaf_rn(k.x, rh, -th)));
     const float2 t = f2_two_sum(a.x, th);
     a.x = t.x;
     a.y = __fadd_rn(a.y, __fadd_rn(t.y, te));

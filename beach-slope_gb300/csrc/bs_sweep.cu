@@ -157,9 +157,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
         if (sizeof(T) == 4) {
             // mixed: the pair quantities are stored in FP32 and computed on
             // the FP32 pipe from double-float positions: the offset x_j - x_i
-            // (f2_diff, ~1e-13 m), r and 1/r (pair_r, r to ~2^-44 before
-            // rounding); r and 1/(r^2 + lam) are the FP32 roundings of the
-            // FP64 values up to ties.  The kernel gradient is F = S g(q),
+            // (f2_diff, ~1e-13 m), r, r^2 and 1/r (pair_r, ~2^-44 before
+            // rounding) and 1/(r^2 + lam) by a double-float Newton step, each
+            // the FP32 rounding of the FP64 value up to ties.  The kernel
+            // gradient is F = S g(q),
             // q = r/h, with one FP32 scale S = cn1/h^2:
             //   q < 1: g = (9q - 12) + (cn2/cn1)(3q - 6/q)
             //   q >= 1: g = -3 (1 + cn2/cn1) (2 - q)^2 / q
@@ -173,15 +174,16 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
             // 1/h^3, cn1, cn2 each rounded).  S is the same for every
             // gradient of the scene: it cancels in the corrected gradients
             // and the Jacobi-scaled rows and elsewhere acts as one rounded
-            // constant.  The correction sums take the stored components times
-            // V (x_j - x_i) with the products' rounding errors kept
-            // (double-float accumulators): the correction matrix multiplies
-            // every pair of the row, so its errors do not average out either.
+            // constant.  The correction sums take the components before their
+            // rounding times V (x_j - x_i), all as (hi, lo) pairs, into
+            // double-float accumulators, as the FP64 form sums its unrounded
+            // values: the correction matrix multiplies every pair of the row,
+            // so its errors do not average out either.
             float2 s00 = make_float2(0.f, 0.f), s01 = s00, s10 = s00, s11 = s00;
             const float kqs = P.kq_s;
             const float2 kr = make_float2(P.kq_rho_h, P.kq_rho_l), k3 = make_float2(P.kq_k3_h, P.kq_k3_l);
             const float2 hf = f2_split(P.h), ihd = f2_split(P.inv_h);
-            const float lamf = (float)P.lam;
+            const float2 lam = make_float2(P.kq_lam_h, P.kq_lam_l);
             const float4 pi4 = D.pos4[r];
             for (int k = 0; k < n; ++k) {
                 const long e = ell(r, k, kmax);
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 const float2 dy = f2_diff(pj4.z, pj4.w, pi4.z, pi4.w);
                 const PairR pr = pair_r(dx, dy);
                 const float rad = pr.rh;
-                const float rinv = __frcp_rn(pr.sh + lamf);
+                const float rinv = f2_rcp(f2_add(make_float2(pr.sh, pr.sl), lam)).x;
                 const float2 q = f2_mul(make_float2(pr.rh, pr.rl), ihd);
                 const float2 iq = f2_rcp(q);
                 float2 g;
@@ -200,13 +202,17 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                     const float2 t2 = f2_add(f2_mulf(q, 3.0f), f2_mulf(iq, -6.0f));
                     g = f2_add(t1, f2_mul(kr, t2));
                 } else {
-                    const float2 s = f2_two_sum(2.0f, -q.x);   // exact: q in [1, 2]
+                    const float2 s = f2_two_sum(2.0f, -q.x);
                     const float2 a = f2_fast_two_sum(s.x, __fsub_rn(s.y, q.y));
                     g = f2_mul(k3, f2_mul(f2_mul(a, a), iq));
                     g = make_float2(-g.x, -g.y);
                 }
                 const float2 F = f2_mulf(g, kqs);
-                const float kx = -f2_prod_rn(F, dx), ky = -f2_prod_rn(F, dy);
+                // F (x_i - x_j) as (hi, lo); hi is the stored FP32 value
+                float2 kx2 = f2_mul(F, dx), ky2 = f2_mul(F, dy);
+                kx2 = make_float2(-kx2.x, -kx2.y);
+                ky2 = make_float2(-ky2.x, -ky2.y);
+                const float kx = kx2.x, ky = ky2.x;
                 st<T>(D.ndist, e, (T)rad);
                 st<T>(D.nrinv, e, (T)rinv);
                 st<T>(D.nkx, e, (T)kx);
@@ -217,10 +223,10 @@ __global__ void __launch_bounds__(BS_THREADS) k_search(Dev D, int do_search, int
                 const float r1e = __fmaf_rn(vj.y, dx.x, __fmaf_rn(vj.x, dx.y, __fmaf_rn(vj.x, dx.x, -r1h)));
                 const float r3h = __fmul_rn(vj.x, dy.x);
                 const float r3e = __fmaf_rn(vj.y, dy.x, __fmaf_rn(vj.x, dy.y, __fmaf_rn(vj.x, dy.x, -r3h)));
-                f2_acc_prod(s00, kx, r1h, r1e);
-                f2_acc_prod(s01, ky, r1h, r1e);
-                f2_acc_prod(s10, kx, r3h, r3e);
-                f2_acc_prod(s11, ky, r3h, r3e);
+                f2_acc_prod(s00, kx2, r1h, r1e);
+                f2_acc_prod(s01, ky2, r1h, r1e);
+                f2_acc_prod(s10, kx2, r3h, r3e);
+                f2_acc_prod(s11, ky2, r3h, r3e);
             }
             a00 = (double)s00.x + (double)s00.y;
             a01 = (double)s01.x + (double)s01.y;
