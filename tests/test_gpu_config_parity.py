@@ -91,7 +91,7 @@ def test_config2_scale_steps_vs_oracle(api, oracle):
         assert e64["vx"] <= 1e-9 and e64["vy"] <= 1e-9, e64
         assert e64["con"] <= 1e-12 and e64["nut"] <= 1e-9, e64
         assert dxm <= 1e-12, dxm
-        # the mixed form against the FP64 oracle (spec bar: p within 1e-6
+        # the mixed form against the FP64 oracle (accuracy bar: p within 1e-6
         # for one step from the same state; the second step carries the first
         # step's position differences: measured 5.8e-8, then 1.2e-6; the
         # velocities carry the FP32 pair sums of the sweeps: 3.8e-7 / 1.0e-6

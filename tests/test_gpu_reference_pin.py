@@ -54,7 +54,7 @@ def test_gpu_fp64_first_phase_matches_reference(api):
 
 def test_gpu_mixed_schedule_against_reference(api):
     """The mixed form on the same schedule: particle order as the reference's,
-    pressure within 1e-6 (the spec bar; measured 3.7e-8), velocities
+    pressure within 1e-6 (the mixed form's accuracy bar; measured 3.7e-8), velocities
     within 3e-5 (measured 9.1e-6: this scene's velocities are ~1e-5 m/s, and
     the mixed sweeps sum in FP32), salinity within 1e-9 and the masses the
     density update derives from it within 1e-12 (FP32 sub-steps; measured
