@@ -207,10 +207,8 @@ def algorithmic_bytes(ctx, kernel, precision, basis_reads=None):
             tot += nnz * (w + 4) + n * (8 + 4 + w + 8 + 4 + 8)
         elif kernel == "search_effpor":
             # own position, vol, flags, cell; list (index + dist, 1/(r2+lam), gradW x,y);
-            # coff, gradvx, flags, count; effpor reads/writes; mixed: coff's (hi, lo) pairs
+            # coff, gradvx, flags, count; effpor reads/writes
             tot += n * (16 + 8 + 2 + 4) + nnz * (4 + 4 * w) + n * (32 + 8 + 1 + 4) + n * (32 + 40)
-            if precision == "mixed":
-                tot += n * 32
     return tot
 
 

@@ -41,10 +41,6 @@ def test_algorithmic_bytes(bench):
     # the particle-level sweeps read 4-byte matrix values in the mixed form, 8 in FP64
     m, d = (bench.algorithmic_bytes(f, "mg_l0_up", p) for p in ("mixed", "fp64"))
     assert d - m == nnz * 4 + n * 4
-    # the search: four 4-byte pair values per neighbour in the mixed form, 8 in
-    # FP64; the mixed search also writes the correction matrix as (hi, lo) pairs
-    m, d = (bench.algorithmic_bytes(f, "search_effpor", p) for p in ("mixed", "fp64"))
-    assert d - m == nnz * 16 - n * 32
 
 
 def test_fp64_work(bench):
