@@ -41,6 +41,11 @@ def test_algorithmic_bytes(bench):
     # the particle-level sweeps read 4-byte matrix values in the mixed form, 8 in FP64
     m, d = (bench.algorithmic_bytes(f, "mg_l0_up", p) for p in ("mixed", "fp64"))
     assert d - m == nnz * 4 + n * 4
+    # the search stores four pair values per neighbour: 4 bytes each in the
+    # mixed form, 8 in FP64 (copies the mixed form keeps for the FP32 pipe,
+    # such as the correction matrix as (hi, lo) pairs, are not algorithmic)
+    m, d = (bench.algorithmic_bytes(f, "search_effpor", p) for p in ("mixed", "fp64"))
+    assert d - m == nnz * 16
 
 
 def test_fp64_work(bench):
