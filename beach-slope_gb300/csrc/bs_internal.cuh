@@ -411,15 +411,6 @@ __device__ __forceinline__ void f2_acc_prod(float2& a, float2 k, float rh, float
     a.x = t.x;
     a.y = __fadd_rn(a.y, __fadd_rn(t.y, te));
 }
-// fl32(2 - r * ih) for a double-float r and ih = (ihh, ihl), r ih in [1, 2]
-// (2 - p exact by Sterbenz)
-__device__ __forceinline__ float f2_two_minus_prod(float rh, float rl, float ihh, float ihl) {
-    const float p = __fmul_rn(rh, ihh);
-    float pe = __fmaf_rn(rh, ihh, -p);
-    pe = __fmaf_rn(rh, ihl, pe);
-    pe = __fmaf_rn(rl, ihh, pe);
-    return __fsub_rn(__fsub_rn(2.0f, p), pe);
-}
 
 // Radial factor F(r) of the hybrid-kernel gradient: grad_i W_ij = F(r) (r_i - r_j)
 // (kernel.f90:94-162: Wabx(p1=j, p2=i) = F * (p2%x - p1%x)).
